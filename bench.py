@@ -1,0 +1,440 @@
+#!/usr/bin/env python
+"""Benchmark of the neural-radiance-cache hot path on GB300.
+
+One step = one 1920x1080 frame of the reference schedule
+(src/rg/NRCRenderGraph.cpp:46-80): 2,073,600 fused cache queries with the
+rendering weights, then 4 chained training steps of 16,384 records each (fused
+encode + forward + relative-L2 backward + weight gradients, then Adam).
+Records are synthetic, drawn from the benchmark configuration's distributions
+and redrawn per frame (a pool of distinct frames is rotated so every frame's
+inputs are cold in L2).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line. With --gpus N > 1 (under torchrun) every rank runs an
+independent replica (the path has no data-path exchange on one box).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "queries/s + train records/s on 1 GB300 (fused vs plain fp16); p50/p99 frame ms"
+Q = 1920 * 1080
+R = 16384
+B = 4
+FLOP_PER_QUERY = 2 * (5 * 64 * 64 + 3 * 64)  # 41,344
+FLOP_PER_TRAIN_RECORD = 115840  # forward + dA + dW MACs x 2
+EVAL_BYTES = 56  # nrc_input
+TRAIN_BYTES = 80  # nrc_train_record
+OUT_BYTES = 12
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=1000)
+    p.add_argument("--warmup", type=int, default=20)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--eval-frames", type=int, default=4, help="distinct frames of eval records rotated")
+    p.add_argument("--train-frames", type=int, default=8, help="distinct frames of train records rotated")
+    p.add_argument("--e2e-steps", type=int, default=100)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-plain", action="store_true")
+    return p.parse_args()
+
+
+# ------------------------------------------------------------------ helpers --
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return d, "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def load_traffic():
+    """Per-launch DRAM bytes of the query kernel at the bench's workload, from
+    the committed ncu summary (profiles/infer_kernel_1080p.md), or None."""
+    path = os.path.join(ROOT, "profiles", "infer_kernel_1080p.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].strip())
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.out = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.out,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.out.close()
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(args):
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        backend = "nccl" if (args.impl == "ours" and torch.cuda.is_available()) else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    elif torch.cuda.is_available() and args.impl == "ours":
+        torch.cuda.set_device(0)
+    return world, rank, local
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+# ------------------------------------------------------------ CPU baseline --
+def cpu_frame_sample(steps: int, warmup: int, fraction: int = 512):
+    """Times the CPU oracle (restatement of the reference's shader math) on all
+    host cores: each step is 1/fraction of a 1080p frame (queries encoded and
+    evaluated, train records encoded, back-propagated and one optimizer step).
+    Returns (queries/s at full-frame composition, threads, sample text)."""
+    import numpy as np
+
+    from oracle import oracle as O
+    from vknrc_gb300 import synthetic as S
+
+    O.build()
+    threads = os.cpu_count() or 1
+    q = Q // fraction
+    r = (B * R) // fraction
+    rng = S.rng_for(77)
+    rec = S.inputs(rng, q)
+    tr = S.train_records(rng, r, sigma=1.5)
+    w = (rng.standard_normal(20672) * np.sqrt(2 / 64)).astype(np.float16).view(np.uint16)
+    hp = O.HParams(1e-3, 0.9, 0.99, 1e-8, 0.99, 1.0, R)
+    opt = O.Optimizer(w.view(np.float16).astype(np.float32), hp)
+
+    def step():
+        enc = O.encode(rec)
+        out = O.forward_f32(w, enc, nthreads=threads)
+        np.maximum(out, 0, out=out)
+        tenc = O.encode(tr[:, 6:])
+        g, _, _ = O.train_grad(w, tenc, tr[:, :3], mode=0, nthreads=threads)
+        n = opt.prepare(r)
+        opt.adam(g.astype(np.float32), n)
+
+    for _ in range(warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step()
+    dt = (time.perf_counter() - t0) / steps
+    frame_s = dt * fraction
+    sample = (f"{steps} steps of 1/{fraction} of a 1080p frame ({q} queries + {r} train records, "
+              f"one optimizer step) on {threads} threads; scaled to full frames")
+    return Q / frame_s, threads, sample, frame_s
+
+
+def reference_arm(args, world, rank):
+    if rank != 0:
+        return
+    steps = max(1, args.steps)
+    warm = max(0, args.warmup)
+    # bounded sample so that the whole run ends within minutes
+    budget = 60.0
+    qps, threads, sample, frame_s = cpu_frame_sample(1, 1)
+    per_step = frame_s / 512
+    steps_run = max(1, min(steps, int(budget / max(per_step, 1e-6))))
+    qps, threads, sample, frame_s = cpu_frame_sample(steps_run, min(warm, 3))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": qps, "unit": "queries/s", "n_gpus": 1, "steps": steps_run,
+        "warmup": min(warm, 3), "ms_per_step": frame_s * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 math, fp16 activations (CPU restatement)", "data": "synthetic",
+        "config": {"workload": "1080p frame: 2,073,600 queries + 4 x 16,384 train records"},
+        "train_records_per_s": B * R / frame_s,
+        "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ GPU arm --
+def make_pools(args, rank):
+    import numpy as np
+    import torch
+
+    from vknrc_gb300 import synthetic as S
+
+    evals, trains = [], []
+    for f in range(args.eval_frames):
+        evals.append(torch.from_numpy(S.inputs(S.rng_for(1000 + rank, f, 0), Q)).cuda())
+    for f in range(args.train_frames):
+        trains.append([torch.from_numpy(S.train_records(S.rng_for(2000 + rank, f, b), R, target="field", sigma=1.0))
+                       .cuda() for b in range(B)])
+    return evals, trains
+
+
+def plain_fp16_infer(c, evals, steps=20):
+    """Unfused baseline on the same GPU: nrc_encode to 64 fp16 features, then six
+    cuBLAS fp16 GEMMs (torch.matmul) with ReLU in between, layer by layer."""
+    import numpy as np
+    import torch
+
+    w = torch.from_numpy(c.get_weights(0).view(np.float16).astype(np.float16)).cuda()
+    Ws = [w[l * 4096:(l + 1) * 4096].view(64, 64).t().contiguous() for l in range(5)]
+    W5 = w[5 * 4096:5 * 4096 + 192].view(3, 64).t().contiguous()
+    enc = torch.empty((Q, 64), dtype=torch.float16, device="cuda")
+    cnt = torch.tensor([Q], dtype=torch.int32, device="cuda")
+
+    def run(x_in):
+        c.encode(x_in, cnt, enc)
+        a = enc
+        for l in range(5):
+            a = torch.relu(a @ Ws[l])
+        return torch.clamp_min((a @ W5).float(), 0)
+
+    for k in range(3):
+        run(evals[k % len(evals)])
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    for k in range(steps):
+        run(evals[k % len(evals)])
+    e.record()
+    torch.cuda.synchronize()
+    return Q * steps / (s.elapsed_time(e) / 1e3)
+
+
+def ours_arm(args, world, rank, local):
+    import numpy as np
+    import torch
+
+    from vknrc_gb300 import Cache
+
+    stream = torch.cuda.current_stream()
+    evals, trains = make_pools(args, rank)
+    cache = Cache(seed=1234 + rank, learning_rate=1e-3, beta1=0.9, beta2=0.99, epsilon=1e-8)
+    out = torch.empty((Q, 3), dtype=torch.float32, device="cuda")
+    eval_cnt = torch.tensor([Q], dtype=torch.int32, device="cuda")
+    train_cnt = [torch.tensor([R], dtype=torch.int32, device="cuda") for _ in range(B)]
+
+    def frame(k, ev=None):
+        cache.infer(evals[k % len(evals)], eval_cnt, out)
+        tb = trains[k % len(trains)]
+        for b in range(B):
+            cache.train(tb[b], train_cnt[b], write_use=(b == B - 1))
+
+    for k in range(args.warmup):
+        frame(k)
+    torch.cuda.synchronize()
+    barrier(world)
+    torch.cuda.synchronize()
+
+    K = args.steps
+    ev_frame = [torch.cuda.Event(enable_timing=True) for _ in range(K + 1)]
+    ev_inf = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.25)
+    t_host0 = time.perf_counter()
+    ev_frame[0].record(stream)
+    for k in range(K):
+        cache.infer(evals[k % len(evals)], eval_cnt, out)
+        ev_inf[k].record(stream)
+        tb = trains[k % len(trains)]
+        for b in range(B):
+            cache.train(tb[b], train_cnt[b], write_use=(b == B - 1))
+        ev_frame[k + 1].record(stream)
+    torch.cuda.synchronize()
+    t_host = time.perf_counter() - t_host0
+    clocks = sampler.stop()
+    barrier(world)
+    frame_ms = [ev_frame[k].elapsed_time(ev_frame[k + 1]) for k in range(K)]
+    infer_ms = [ev_frame[k].elapsed_time(ev_inf[k]) for k in range(K)]
+    total_s = ev_frame[0].elapsed_time(ev_frame[K]) / 1e3
+    total_s = max_over_ranks(total_s, world)
+    err = cache.error()
+    if err != 0:
+        raise RuntimeError(f"device error status {err} during the benchmark")
+
+    # end to end through the C ABI with host buffers: H2D of each frame's records
+    # from pinned memory, the frame, D2H of the query results
+    E = max(1, min(args.e2e_steps, K))
+    h_eval = [evals[f].cpu().pin_memory() for f in range(min(2, len(evals)))]
+    h_train = [[t.cpu().pin_memory() for t in trains[f]] for f in range(min(2, len(trains)))]
+    d_eval = torch.empty_like(evals[0])
+    d_train = [torch.empty_like(trains[0][0]) for _ in range(B)]
+    h_out = torch.empty((Q, 3), dtype=torch.float32).pin_memory()
+    h2d = Q * EVAL_BYTES + B * R * TRAIN_BYTES
+    d2h = Q * OUT_BYTES
+
+    def e2e_frame(k):
+        d_eval.copy_(h_eval[k % len(h_eval)], non_blocking=True)
+        for b in range(B):
+            d_train[b].copy_(h_train[k % len(h_train)][b], non_blocking=True)
+        cache.infer(d_eval, eval_cnt, out)
+        for b in range(B):
+            cache.train(d_train[b], train_cnt[b], write_use=(b == B - 1))
+        h_out.copy_(out, non_blocking=True)
+
+    for k in range(3):
+        e2e_frame(k)
+    torch.cuda.synchronize()
+    barrier(world)
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record(stream)
+    for k in range(E):
+        e2e_frame(k)
+    e.record(stream)
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(s.elapsed_time(e) / 1e3, world)
+
+    plain = None
+    if not args.no_plain:
+        plain = plain_fp16_infer(cache, evals)
+
+    peaks, peak_kind = load_peaks()
+    infer_s = statistics.mean(infer_ms) / 1e3
+    achieved = FLOP_PER_QUERY * Q / infer_s / 1e12
+    peak = float(peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops", 1700.0)))
+    traffic = load_traffic()
+    result = {
+        "metric": METRIC,
+        "value": world * Q * K / total_s,
+        "unit": "queries/s",
+        "n_gpus": world,
+        "steps": K,
+        "warmup": args.warmup,
+        "ms_per_step": total_s * 1e3 / K,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "fp16 (fp32 accumulate)",
+        "data": "synthetic",
+        "config": {
+            "workload": "1080p frame: 2,073,600 queries + 4 x 16,384 train records (fused infer + 4 Adam steps)",
+            "records": "seeded synthetic; 4 distinct eval frames (464 MB) and 8 distinct train frames rotated",
+            "l2": "inputs larger than L2: each frame's 116 MB of records is cold (4-frame rotation)",
+            "hyper": "lr 1e-3, beta 0.9/0.99, eps 1e-8",
+            "parallelism": f"replicas x{world}",
+        },
+        "train_records_per_s": world * B * R * K / total_s,
+        "frame_ms": {"p50": statistics.median(frame_ms), "p99": float(np.quantile(frame_ms, 0.99)),
+                     "mean": statistics.mean(frame_ms)},
+        "infer_ms": {"mean": statistics.mean(infer_ms), "p50": statistics.median(infer_ms)},
+        "gpu_launches": K * (1 + 2 * B),
+        "host_s": t_host,
+        "roofline": {
+            "bound": "tensor", "kernel": "infer_kernel<records> (nrc_infer)",
+            "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+            "peak_source": f"bf16_tflops_sustained ({peak_kind})",
+            "traffic": traffic,
+            "algorithmic_flop_per_launch": FLOP_PER_QUERY * Q,
+            "algorithmic_bytes_per_launch": Q * (EVAL_BYTES + OUT_BYTES),
+        },
+        "e2e": {"value": world * Q * E / e2e_s, "unit": "queries/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "steps": E},
+        "clocks": clocks,
+    }
+    if plain is not None:
+        result["plain_fp16"] = {"queries_per_s": plain, "what": "nrc_encode + 6 torch fp16 GEMMs (cuBLAS), infer only",
+                                "fused_infer_queries_per_s": Q / infer_s}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        qps, threads, sample, _ = cpu_frame_sample(40, 2)
+        result["cpu_baseline"] = {"value": qps, "unit": "queries/s", "cores": threads, "kind": "port",
+                                  "sample": sample}
+    cache.close()
+    return result
+
+
+def main():
+    args = parse_args()
+    world, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        reference_arm(args, world, rank)
+    else:
+        res = ours_arm(args, world, rank, local)
+        if rank == 0:
+            print(json.dumps(res), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

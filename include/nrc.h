@@ -1,0 +1,206 @@
+/*
+ * nrc.h — C ABI of the GB300 neural-radiance-cache hot path (libnrc.so).
+ *
+ * Drop-in replacement for the compute side of the reference renderer's cache
+ * passes: record encoding, the fused 64-wide MLP query, the fused relative-L2
+ * gradient pass and the Adam update. Every entry point below names the
+ * reference interface it replaces (paths relative to the reference project).
+ *
+ * Conventions
+ *  - Plain device pointers and sizes; no framework types. `stream` is a
+ *    cudaStream_t passed as void* (NULL = legacy default stream).
+ *  - Counts live in device memory (`d_count`), as the reference's count buffers
+ *    do, so no call needs a host synchronisation. `capacity` is the host-side
+ *    bound on the count (the number of records the buffer holds); the device
+ *    count is clamped to it, so a bad count can never read past the buffer.
+ *  - All compute calls are stream-ordered and asynchronous and return an
+ *    nrc_status. Argument errors are reported at the call; device-side errors
+ *    (a bounded wait that ran out) are latched in the context and read with
+ *    nrc_get_error().
+ *  - One context = one cache (weights + Adam state). Contexts are independent;
+ *    calls on one context must be ordered by the caller (one stream, or events).
+ *  - Device buffers must be 16-byte aligned (cudaMalloc gives 256).
+ */
+#ifndef NRC_H
+#define NRC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define NRC_API __attribute__((visibility("default")))
+#else
+#define NRC_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Network shape: 64 encoded inputs -> 5 x 64 ReLU -> 3 outputs
+ * (src/VkNRCState.hpp:23-25, shader/src/Constant.glsl:6). */
+#define NRC_WIDTH 64
+#define NRC_HIDDEN_LAYERS 5
+#define NRC_OUTPUTS 3
+#define NRC_PARAM_COUNT 20672 /* 5*64*64 + 3*64 */
+#define NRC_TRAIN_BATCH_SIZE 16384 /* shader/src/Constant.glsl:10 */
+#define NRC_TRAIN_BATCH_COUNT 4    /* shader/src/Constant.glsl:9 */
+
+/* Unpacked path-vertex input, field for field UnpackedNRCInput
+ * (shader/src/NRCRecord.glsl:40-45); scattered_dir and normal are already
+ * sphere-encoded (NRCSphEncode, NRCRecord.glsl:47-49). 56 bytes. */
+typedef struct nrc_input {
+  float position[3];
+  float scattered_dir[2];
+  float normal[2];
+  float roughness;
+  float diffuse[3];
+  float specular[3];
+} nrc_input;
+
+/* Training record: NRCTrainRecord (shader/src/NRCRecord.glsl:35-38) with its
+ * packed input replaced by the unpacked one. The training target is `bias`
+ * (shader/src/nrc_gradient.comp:35). 80 bytes. */
+typedef struct nrc_train_record {
+  float bias[3];
+  float factor[3];
+  nrc_input input;
+} nrc_train_record;
+
+/* Optimizer step state and per-parameter entry (src/VkNRCState.cpp:117-123). */
+typedef struct nrc_optimizer_state {
+  uint32_t t;
+  float beta1_t, beta2_t, alpha_t, alpha_t_1;
+} nrc_optimizer_state;
+
+typedef struct nrc_optimizer_entry {
+  float m, v, weight, ema_weight;
+} nrc_optimizer_entry;
+
+/* Hyper-parameters. nrc_default_config() fills the reference's values:
+ * lr 0.002, eps 1e-8 (shader/src/nrc_optimize.comp:10-11), beta 0.9/0.999,
+ * EMA 0.99, loss scale 1 (shader/src/Constant.glsl:8-13), batch cap 16384. */
+typedef struct nrc_config {
+  uint32_t train_batch_size; /* count cap of one nrc_train call */
+  float learning_rate;
+  float beta1, beta2;
+  float epsilon;
+  float ema_alpha;
+  float loss_scale;
+  uint32_t use_ema_weights; /* use_weights receives the EMA instead of the weights */
+  uint32_t deterministic;   /* 1: gradients reduced in a fixed order (run-to-run identical) */
+  uint32_t track_loss;      /* 1: accumulate the relative-L2 loss (check path, FP64 sum) */
+  uint64_t seed;            /* He initialisation seed */
+} nrc_config;
+
+typedef enum nrc_status {
+  NRC_OK = 0,
+  NRC_ERROR_INVALID_ARGUMENT = 1,
+  NRC_ERROR_CUDA = 2,
+  NRC_ERROR_NO_DEVICE = 3,
+  NRC_ERROR_UNSUPPORTED_DEVICE = 4, /* not an sm_103 (GB300) device */
+  NRC_ERROR_OUT_OF_MEMORY = 5,
+  NRC_ERROR_DEVICE_TIMEOUT = 6, /* a kernel's bounded wait ran out (latched) */
+  NRC_ERROR_MISALIGNED = 7
+} nrc_status;
+
+/* Which fp16 weight vector a query uses. The reference renders with
+ * use_weights (last frame's result) and trains on weights
+ * (src/rg/NRCRenderGraph.cpp:52, :58-68). */
+typedef enum nrc_weight_set { NRC_WEIGHTS_USE = 0, NRC_WEIGHTS_TRAIN = 1 } nrc_weight_set;
+
+typedef struct nrc_context nrc_context;
+
+NRC_API const char* nrc_status_string(int status);
+
+/* Fills the reference's defaults. */
+NRC_API int nrc_default_config(nrc_config* cfg);
+
+/* Creates a cache on the current CUDA device and initialises it as
+ * VkNRCState::ResetMLPBuffers does (src/VkNRCState.cpp:138-180): He-normal
+ * weights N(0, sqrt(2/64)) from std::mt19937(seed) and
+ * std::normal_distribution<float>, fp16 copies in weights and use_weights, zero
+ * moments, state {0, 1, 1, 1, 0}. Synchronous. */
+NRC_API int nrc_create(const nrc_config* cfg, nrc_context** out);
+NRC_API int nrc_destroy(nrc_context* ctx);
+
+/* Re-initialises weights and optimizer ("Re-Train", src/main.cpp:144-147). Synchronous. */
+NRC_API int nrc_reset(nrc_context* ctx, uint64_t seed);
+
+/* The He initialisation of nrc_create on the host, without a device:
+ * out_weights receives NRC_PARAM_COUNT fp32 values (src/VkNRCState.cpp:131-136). */
+NRC_API int nrc_he_init_host(uint64_t seed, float* out_weights);
+
+/* Input encoding alone: NRCInputEncode (shader/src/NRCRecord.glsl:78-95) of
+ * min(*d_count, capacity) records into 64 fp16 features each (d_encoded,
+ * n x 64 halves, feature order of the reference). */
+NRC_API int nrc_encode(nrc_context* ctx, const nrc_input* d_inputs, const uint32_t* d_count, uint32_t capacity,
+               uint16_t* d_encoded, void* stream);
+
+/* Sphere encoding of unit vectors (NRCSphEncode, NRCRecord.glsl:47-49):
+ * d_dirs n x 3 floats -> d_out n x 2 floats. */
+NRC_API int nrc_sph_encode(const float* d_dirs, const uint32_t* d_count, uint32_t capacity, float* d_out, void* stream);
+
+/* Cache query: encode + 6-layer fused MLP + clamp to >= 0, one rgb (3 floats)
+ * per input. Replaces the compute of NNDispatch<NNInference>
+ * (src/rg/NNDispatch.hpp:51-54, src/rg/NNInference.cpp:67-71,
+ * shader/src/nrc_inference.comp:30-48). */
+NRC_API int nrc_infer(nrc_context* ctx, const nrc_input* d_inputs, const uint32_t* d_count, uint32_t capacity,
+              float* d_out_rgb, int weight_set, void* stream);
+
+/* The same query from pre-encoded inputs (n x 64 fp16), as the reference's
+ * test kernel test/evaluate_NV.comp takes them. Output unclamped, as there. */
+NRC_API int nrc_infer_encoded(nrc_context* ctx, const uint16_t* d_encoded, const uint32_t* d_count, uint32_t capacity,
+                      float* d_out_rgb, int weight_set, void* stream);
+
+/* One training step on min(*d_count, train_batch_size, capacity) records:
+ * nrc_train_prepare.comp (count clamp, written back to *d_count; step state
+ * advanced only if n > 0) + nrc_gradient.comp (fused encode, forward,
+ * relative-L2 loss gradient, backward, weight gradients) + nrc_optimize.comp
+ * (Adam + EMA, fp16 weights; use_weights too when write_use_weights != 0).
+ * Replaces rg::NNTrain (src/rg/NNTrain.hpp:95-118, src/rg/NNTrain.cpp:29-33,
+ * 83-87, 124-133). */
+NRC_API int nrc_train(nrc_context* ctx, const nrc_train_record* d_records, uint32_t* d_count, uint32_t capacity,
+              int write_use_weights, void* stream);
+
+/* Weight-gradient pass alone (no optimizer step): d_grad receives the
+ * NRC_PARAM_COUNT fp32 gradient sums over min(*d_count, capacity) records
+ * (the reference's gradients buffer, src/rg/NNTrain.hpp:96-98), computed with
+ * the training weights. */
+NRC_API int nrc_gradient(nrc_context* ctx, const nrc_train_record* d_records, const uint32_t* d_count, uint32_t capacity,
+                 float* d_grad, void* stream);
+
+/* One frame of the reference schedule (src/rg/NRCRenderGraph.cpp:46-80):
+ * query all eval inputs with use_weights, then NRC_TRAIN_BATCH_COUNT chained
+ * training steps, the last one writing use_weights. */
+NRC_API int nrc_frame(nrc_context* ctx, const nrc_input* d_eval_inputs, const uint32_t* d_eval_count, uint32_t eval_capacity,
+              float* d_out_rgb, const nrc_train_record* const* d_train_records, uint32_t* const* d_train_counts,
+              uint32_t train_capacity, void* stream);
+
+/* Host copies of the parameter state (synchronous). `which` selects
+ * NRC_WEIGHTS_USE or NRC_WEIGHTS_TRAIN for the fp16 vectors. */
+NRC_API int nrc_get_weights(nrc_context* ctx, int which, uint16_t* host_w16);
+/* Sets both fp16 vectors and the fp32 master/EMA copies from host fp16
+ * weights; moments and step state are left as they are. */
+NRC_API int nrc_set_weights(nrc_context* ctx, const uint16_t* host_w16);
+NRC_API int nrc_get_optimizer(nrc_context* ctx, nrc_optimizer_state* host_state, nrc_optimizer_entry* host_entries);
+NRC_API int nrc_set_optimizer(nrc_context* ctx, const nrc_optimizer_state* host_state,
+                      const nrc_optimizer_entry* host_entries);
+
+/* Check path (config track_loss): sum of the per-record relative-L2 loss and
+ * the number of records since the last call; resets both. Synchronous. */
+NRC_API int nrc_get_loss(nrc_context* ctx, double* loss_sum, uint64_t* records);
+
+/* Reads and clears the context's latched device error word; returns
+ * NRC_ERROR_DEVICE_TIMEOUT if a kernel reported a timed-out wait. Synchronous. */
+NRC_API int nrc_get_error(nrc_context* ctx);
+
+/* Device pointers of the context's parameter buffers, for callers that bind
+ * them directly (e.g. through external-memory interop). Any may be NULL. */
+NRC_API int nrc_get_device_buffers(nrc_context* ctx, uint16_t** weights, uint16_t** use_weights,
+                           nrc_optimizer_entry** entries, nrc_optimizer_state** state);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NRC_H */

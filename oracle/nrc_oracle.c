@@ -1,0 +1,432 @@
+/*
+ * CPU oracle for the neural-radiance-cache hot path — TEST INFRASTRUCTURE ONLY.
+ * See nrc_oracle.h for what is pinned against the reference and how.
+ *
+ * Build: oracle/build_oracle.sh (gcc -O2 -ffp-contract=off). Contraction is off so
+ * that every fused multiply-add below is an explicit fmaf() and the op sequence is
+ * the same on x86 and aarch64.
+ */
+#include "nrc_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* ------------------------------------------------------------ fp16 -- */
+uint16_t oracle_f32_to_f16(float x) {
+  _Float16 h = (_Float16)x; /* IEEE round-to-nearest-even, as packHalf2x16 on the GPU */
+  uint16_t b;
+  memcpy(&b, &h, 2);
+  return b;
+}
+
+float oracle_f16_to_f32(uint16_t b) {
+  _Float16 h;
+  memcpy(&h, &b, 2);
+  return (float)h;
+}
+
+/* ------------------------------------------------------------- exp -- */
+/* e^x by Cody & Waite argument reduction (x = k ln2 + r, ln2 split into a
+ * 16-bit-exact high part and a low correction) and the degree-7 Taylor
+ * polynomial of e^r on |r| <= ln2/2 (truncation error < 6e-9 relative), then an
+ * exact scale by 2^k. The GPU kernels use the same sequence, so the encoded
+ * roughness feature is identical on both. GLSL's exp() is only specified to
+ * 3 + 2|x| ulp, which this meets. */
+float oracle_expf(float x) {
+  x = fminf(fmaxf(x, -87.0f), 88.0f); /* NaN maps to -87, as on the GPU */
+  const float k = rintf(x * 1.44269504f);
+  float r = fmaf(k, -0.693145751953125f, x);
+  r = fmaf(k, -1.42860677e-06f, r);
+  float p = 1.98412698e-04f;       /* 1/7! */
+  p = fmaf(p, r, 1.38888889e-03f); /* 1/6! */
+  p = fmaf(p, r, 8.33333333e-03f); /* 1/5! */
+  p = fmaf(p, r, 4.16666667e-02f); /* 1/4! */
+  p = fmaf(p, r, 1.66666667e-01f); /* 1/3! */
+  p = fmaf(p, r, 0.5f);
+  p = fmaf(p, r, 1.0f);
+  p = fmaf(p, r, 1.0f);
+  const int32_t ki = (int32_t)k;
+  const uint32_t sbits = (uint32_t)(ki + 127) << 23;
+  float s;
+  memcpy(&s, &sbits, 4);
+  return p * s;
+}
+
+/* ---------------------------------------------------------- encode -- */
+/* NRCSphEncode, NRCRecord.glsl:47-49 (M_PI in single precision as GLSL has it). */
+void oracle_sph_encode(const float* dirs, int64_t n, float* out) {
+  const float pi = 3.14159265358979323846f;
+  for (int64_t i = 0; i < n; ++i) {
+    const float x = dirs[3 * i], y = dirs[3 * i + 1], z = dirs[3 * i + 2];
+    const float zc = z < -1.0f ? -1.0f : (z > 1.0f ? 1.0f : z);
+    out[2 * i] = (x == 0.0f && y == 0.0f) ? 0.5f : 0.5f + atan2f(y, x) / (2.0f * pi);
+    out[2 * i + 1] = acosf(zc) / pi;
+  }
+}
+
+/* _nrc_tri, NRCRecord.glsl:65-68: 2|mod(x - 0.5, 2) - 1| - 1 with GLSL's
+ * mod(a, b) = a - b floor(a / b). mod is exact here; m - 1 and the final -1 round. */
+static inline float tri(float x) {
+  const float y = x - 0.5f;
+  const float f = floorf(y * 0.5f);
+  const float m = fmaf(-2.0f, f, y);
+  const float t = m - 1.0f;
+  return fmaf(2.0f, fabsf(t), -1.0f);
+}
+
+/* _quartic_cdf at radius 1/4, NRCRecord.glsl:51-56:
+ * clamp(15/16 u (1 - 2/3 u^2 + 1/5 u^4) + 1/2, 0, 1), u = 4 (edge - x),
+ * evaluated in Horner form with fused multiply-adds. */
+static inline float qcdf(float edge4, float x) {
+  const float u = fmaf(x, -4.0f, edge4);
+  const float u2 = u * u;
+  const float s = fmaf(fmaf(u2, 0.2f, -0.6666667f), u2, 1.0f);
+  const float c = fmaf(0.9375f * u, s, 0.5f);
+  return fminf(fmaxf(c, 0.0f), 1.0f);
+}
+
+/* NRCOneBlob4Encode, NRCRecord.glsl:58-63: bins [0,.25),[.25,.5),[.5,.75),[.75,1]. */
+static inline void oneblob4(float x, float* o) {
+  const float f0 = qcdf(0.0f, x), f1 = qcdf(1.0f, x), f2 = qcdf(2.0f, x), f3 = qcdf(3.0f, x),
+              f4 = qcdf(4.0f, x);
+  o[0] = f1 - f0;
+  o[1] = f2 - f1;
+  o[2] = f3 - f2;
+  o[3] = f4 - f3;
+}
+
+/* NRCInputEncode, NRCRecord.glsl:78-95. Feature order:
+ *   [0,12) pos.x freq 2^0..2^11, [12,24) pos.y, [24,36) pos.z,
+ *   [36,40) ob(dir.u), [40,44) ob(dir.v), [44,48) ob(normal.u), [48,52) ob(normal.v),
+ *   [52,56) ob(1 - e^-roughness), [56,59) diffuse, [59,62) specular, 62, 63 = 1. */
+void oracle_encode(const float* records, int64_t n, uint16_t* enc) {
+  for (int64_t i = 0; i < n; ++i) {
+    const float* r = records + ORACLE_IN_FLOATS * i;
+    float f[64];
+    for (int c = 0; c < 3; ++c) {
+      float scale = 1.0f;
+      for (int k = 0; k < 12; ++k, scale *= 2.0f) f[12 * c + k] = tri(r[c] * scale);
+    }
+    oneblob4(r[3], f + 36);
+    oneblob4(r[4], f + 40);
+    oneblob4(r[5], f + 44);
+    oneblob4(r[6], f + 48);
+    oneblob4(1.0f - oracle_expf(-r[7]), f + 52);
+    for (int c = 0; c < 6; ++c) f[56 + c] = r[8 + c];
+    f[62] = 1.0f;
+    f[63] = 1.0f;
+    for (int c = 0; c < 64; ++c) enc[64 * i + c] = oracle_f32_to_f16(f[c]);
+  }
+}
+
+/* ----------------------------------------------------------- threads -- */
+typedef void (*range_fn)(void* ctx, int64_t begin, int64_t end, int tid);
+typedef struct {
+  range_fn fn;
+  void* ctx;
+  int64_t begin, end;
+  int tid;
+} range_job;
+
+static void* range_trampoline(void* p) {
+  range_job* j = (range_job*)p;
+  j->fn(j->ctx, j->begin, j->end, j->tid);
+  return NULL;
+}
+
+static void parallel_for(int64_t n, int nthreads, range_fn fn, void* ctx) {
+  if (nthreads <= 1 || n < 2) {
+    fn(ctx, 0, n, 0);
+    return;
+  }
+  if (nthreads > 256) nthreads = 256;
+  pthread_t th[256];
+  range_job jobs[256];
+  const int64_t chunk = (n + nthreads - 1) / nthreads;
+  int used = 0;
+  for (int t = 0; t < nthreads; ++t) {
+    const int64_t b = t * chunk, e = b + chunk < n ? b + chunk : n;
+    if (b >= e) break;
+    jobs[t] = (range_job){fn, ctx, b, e, t};
+    pthread_create(&th[t], NULL, range_trampoline, &jobs[t]);
+    ++used;
+  }
+  for (int t = 0; t < used; ++t) pthread_join(th[t], NULL);
+}
+
+/* ---------------------------------------------------------- forward -- */
+/* Weight layer l as float, transposed to wt[in][out] so that the inner loop runs
+ * over outputs with each output summed in input order 0..63. */
+typedef struct {
+  float wt[5][64][64];
+  float w5t[64][3];
+  double wtd[5][64][64];
+  double w5td[64][3];
+} wcache;
+
+static void load_weights(const uint16_t* w, wcache* c) {
+  for (int l = 0; l < 5; ++l)
+    for (int o = 0; o < 64; ++o)
+      for (int i = 0; i < 64; ++i) {
+        const float v = oracle_f16_to_f32(w[l * 4096 + o * 64 + i]);
+        c->wt[l][i][o] = v;
+        c->wtd[l][i][o] = v;
+      }
+  for (int o = 0; o < 3; ++o)
+    for (int i = 0; i < 64; ++i) {
+      const float v = oracle_f16_to_f32(w[5 * 4096 + o * 64 + i]);
+      c->w5t[i][o] = v;
+      c->w5td[i][o] = v;
+    }
+}
+
+/* One record forward, fp16 activations, fp32 sums. acts[l] receives the input of
+ * layer l (l = 0..5), out the three fp32 outputs (no clamp). */
+static void fwd_f32(const wcache* c, const uint16_t* e, float acts[6][64], float out[3]) {
+  for (int i = 0; i < 64; ++i) acts[0][i] = oracle_f16_to_f32(e[i]);
+  for (int l = 0; l < 5; ++l) {
+    float z[64];
+    for (int o = 0; o < 64; ++o) z[o] = 0.0f;
+    for (int i = 0; i < 64; ++i) {
+      const float a = acts[l][i];
+      for (int o = 0; o < 64; ++o) z[o] += c->wt[l][i][o] * a;
+    }
+    for (int o = 0; o < 64; ++o) acts[l + 1][o] = oracle_f16_to_f32(oracle_f32_to_f16(z[o] > 0.0f ? z[o] : 0.0f));
+  }
+  out[0] = out[1] = out[2] = 0.0f;
+  for (int i = 0; i < 64; ++i)
+    for (int o = 0; o < 3; ++o) out[o] += c->w5t[i][o] * acts[5][i];
+}
+
+static void fwd_f64(const wcache* c, const uint16_t* e, double acts[6][64], double out[3]) {
+  for (int i = 0; i < 64; ++i) acts[0][i] = oracle_f16_to_f32(e[i]);
+  for (int l = 0; l < 5; ++l) {
+    double z[64];
+    for (int o = 0; o < 64; ++o) z[o] = 0.0;
+    for (int i = 0; i < 64; ++i) {
+      const double a = acts[l][i];
+      for (int o = 0; o < 64; ++o) z[o] += c->wtd[l][i][o] * a;
+    }
+    for (int o = 0; o < 64; ++o) acts[l + 1][o] = z[o] > 0.0 ? z[o] : 0.0;
+  }
+  out[0] = out[1] = out[2] = 0.0;
+  for (int i = 0; i < 64; ++i)
+    for (int o = 0; o < 3; ++o) out[o] += c->w5td[i][o] * acts[5][i];
+}
+
+typedef struct {
+  const wcache* c;
+  const uint16_t* enc;
+  float* out32;
+  double* out64;
+} fwd_ctx;
+
+static void fwd32_range(void* p, int64_t b, int64_t e, int tid) {
+  (void)tid;
+  fwd_ctx* x = (fwd_ctx*)p;
+  float acts[6][64];
+  for (int64_t i = b; i < e; ++i) fwd_f32(x->c, x->enc + 64 * i, acts, x->out32 + 3 * i);
+}
+
+static void fwd64_range(void* p, int64_t b, int64_t e, int tid) {
+  (void)tid;
+  fwd_ctx* x = (fwd_ctx*)p;
+  double acts[6][64];
+  for (int64_t i = b; i < e; ++i) fwd_f64(x->c, x->enc + 64 * i, acts, x->out64 + 3 * i);
+}
+
+void oracle_forward_f32(const uint16_t* w, const uint16_t* enc, int64_t n, float* out, int nthreads) {
+  wcache* c = (wcache*)malloc(sizeof(wcache));
+  load_weights(w, c);
+  fwd_ctx x = {c, enc, out, NULL};
+  parallel_for(n, nthreads, fwd32_range, &x);
+  free(c);
+}
+
+void oracle_forward_f64(const uint16_t* w, const uint16_t* enc, int64_t n, double* out, int nthreads) {
+  wcache* c = (wcache*)malloc(sizeof(wcache));
+  load_weights(w, c);
+  fwd_ctx x = {c, enc, NULL, out};
+  parallel_for(n, nthreads, fwd64_range, &x);
+  free(c);
+}
+
+/* ------------------------------------------------------------ train -- */
+/* Relative-L2 luminance loss gradient, NN_nv.glsl:178-196: dL/dp = 2 s (p - t) /
+ * (lum(max(p,0))^2 + 0.01), lum weights (0.299, 0.587, 0.114), the denominator
+ * held constant. The GPU path evaluates it in fp32 in this order. */
+static inline void loss_grad_f32(const float p[3], const float t[3], float s, float d[3]) {
+  const float px = p[0] > 0.0f ? p[0] : 0.0f, py = p[1] > 0.0f ? p[1] : 0.0f, pz = p[2] > 0.0f ? p[2] : 0.0f;
+  const float lum = fmaf(0.114f, pz, fmaf(0.587f, py, 0.299f * px));
+  const float den = fmaf(lum, lum, 0.01f);
+  const float s2 = 2.0f * s;
+  for (int c = 0; c < 3; ++c) d[c] = (s2 * (p[c] - t[c])) / den;
+}
+
+static inline double loss_value(const double p[3], const float t[3]) {
+  const double px = p[0] > 0 ? p[0] : 0, py = p[1] > 0 ? p[1] : 0, pz = p[2] > 0 ? p[2] : 0;
+  const double lum = 0.299 * px + 0.587 * py + 0.114 * pz;
+  const double den = lum * lum + 0.01;
+  double s = 0;
+  for (int c = 0; c < 3; ++c) s += (p[c] - t[c]) * (p[c] - t[c]) / den;
+  return s;
+}
+
+typedef struct {
+  const wcache* c;
+  const uint16_t* enc;
+  const float* target;
+  float loss_scale;
+  int mode;
+  double* grad[256];
+  double* gabs[256];
+  double loss[256];
+} train_ctx;
+
+static void train_range(void* p, int64_t b, int64_t e, int tid) {
+  train_ctx* x = (train_ctx*)p;
+  const wcache* c = x->c;
+  double* G = x->grad[tid];
+  double* A = x->gabs[tid];
+  double loss = 0.0;
+  for (int64_t r = b; r < e; ++r) {
+    const float* t = x->target + 3 * r;
+    /* acts[l] = input of layer l; g = gradient w.r.t. the output of the current layer */
+    double acts[6][64], g[64], gn[64];
+    double out[3];
+    if (x->mode == 0) {
+      float a32[6][64], o32[3], d[3];
+      fwd_f32(c, x->enc + 64 * r, a32, o32);
+      for (int l = 0; l < 6; ++l)
+        for (int i = 0; i < 64; ++i) acts[l][i] = a32[l][i];
+      loss_grad_f32(o32, t, x->loss_scale, d);
+      for (int k = 0; k < 3; ++k) {
+        out[k] = o32[k];
+        g[k] = oracle_f16_to_f32(oracle_f32_to_f16(d[k])); /* packed to fp16, NN_nv.glsl:185-186 */
+      }
+    } else {
+      fwd_f64(c, x->enc + 64 * r, acts, out);
+      const double px = out[0] > 0 ? out[0] : 0, py = out[1] > 0 ? out[1] : 0, pz = out[2] > 0 ? out[2] : 0;
+      const double lum = 0.299 * px + 0.587 * py + 0.114 * pz;
+      const double den = lum * lum + 0.01;
+      for (int k = 0; k < 3; ++k) g[k] = 2.0 * x->loss_scale * (out[k] - t[k]) / den;
+    }
+    loss += loss_value(out, t);
+    /* output layer: dW5[k][i] += g[k] act5[i]; dA5 = W5^T g masked by act5 > 0 */
+    for (int k = 0; k < 3; ++k)
+      for (int i = 0; i < 64; ++i) {
+        const double term = g[k] * acts[5][i];
+        G[5 * 4096 + k * 64 + i] += term;
+        if (A) A[5 * 4096 + k * 64 + i] += fabs(term);
+      }
+    for (int i = 0; i < 64; ++i) {
+      double s = 0.0;
+      for (int k = 0; k < 3; ++k) s += g[k] * c->w5td[i][k];
+      /* ReLU mask; NaN sums are zeroed as the reference's NaN-mask trick does (NN_nv.glsl:240-243) */
+      gn[i] = (acts[5][i] > 0.0 && s == s) ? s : 0.0;
+      if (x->mode == 0) gn[i] = oracle_f16_to_f32(oracle_f32_to_f16((float)gn[i]));
+    }
+    for (int l = 4; l >= 0; --l) {
+      for (int o = 0; o < 64; ++o) g[o] = gn[o];
+      for (int o = 0; o < 64; ++o)
+        for (int i = 0; i < 64; ++i) {
+          const double term = g[o] * acts[l][i];
+          G[l * 4096 + o * 64 + i] += term;
+          if (A) A[l * 4096 + o * 64 + i] += fabs(term);
+        }
+      if (l == 0) break;
+      for (int i = 0; i < 64; ++i) {
+        double s = 0.0;
+        for (int o = 0; o < 64; ++o) s += g[o] * c->wtd[l][i][o];
+        gn[i] = (acts[l][i] > 0.0 && s == s) ? s : 0.0; /* NN_nv.glsl:272-277 */
+        if (x->mode == 0) gn[i] = oracle_f16_to_f32(oracle_f32_to_f16((float)gn[i]));
+      }
+    }
+  }
+  x->loss[tid] = loss;
+}
+
+void oracle_train_grad(const uint16_t* w, const uint16_t* enc, const float* target, int64_t n,
+                       float loss_scale, int mode, double* grad, double* grad_abs, double* loss_sum,
+                       int nthreads) {
+  if (nthreads <= 0) nthreads = 1;
+  if (nthreads > 256) nthreads = 256;
+  wcache* c = (wcache*)malloc(sizeof(wcache));
+  load_weights(w, c);
+  train_ctx* x = (train_ctx*)calloc(1, sizeof(train_ctx));
+  x->c = c;
+  x->enc = enc;
+  x->target = target;
+  x->loss_scale = loss_scale;
+  x->mode = mode;
+  for (int t = 0; t < nthreads; ++t) {
+    x->grad[t] = (double*)calloc(ORACLE_P, sizeof(double));
+    x->gabs[t] = grad_abs ? (double*)calloc(ORACLE_P, sizeof(double)) : NULL;
+  }
+  parallel_for(n, nthreads, train_range, x);
+  /* fixed-order merge: the result does not depend on thread timing */
+  for (int i = 0; i < ORACLE_P; ++i) {
+    double s = 0.0, a = 0.0;
+    for (int t = 0; t < nthreads; ++t) {
+      s += x->grad[t][i];
+      if (grad_abs) a += x->gabs[t][i];
+    }
+    grad[i] = s;
+    if (grad_abs) grad_abs[i] = a;
+  }
+  if (loss_sum) {
+    double l = 0.0;
+    for (int t = 0; t < nthreads; ++t) l += x->loss[t];
+    *loss_sum = l;
+  }
+  for (int t = 0; t < nthreads; ++t) {
+    free(x->grad[t]);
+    free(x->gabs[t]);
+  }
+  free(x);
+  free(c);
+}
+
+/* -------------------------------------------------------- optimizer -- */
+uint32_t oracle_prepare(uint32_t count, const oracle_hparams* hp, oracle_opt_state* st) {
+  const uint32_t n = count < hp->batch_cap ? count : hp->batch_cap;
+  if (n > 0) {
+    st->t += 1;
+    st->beta1_t *= hp->beta1;
+    st->beta2_t *= hp->beta2;
+    st->alpha_t_1 = st->alpha_t;
+    st->alpha_t *= hp->ema_alpha;
+  }
+  return n;
+}
+
+/* nrc_optimize.comp:32-54, with its EMA formula kept as written:
+ * ema = (1 - a)/eta_t * w + a * eta_{t-1} * ema, eta_t = 1 - a^t. */
+void oracle_adam(float* entries, const float* grad, uint32_t count, const oracle_opt_state* st,
+                 const oracle_hparams* hp, uint16_t* w16, uint16_t* use16, int use_ema) {
+  if (count == 0) return;
+  const float b1 = hp->beta1, b2 = hp->beta2;
+  const float omb1 = 1.0f - b1, omb2 = 1.0f - b2;
+  const float c1 = 1.0f - st->beta1_t, c2 = 1.0f - st->beta2_t;
+  const float eta_t = 1.0f - st->alpha_t, eta_t1 = 1.0f - st->alpha_t_1;
+  const float ea = (1.0f - hp->ema_alpha) / eta_t, eb = hp->ema_alpha * eta_t1;
+  const float fcount = (float)count;
+  for (int i = 0; i < ORACLE_P; ++i) {
+    float* e = entries + 4 * i;
+    float g = grad[i] / fcount / hp->loss_scale;
+    if (isnan(g) || isinf(g)) g = 0.0f;
+    const float m = fmaf(b1, e[0], omb1 * g);
+    const float v = fmaf(b2, e[1], omb2 * (g * g));
+    const float hm = m / c1, hv = v / c2;
+    const float w = e[2] - (hp->learning_rate * hm) / (sqrtf(hv) + hp->epsilon);
+    const float ema = fmaf(ea, w, eb * e[3]);
+    e[0] = m;
+    e[1] = v;
+    e[2] = w;
+    e[3] = ema;
+    w16[i] = oracle_f32_to_f16(w);
+    if (use16) use16[i] = oracle_f32_to_f16(use_ema ? ema : w);
+  }
+}

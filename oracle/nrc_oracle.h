@@ -1,0 +1,88 @@
+/*
+ * CPU oracle for the neural-radiance-cache hot path — TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain-C restatement of the reference's shader math, used by tests/, by
+ * __graft_entry__.smoke() and by bench.py's CPU-baseline leg as the checker. The
+ * product (libnrc.so) never links, loads or calls anything in this directory.
+ *
+ * Parity status:
+ *   - Record encoding: pinned against the reference's own NRCRecord.glsl compiled
+ *     as C++ (oracle/ref/ref_glsl.cpp) through committed golden vectors.
+ *   - MLP forward: pinned against the reference's own CPU MLP (test/main.cpp
+ *     Evaluate()) through committed golden vectors.
+ *   - Gradient / Adam: restated from shader/src/NN_nv.glsl, nrc_gradient.comp and
+ *     nrc_optimize.comp. The reference's CPU Train() does not compute the shader's
+ *     gradient (wrong loss seed, indicator instead of ReLU mask), so these are
+ *     checked by a finite-difference test of the restated loss, not by reference
+ *     outputs.
+ *
+ * Conventions (reference layout, src/VkNRCState.hpp:22-25, NN_nv.glsl:20,69-82):
+ *   weights fp16[20672]: layer l<5 at l*4096, row-major W[out=64][in=64];
+ *   output layer at 5*4096, row-major W[3][64]. y = W x.
+ */
+#ifndef NRC_ORACLE_H
+#define NRC_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ORACLE_P 20672
+#define ORACLE_IN_FLOATS 14
+
+/* Scalar pieces (exported so tests can pin them individually). */
+float oracle_expf(float x);
+uint16_t oracle_f32_to_f16(float x);
+float oracle_f16_to_f32(uint16_t h);
+
+/* NRCSphEncode (NRCRecord.glsl:47-49): dirs n x 3 -> out n x 2. */
+void oracle_sph_encode(const float* dirs, int64_t n, float* out);
+
+/* NRCInputEncode (NRCRecord.glsl:51-95): records n x 14 -> enc n x 64 fp16 bits. */
+void oracle_encode(const float* records, int64_t n, uint16_t* enc);
+
+/* Forward, fp16 activations between layers, fp32 accumulation (the GPU path's
+ * arithmetic). out: n x 3 fp32, unclamped. nthreads <= 0 means 1. */
+void oracle_forward_f32(const uint16_t* w, const uint16_t* enc, int64_t n, float* out, int nthreads);
+
+/* Forward in FP64 from the same fp16 weights/inputs, no intermediate rounding. */
+void oracle_forward_f64(const uint16_t* w, const uint16_t* enc, int64_t n, double* out, int nthreads);
+
+/* Gradient of the relative-L2 luminance loss (NN_nv.glsl:178-196, nrc_gradient.comp:26-58)
+ * summed over n records, written to grad[20672] (not divided by n).
+ *   mode 0: the GPU path's arithmetic: fp16 activations, fp16 dL/dout and fp16 dA
+ *           (as the reference stores them), fp32 sums;
+ *   mode 1: FP64 throughout (no fp16 rounding of activations or gradients).
+ * target: n x 3. loss_sum (nullable): sum over records of the per-record loss
+ * sum_c (p_c - t_c)^2 / (lum(max(p,0))^2 + 0.01), in double.
+ * grad_abs (nullable): per-parameter sum of |term|, for error normalisation. */
+void oracle_train_grad(const uint16_t* w, const uint16_t* enc, const float* target, int64_t n,
+                       float loss_scale, int mode, double* grad, double* grad_abs, double* loss_sum,
+                       int nthreads);
+
+/* Optimizer state and entries (src/VkNRCState.cpp:117-123). */
+typedef struct oracle_opt_state {
+  uint32_t t;
+  float beta1_t, beta2_t, alpha_t, alpha_t_1;
+} oracle_opt_state;
+
+typedef struct oracle_hparams {
+  float learning_rate, beta1, beta2, epsilon, ema_alpha, loss_scale;
+  uint32_t batch_cap;
+} oracle_hparams;
+
+/* nrc_train_prepare.comp:16-29: clamp the count, advance the step state if n > 0.
+ * Returns the clamped count. */
+uint32_t oracle_prepare(uint32_t count, const oracle_hparams* hp, oracle_opt_state* st);
+
+/* nrc_optimize.comp:32-54 for all parameters. entries: P x {m, v, w, ema}.
+ * grad: fp32 gradient sums. w16 receives fp16 weights; use16 (nullable) receives
+ * fp16 of (use_ema ? ema : w). No-op when count == 0. */
+void oracle_adam(float* entries, const float* grad, uint32_t count, const oracle_opt_state* st,
+                 const oracle_hparams* hp, uint16_t* w16, uint16_t* use16, int use_ema);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,178 @@
+"""ctypes wrapper of the CPU oracle (oracle/_build/liboracle.so) — TEST INFRASTRUCTURE.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import this
+module, and only as the checker. The product library never uses it.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+REF_LIB_PATH = os.path.join(HERE, "_ref", "libnrcref.so")
+
+P = 20672
+
+_lib = None
+_ref = None
+
+
+def build() -> None:
+    subprocess.run(["bash", os.path.join(HERE, "build_oracle.sh")], check=True)
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        _lib = ctypes.CDLL(LIB_PATH)
+        vp, i64, i32, f32 = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_float
+        _lib.oracle_encode.argtypes = [vp, i64, vp]
+        _lib.oracle_sph_encode.argtypes = [vp, i64, vp]
+        _lib.oracle_forward_f32.argtypes = [vp, vp, i64, vp, i32]
+        _lib.oracle_forward_f64.argtypes = [vp, vp, i64, vp, i32]
+        _lib.oracle_train_grad.argtypes = [vp, vp, vp, i64, f32, i32, vp, vp, vp, i32]
+        _lib.oracle_prepare.argtypes = [ctypes.c_uint32, vp, vp]
+        _lib.oracle_prepare.restype = ctypes.c_uint32
+        _lib.oracle_adam.argtypes = [vp, vp, ctypes.c_uint32, vp, vp, vp, vp, i32]
+        _lib.oracle_expf.argtypes = [f32]
+        _lib.oracle_expf.restype = f32
+    return _lib
+
+
+def ref_lib():
+    """The reference's own CPU code (built from the reference tree), or None."""
+    global _ref
+    if _ref is None and os.path.exists(REF_LIB_PATH):
+        _ref = ctypes.CDLL(REF_LIB_PATH)
+        vp, i64 = ctypes.c_void_p, ctypes.c_int64
+        _ref.ref_encode.argtypes = [vp, i64, vp]
+        _ref.ref_sph_encode.argtypes = [vp, i64, vp]
+        _ref.ref_evaluate.argtypes = [vp, vp, i64, vp]
+        _ref.ref_train.argtypes = [vp, vp, vp, i64, vp]
+    return _ref
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _c(a, dtype):
+    return np.ascontiguousarray(a, dtype=dtype)
+
+
+def encode(records: np.ndarray) -> np.ndarray:
+    """records (n, 14) float32 -> (n, 64) uint16 fp16 bit patterns."""
+    r = _c(records, np.float32).reshape(-1, 14)
+    out = np.empty((r.shape[0], 64), np.uint16)
+    lib().oracle_encode(_p(r), r.shape[0], _p(out))
+    return out
+
+
+def sph_encode(dirs: np.ndarray) -> np.ndarray:
+    d = _c(dirs, np.float32).reshape(-1, 3)
+    out = np.empty((d.shape[0], 2), np.float32)
+    lib().oracle_sph_encode(_p(d), d.shape[0], _p(out))
+    return out
+
+
+def expf(x: float) -> float:
+    return lib().oracle_expf(x)
+
+
+def forward_f32(weights: np.ndarray, enc: np.ndarray, nthreads: int = 1) -> np.ndarray:
+    w = _c(weights, np.uint16)
+    e = _c(enc, np.uint16).reshape(-1, 64)
+    out = np.empty((e.shape[0], 3), np.float32)
+    lib().oracle_forward_f32(_p(w), _p(e), e.shape[0], _p(out), nthreads)
+    return out
+
+
+def forward_f64(weights: np.ndarray, enc: np.ndarray, nthreads: int = 1) -> np.ndarray:
+    w = _c(weights, np.uint16)
+    e = _c(enc, np.uint16).reshape(-1, 64)
+    out = np.empty((e.shape[0], 3), np.float64)
+    lib().oracle_forward_f64(_p(w), _p(e), e.shape[0], _p(out), nthreads)
+    return out
+
+
+def train_grad(weights, enc, target, loss_scale=1.0, mode=0, nthreads=1, want_abs=False):
+    """Returns (grad[P] float64 sum over records, grad_abs or None, loss_sum)."""
+    w = _c(weights, np.uint16)
+    e = _c(enc, np.uint16).reshape(-1, 64)
+    t = _c(target, np.float32).reshape(-1, 3)
+    g = np.zeros(P, np.float64)
+    a = np.zeros(P, np.float64) if want_abs else None
+    loss = ctypes.c_double(0.0)
+    lib().oracle_train_grad(_p(w), _p(e), _p(t), e.shape[0], loss_scale, mode, _p(g),
+                            _p(a) if a is not None else None, ctypes.byref(loss), nthreads)
+    return g, a, loss.value
+
+
+class OptState(ctypes.Structure):
+    _fields_ = [("t", ctypes.c_uint32), ("beta1_t", ctypes.c_float), ("beta2_t", ctypes.c_float),
+                ("alpha_t", ctypes.c_float), ("alpha_t_1", ctypes.c_float)]
+
+
+class HParams(ctypes.Structure):
+    _fields_ = [("learning_rate", ctypes.c_float), ("beta1", ctypes.c_float), ("beta2", ctypes.c_float),
+                ("epsilon", ctypes.c_float), ("ema_alpha", ctypes.c_float), ("loss_scale", ctypes.c_float),
+                ("batch_cap", ctypes.c_uint32)]
+
+
+class Optimizer:
+    """Host mirror of the reference's optimizer state (nrc_train_prepare + nrc_optimize)."""
+
+    def __init__(self, weights_f32: np.ndarray, hp: HParams):
+        self.hp = hp
+        self.state = OptState(0, 1.0, 1.0, 1.0, 0.0)
+        self.entries = np.zeros((P, 4), np.float32)
+        self.entries[:, 2] = weights_f32
+        self.entries[:, 3] = weights_f32
+
+    def prepare(self, count: int) -> int:
+        return lib().oracle_prepare(count, ctypes.byref(self.hp), ctypes.byref(self.state))
+
+    def adam(self, grad32: np.ndarray, count: int, write_use: bool = True, use_ema: bool = False):
+        g = _c(grad32, np.float32)
+        w16 = np.zeros(P, np.uint16)
+        use16 = np.zeros(P, np.uint16) if write_use else None
+        lib().oracle_adam(_p(self.entries), _p(g), count, ctypes.byref(self.state), ctypes.byref(self.hp),
+                          _p(w16), _p(use16) if use16 is not None else None, int(use_ema))
+        return w16, use16
+
+
+def ref_encode(records: np.ndarray):
+    r = ref_lib()
+    if r is None:
+        return None
+    rec = _c(records, np.float32).reshape(-1, 14)
+    out = np.empty((rec.shape[0], 64), np.uint16)
+    r.ref_encode(_p(rec), rec.shape[0], _p(out))
+    return out
+
+
+def ref_sph_encode(dirs: np.ndarray):
+    r = ref_lib()
+    if r is None:
+        return None
+    d = _c(dirs, np.float32).reshape(-1, 3)
+    out = np.empty((d.shape[0], 2), np.float32)
+    r.ref_sph_encode(_p(d), d.shape[0], _p(out))
+    return out
+
+
+def ref_evaluate(weights: np.ndarray, enc: np.ndarray):
+    r = ref_lib()
+    if r is None:
+        return None
+    w = _c(weights, np.uint16)
+    e = _c(enc, np.uint16).reshape(-1, 64)
+    out = np.empty((e.shape[0], 3), np.uint16)
+    r.ref_evaluate(_p(w), _p(e), e.shape[0], _p(out))
+    return out

@@ -1,0 +1,418 @@
+// C ABI of libnrc.so (include/nrc.h): context ownership, argument checks and
+// kernel launches. Host code only; kernels live in nrc_infer.cu, nrc_train.cu
+// and nrc_encode.cu.
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <random>
+#include <vector>
+
+#include "nrc_common.cuh"
+#include "nrc_kernels.h"
+
+struct nrc_context {
+  nrc_config cfg;
+  int device = 0;
+  int num_sms = 0;
+  void* block = nullptr;  // one device allocation, carved below
+  __half* w16 = nullptr;  // training weights (reference: weights)
+  __half* use16 = nullptr;  // rendering weights (reference: use_weights)
+  nrc_optimizer_entry* entries = nullptr;
+  nrc_optimizer_state* state = nullptr;
+  float* grad = nullptr;      // atomic gradient accumulator, zero between steps
+  float* partials = nullptr;  // deterministic mode: one gradient vector per CTA
+  uint32_t* err = nullptr;
+  double* loss_acc = nullptr;
+  unsigned long long* loss_count = nullptr;
+};
+
+namespace {
+
+using nrc::kParams;
+
+int from_cuda(cudaError_t e) {
+  if (e == cudaSuccess) return NRC_OK;
+  if (e == cudaErrorMemoryAllocation) return NRC_ERROR_OUT_OF_MEMORY;
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return NRC_ERROR_NO_DEVICE;
+  return NRC_ERROR_CUDA;
+}
+
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+size_t up256(size_t x) { return (x + 255) & ~size_t(255); }
+
+int configure_kernels() {
+  // Dynamic shared-memory limits on the current device; idempotent.
+  cudaError_t e = nrc::configure_infer_kernels();
+  if (e == cudaSuccess) e = nrc::configure_train_kernels();
+  return from_cuda(e);
+}
+
+void he_init(uint64_t seed, float* w) {
+  // src/VkNRCState.cpp:131-136: std::normal_distribution<float>{0, sqrt(2/64)}
+  // over std::mt19937, one draw per parameter in index order.
+  std::mt19937 rng(static_cast<std::mt19937::result_type>(seed));
+  std::normal_distribution<float> norm{0.0f, std::sqrt(2.0f / float(NRC_WIDTH))};
+  for (int i = 0; i < kParams; ++i) w[i] = norm(rng);
+}
+
+uint16_t f32_to_f16_bits(float x) {
+  const __half h = __float2half_rn(x);
+  uint16_t b;
+  std::memcpy(&b, &h, 2);
+  return b;
+}
+
+float f16_bits_to_f32(uint16_t b) {
+  __half h;
+  std::memcpy(&h, &b, 2);
+  return __half2float(h);
+}
+
+int upload_init(nrc_context* c, uint64_t seed) {
+  std::vector<float> w(kParams);
+  he_init(seed, w.data());
+  std::vector<uint16_t> w16(kParams);
+  std::vector<nrc_optimizer_entry> ent(kParams);
+  for (int i = 0; i < kParams; ++i) {
+    w16[i] = f32_to_f16_bits(w[i]);
+    ent[i] = nrc_optimizer_entry{0.0f, 0.0f, w[i], w[i]};
+  }
+  const nrc_optimizer_state st{0u, 1.0f, 1.0f, 1.0f, 0.0f};
+  cudaError_t e;
+  if ((e = cudaMemcpy(c->w16, w16.data(), kParams * 2, cudaMemcpyHostToDevice)) != cudaSuccess) return from_cuda(e);
+  if ((e = cudaMemcpy(c->use16, w16.data(), kParams * 2, cudaMemcpyHostToDevice)) != cudaSuccess) return from_cuda(e);
+  if ((e = cudaMemcpy(c->entries, ent.data(), kParams * sizeof(nrc_optimizer_entry), cudaMemcpyHostToDevice)) !=
+      cudaSuccess)
+    return from_cuda(e);
+  if ((e = cudaMemcpy(c->state, &st, sizeof(st), cudaMemcpyHostToDevice)) != cudaSuccess) return from_cuda(e);
+  if ((e = cudaMemset(c->grad, 0, kParams * sizeof(float))) != cudaSuccess) return from_cuda(e);
+  return NRC_OK;
+}
+
+int check_ctx(nrc_context* c) {
+  if (c == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess) return NRC_ERROR_CUDA;
+  if (dev != c->device) return NRC_ERROR_INVALID_ARGUMENT;  // calls must run on the context's device
+  return NRC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* nrc_status_string(int s) {
+  switch (s) {
+    case NRC_OK: return "ok";
+    case NRC_ERROR_INVALID_ARGUMENT: return "invalid argument";
+    case NRC_ERROR_CUDA: return "CUDA error";
+    case NRC_ERROR_NO_DEVICE: return "no CUDA device";
+    case NRC_ERROR_UNSUPPORTED_DEVICE: return "unsupported device (requires sm_103, GB300)";
+    case NRC_ERROR_OUT_OF_MEMORY: return "out of device memory";
+    case NRC_ERROR_DEVICE_TIMEOUT: return "a kernel's bounded wait timed out";
+    case NRC_ERROR_MISALIGNED: return "device buffer not 16-byte aligned";
+    default: return "unknown status";
+  }
+}
+
+int nrc_default_config(nrc_config* cfg) {
+  if (cfg == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  *cfg = nrc_config{};
+  cfg->train_batch_size = NRC_TRAIN_BATCH_SIZE;
+  cfg->learning_rate = 0.002f;  // shader/src/nrc_optimize.comp:10
+  cfg->beta1 = 0.9f;            // shader/src/Constant.glsl:11-12
+  cfg->beta2 = 0.999f;
+  cfg->epsilon = 1e-8f;         // shader/src/nrc_optimize.comp:11
+  cfg->ema_alpha = 0.99f;       // shader/src/Constant.glsl:13
+  cfg->loss_scale = 1.0f;       // shader/src/Constant.glsl:8
+  cfg->use_ema_weights = 0;     // src/VkNRCState.hpp:36
+  cfg->deterministic = 0;
+  cfg->track_loss = 0;
+  cfg->seed = 0;
+  return NRC_OK;
+}
+
+int nrc_he_init_host(uint64_t seed, float* out) {
+  if (out == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  he_init(seed, out);
+  return NRC_OK;
+}
+
+int nrc_create(const nrc_config* cfg_in, nrc_context** out) {
+  if (out == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  *out = nullptr;
+  nrc_config cfg;
+  if (cfg_in) cfg = *cfg_in;
+  else nrc_default_config(&cfg);
+  if (cfg.train_batch_size == 0 || !(cfg.learning_rate >= 0.0f) || !(cfg.loss_scale != 0.0f))
+    return NRC_ERROR_INVALID_ARGUMENT;
+  int dev = 0, count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess || count == 0) return NRC_ERROR_NO_DEVICE;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return from_cuda(e);
+  cudaDeviceProp prop;
+  if ((e = cudaGetDeviceProperties(&prop, dev)) != cudaSuccess) return from_cuda(e);
+  if (!(prop.major == 10 && prop.minor == 3)) return NRC_ERROR_UNSUPPORTED_DEVICE;
+  int s = configure_kernels();
+  if (s != NRC_OK) return s;
+
+  nrc_context* c = new (std::nothrow) nrc_context();
+  if (c == nullptr) return NRC_ERROR_OUT_OF_MEMORY;
+  c->cfg = cfg;
+  c->device = dev;
+  c->num_sms = prop.multiProcessorCount;
+  const size_t o_w16 = 0;
+  const size_t o_use = o_w16 + up256(kParams * 2);
+  const size_t o_ent = o_use + up256(kParams * 2);
+  const size_t o_st = o_ent + up256(kParams * sizeof(nrc_optimizer_entry));
+  const size_t o_grad = o_st + up256(sizeof(nrc_optimizer_state));
+  const size_t o_err = o_grad + up256(kParams * sizeof(float));
+  const size_t o_loss = o_err + 256;
+  const size_t o_part = o_loss + 256;
+  const size_t part_bytes = cfg.deterministic ? up256(size_t(c->num_sms) * kParams * sizeof(float)) : 0;
+  const size_t total = o_part + part_bytes;
+  if ((e = cudaMalloc(&c->block, total)) != cudaSuccess) {
+    delete c;
+    return from_cuda(e);
+  }
+  uint8_t* b = static_cast<uint8_t*>(c->block);
+  c->w16 = reinterpret_cast<__half*>(b + o_w16);
+  c->use16 = reinterpret_cast<__half*>(b + o_use);
+  c->entries = reinterpret_cast<nrc_optimizer_entry*>(b + o_ent);
+  c->state = reinterpret_cast<nrc_optimizer_state*>(b + o_st);
+  c->grad = reinterpret_cast<float*>(b + o_grad);
+  c->err = reinterpret_cast<uint32_t*>(b + o_err);
+  c->loss_acc = reinterpret_cast<double*>(b + o_loss);
+  c->loss_count = reinterpret_cast<unsigned long long*>(b + o_loss + 8);
+  c->partials = cfg.deterministic ? reinterpret_cast<float*>(b + o_part) : nullptr;
+  if ((e = cudaMemset(c->err, 0, 256 + 256)) != cudaSuccess) {
+    cudaFree(c->block);
+    delete c;
+    return from_cuda(e);
+  }
+  s = upload_init(c, cfg.seed);
+  if (s == NRC_OK) s = from_cuda(cudaDeviceSynchronize());
+  if (s != NRC_OK) {
+    cudaFree(c->block);
+    delete c;
+    return s;
+  }
+  *out = c;
+  return NRC_OK;
+}
+
+int nrc_destroy(nrc_context* c) {
+  if (c == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  int dev = -1;
+  cudaGetDevice(&dev);
+  if (dev != c->device) cudaSetDevice(c->device);
+  cudaDeviceSynchronize();
+  cudaFree(c->block);
+  if (dev >= 0 && dev != c->device) cudaSetDevice(dev);
+  delete c;
+  return NRC_OK;
+}
+
+int nrc_reset(nrc_context* c, uint64_t seed) {
+  int s = check_ctx(c);
+  if (s != NRC_OK) return s;
+  cudaDeviceSynchronize();
+  c->cfg.seed = seed;
+  s = upload_init(c, seed);
+  if (s == NRC_OK) s = from_cuda(cudaDeviceSynchronize());
+  return s;
+}
+
+int nrc_encode(nrc_context* c, const nrc_input* in, const uint32_t* d_count, uint32_t capacity, uint16_t* out,
+               void* stream) {
+  int s = check_ctx(c);
+  if (s != NRC_OK) return s;
+  if (capacity == 0) return NRC_OK;
+  if (in == nullptr || d_count == nullptr || out == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  if (!aligned16(in) || !aligned16(out)) return NRC_ERROR_MISALIGNED;
+  return from_cuda(nrc::launch_encode(in, d_count, capacity, out, c->num_sms, static_cast<cudaStream_t>(stream)));
+}
+
+int nrc_sph_encode(const float* dirs, const uint32_t* d_count, uint32_t capacity, float* out, void* stream) {
+  if (capacity == 0) return NRC_OK;
+  if (dirs == nullptr || d_count == nullptr || out == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  if ((reinterpret_cast<uintptr_t>(out) & 7u) != 0 || (reinterpret_cast<uintptr_t>(dirs) & 3u) != 0)
+    return NRC_ERROR_MISALIGNED;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return from_cuda(nrc::launch_sph_encode(dirs, d_count, capacity, out, sms, static_cast<cudaStream_t>(stream)));
+}
+
+static const __half* weights_of(nrc_context* c, int which) {
+  return which == NRC_WEIGHTS_TRAIN ? c->w16 : c->use16;
+}
+
+int nrc_infer(nrc_context* c, const nrc_input* in, const uint32_t* d_count, uint32_t capacity, float* out,
+              int weight_set, void* stream) {
+  int s = check_ctx(c);
+  if (s != NRC_OK) return s;
+  if (weight_set != NRC_WEIGHTS_USE && weight_set != NRC_WEIGHTS_TRAIN) return NRC_ERROR_INVALID_ARGUMENT;
+  if (capacity == 0) return NRC_OK;
+  if (in == nullptr || d_count == nullptr || out == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  if (!aligned16(in) || (reinterpret_cast<uintptr_t>(out) & 3u)) return NRC_ERROR_MISALIGNED;
+  return from_cuda(nrc::launch_infer(in, false, d_count, capacity, weights_of(c, weight_set), out, true, c->err,
+                                     c->num_sms, static_cast<cudaStream_t>(stream)));
+}
+
+int nrc_infer_encoded(nrc_context* c, const uint16_t* enc, const uint32_t* d_count, uint32_t capacity, float* out,
+                      int weight_set, void* stream) {
+  int s = check_ctx(c);
+  if (s != NRC_OK) return s;
+  if (weight_set != NRC_WEIGHTS_USE && weight_set != NRC_WEIGHTS_TRAIN) return NRC_ERROR_INVALID_ARGUMENT;
+  if (capacity == 0) return NRC_OK;
+  if (enc == nullptr || d_count == nullptr || out == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  if (!aligned16(enc) || (reinterpret_cast<uintptr_t>(out) & 3u)) return NRC_ERROR_MISALIGNED;
+  return from_cuda(nrc::launch_infer(enc, true, d_count, capacity, weights_of(c, weight_set), out, false, c->err,
+                                     c->num_sms, static_cast<cudaStream_t>(stream)));
+}
+
+static int train_step(nrc_context* c, const nrc_train_record* rec, uint32_t* d_count, uint32_t capacity,
+                      bool write_use, cudaStream_t st) {
+  const nrc_config& g = c->cfg;
+  cudaError_t e = nrc::launch_train_grad(rec, d_count, capacity, g.train_batch_size, c->w16, c->grad, c->partials,
+                                         c->state, g.loss_scale, g.beta1, g.beta2, g.ema_alpha, true,
+                                         g.track_loss ? c->loss_acc : nullptr,
+                                         g.track_loss ? c->loss_count : nullptr, c->err, c->num_sms, st);
+  if (e != cudaSuccess) return from_cuda(e);
+  const uint32_t grad_ctas = nrc::train_grid(capacity, g.train_batch_size, c->num_sms);
+  e = nrc::launch_adam(d_count, capacity, g.train_batch_size, c->grad, c->partials, grad_ctas, c->entries, c->state,
+                       c->w16, write_use ? c->use16 : nullptr, g.learning_rate, g.beta1, g.beta2, g.epsilon,
+                       g.ema_alpha, g.loss_scale, g.use_ema_weights != 0, st);
+  return from_cuda(e);
+}
+
+int nrc_train(nrc_context* c, const nrc_train_record* rec, uint32_t* d_count, uint32_t capacity,
+              int write_use_weights, void* stream) {
+  int s = check_ctx(c);
+  if (s != NRC_OK) return s;
+  if (d_count == nullptr || (capacity > 0 && rec == nullptr)) return NRC_ERROR_INVALID_ARGUMENT;
+  if (rec != nullptr && !aligned16(rec)) return NRC_ERROR_MISALIGNED;
+  return train_step(c, rec, d_count, capacity, write_use_weights != 0, static_cast<cudaStream_t>(stream));
+}
+
+int nrc_gradient(nrc_context* c, const nrc_train_record* rec, const uint32_t* d_count, uint32_t capacity,
+                 float* d_grad, void* stream) {
+  int s = check_ctx(c);
+  if (s != NRC_OK) return s;
+  if (d_count == nullptr || d_grad == nullptr || (capacity > 0 && rec == nullptr)) return NRC_ERROR_INVALID_ARGUMENT;
+  if ((rec != nullptr && !aligned16(rec)) || !aligned16(d_grad)) return NRC_ERROR_MISALIGNED;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  // the reference clears its gradient buffer before the pass (src/rg/NNTrain.hpp:96-98)
+  cudaError_t e = cudaMemsetAsync(d_grad, 0, kParams * sizeof(float), st);
+  if (e != cudaSuccess) return from_cuda(e);
+  if (capacity == 0) return NRC_OK;
+  e = nrc::launch_train_grad(rec, const_cast<uint32_t*>(d_count), capacity, 0xFFFFFFFFu, c->w16, d_grad, nullptr,
+                             c->state, c->cfg.loss_scale, c->cfg.beta1, c->cfg.beta2, c->cfg.ema_alpha, false, nullptr,
+                             nullptr, c->err, c->num_sms, st);
+  return from_cuda(e);
+}
+
+int nrc_frame(nrc_context* c, const nrc_input* eval_in, const uint32_t* d_eval_count, uint32_t eval_capacity,
+              float* out, const nrc_train_record* const* train_rec, uint32_t* const* train_counts,
+              uint32_t train_capacity, void* stream) {
+  int s = check_ctx(c);
+  if (s != NRC_OK) return s;
+  if (train_rec == nullptr || train_counts == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  s = nrc_infer(c, eval_in, d_eval_count, eval_capacity, out, NRC_WEIGHTS_USE, stream);
+  if (s != NRC_OK) return s;
+  for (int b = 0; b < NRC_TRAIN_BATCH_COUNT; ++b) {
+    s = nrc_train(c, train_rec[b], train_counts[b], train_capacity, b == NRC_TRAIN_BATCH_COUNT - 1, stream);
+    if (s != NRC_OK) return s;
+  }
+  return NRC_OK;
+}
+
+int nrc_get_weights(nrc_context* c, int which, uint16_t* host) {
+  int s = check_ctx(c);
+  if (s != NRC_OK) return s;
+  if (host == nullptr || (which != NRC_WEIGHTS_USE && which != NRC_WEIGHTS_TRAIN)) return NRC_ERROR_INVALID_ARGUMENT;
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(host, weights_of(c, which), kParams * 2, cudaMemcpyDeviceToHost);
+  return from_cuda(e);
+}
+
+int nrc_set_weights(nrc_context* c, const uint16_t* host) {
+  int s = check_ctx(c);
+  if (s != NRC_OK) return s;
+  if (host == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  std::vector<nrc_optimizer_entry> ent(kParams);
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess)
+    e = cudaMemcpy(ent.data(), c->entries, kParams * sizeof(nrc_optimizer_entry), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return from_cuda(e);
+  for (int i = 0; i < kParams; ++i) {
+    const float w = f16_bits_to_f32(host[i]);
+    ent[i].weight = w;
+    ent[i].ema_weight = w;
+  }
+  if ((e = cudaMemcpy(c->entries, ent.data(), kParams * sizeof(nrc_optimizer_entry), cudaMemcpyHostToDevice)) ==
+          cudaSuccess &&
+      (e = cudaMemcpy(c->w16, host, kParams * 2, cudaMemcpyHostToDevice)) == cudaSuccess)
+    e = cudaMemcpy(c->use16, host, kParams * 2, cudaMemcpyHostToDevice);
+  return from_cuda(e);
+}
+
+int nrc_get_optimizer(nrc_context* c, nrc_optimizer_state* st, nrc_optimizer_entry* ent) {
+  int s = check_ctx(c);
+  if (s != NRC_OK) return s;
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess && st) e = cudaMemcpy(st, c->state, sizeof(*st), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && ent) e = cudaMemcpy(ent, c->entries, kParams * sizeof(*ent), cudaMemcpyDeviceToHost);
+  return from_cuda(e);
+}
+
+int nrc_set_optimizer(nrc_context* c, const nrc_optimizer_state* st, const nrc_optimizer_entry* ent) {
+  int s = check_ctx(c);
+  if (s != NRC_OK) return s;
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess && st) e = cudaMemcpy(c->state, st, sizeof(*st), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && ent) e = cudaMemcpy(c->entries, ent, kParams * sizeof(*ent), cudaMemcpyHostToDevice);
+  return from_cuda(e);
+}
+
+int nrc_get_loss(nrc_context* c, double* loss_sum, uint64_t* records) {
+  int s = check_ctx(c);
+  if (s != NRC_OK) return s;
+  if (loss_sum == nullptr || records == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  struct {
+    double sum;
+    unsigned long long n;
+  } h;
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(&h, c->loss_acc, 16, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemset(c->loss_acc, 0, 16);
+  if (e != cudaSuccess) return from_cuda(e);
+  *loss_sum = h.sum;
+  *records = h.n;
+  return NRC_OK;
+}
+
+int nrc_get_error(nrc_context* c) {
+  int s = check_ctx(c);
+  if (s != NRC_OK) return s;
+  uint32_t h = 0;
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(&h, c->err, 4, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemset(c->err, 0, 4);
+  if (e != cudaSuccess) return from_cuda(e);
+  return h ? NRC_ERROR_DEVICE_TIMEOUT : NRC_OK;
+}
+
+int nrc_get_device_buffers(nrc_context* c, uint16_t** w, uint16_t** use, nrc_optimizer_entry** ent,
+                           nrc_optimizer_state** st) {
+  if (c == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  if (w) *w = reinterpret_cast<uint16_t*>(c->w16);
+  if (use) *use = reinterpret_cast<uint16_t*>(c->use16);
+  if (ent) *ent = c->entries;
+  if (st) *st = c->state;
+  return NRC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,130 @@
+// Shared constants and device code for the neural-radiance-cache kernels:
+// record layouts, the fp32 input encoding, and the weight staging into
+// shared memory in the tensor-core operand layout.
+#pragma once
+#include <cstdint>
+#include <cuda_fp16.h>
+
+#include "../../include/nrc.h"
+#include "ptx.cuh"
+
+namespace nrc {
+
+constexpr int kWidth = 64;            // hidden width (src/VkNRCState.hpp:23)
+constexpr int kHidden = 5;            // hidden layers (Constant.glsl:6)
+constexpr int kOut = 3;               // outputs
+constexpr int kOutPad = 16;           // output rows padded for the MMA (NN_nv.glsl:77-82)
+constexpr int kLayerElems = kWidth * kWidth;
+constexpr int kParams = kHidden * kLayerElems + kOut * kWidth;  // 20672
+constexpr int kTile = 128;            // records per MMA tile (M)
+constexpr int kInFloats = 14;         // nrc_input
+constexpr int kTrainFloats = 20;      // nrc_train_record
+constexpr uint32_t kWaitLimitNs = 2000000000u;  // bounded waits: 2 s
+
+static_assert(sizeof(nrc_input) == kInFloats * 4, "nrc_input layout");
+static_assert(sizeof(nrc_train_record) == kTrainFloats * 4, "nrc_train_record layout");
+
+// Shared-memory bytes of the staged weights: 5 layers x 64 rows x 128 B, then the
+// output layer as 16 rows (3 real, 13 zero) x 128 B.
+constexpr uint32_t kWeightSmemBytes = kHidden * 8192 + kOutPad * 128;
+
+// Copy the fp16 parameter vector (reference layout: layer l row-major [out][in] at
+// l*4096; output layer [3][64] at 5*4096) into shared memory as 128-byte-swizzled
+// K-major tiles: layer l at smem_w + l*8192, output layer at smem_w + 5*8192.
+__device__ __forceinline__ void stage_weights(uint8_t* smem_w, const __half* __restrict__ w16) {
+  constexpr int kHiddenChunks = kHidden * kWidth * 8;  // 16-byte chunks
+  constexpr int kOutChunks = kOutPad * 8;
+  const uint4* src = reinterpret_cast<const uint4*>(w16);
+  for (int idx = threadIdx.x; idx < kHiddenChunks + kOutChunks; idx += blockDim.x) {
+    if (idx < kHiddenChunks) {
+      const int l = idx >> 9, row = (idx >> 3) & 63, c = idx & 7;
+      const uint4 v = __ldg(src + idx);  // (l*4096 + row*64 + c*8) / 8 == idx
+      *reinterpret_cast<uint4*>(smem_w + l * 8192 + sw128_offset(row, c)) = v;
+    } else {
+      const int j = idx - kHiddenChunks, row = j >> 3, c = j & 7;
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (row < kOut) v = __ldg(src + (kHidden * kLayerElems) / 8 + row * 8 + c);
+      *reinterpret_cast<uint4*>(smem_w + kHidden * 8192 + sw128_offset(row, c)) = v;
+    }
+  }
+}
+
+// ------------------------------------------------------------- encoding --
+// Restatement of shader/src/NRCRecord.glsl:51-95 in an explicit fp32 op
+// sequence (no compiler contraction), identical to the CPU oracle's.
+
+// _nrc_tri (NRCRecord.glsl:65-68) of x = p * 2^k: 2|mod(x - 0.5, 2) - 1| - 1.
+// p * 2^k is exact, so the first op fuses it with the -0.5.
+__device__ __forceinline__ float enc_tri(float p, float scale) {
+  const float y = __fmaf_rn(p, scale, -0.5f);
+  const float f = floorf(__fmul_rn(y, 0.5f));
+  const float m = __fmaf_rn(-2.0f, f, y);
+  const float t = __fadd_rn(m, -1.0f);
+  return __fmaf_rn(2.0f, fabsf(t), -1.0f);
+}
+
+// _quartic_cdf at radius 1/4 (NRCRecord.glsl:51-56), u = 4 (edge - x).
+__device__ __forceinline__ float enc_qcdf(float edge4, float x) {
+  const float u = __fmaf_rn(x, -4.0f, edge4);
+  const float u2 = __fmul_rn(u, u);
+  const float s = __fmaf_rn(__fmaf_rn(u2, 0.2f, -0.6666667f), u2, 1.0f);
+  const float c = __fmaf_rn(__fmul_rn(0.9375f, u), s, 0.5f);
+  return __saturatef(c);
+}
+
+// NRCOneBlob4Encode (NRCRecord.glsl:58-63), packed to two f16x2 words.
+__device__ __forceinline__ void enc_oneblob4(float x, uint32_t& w0, uint32_t& w1) {
+  const float f0 = enc_qcdf(0.0f, x), f1 = enc_qcdf(1.0f, x), f2 = enc_qcdf(2.0f, x);
+  const float f3 = enc_qcdf(3.0f, x), f4 = enc_qcdf(4.0f, x);
+  w0 = pack_f16x2(__fsub_rn(f1, f0), __fsub_rn(f2, f1));
+  w1 = pack_f16x2(__fsub_rn(f3, f2), __fsub_rn(f4, f3));
+}
+
+// e^x by Cody-Waite reduction and a degree-7 Taylor polynomial (the same
+// sequence as the CPU oracle, so the roughness feature is bit-identical).
+__device__ __forceinline__ float enc_expf(float x) {
+  x = fminf(fmaxf(x, -87.0f), 88.0f);  // NaN becomes -87 here; inputs are finite
+  const float k = rintf(__fmul_rn(x, 1.44269504f));
+  float r = __fmaf_rn(k, -0.693145751953125f, x);
+  r = __fmaf_rn(k, -1.42860677e-06f, r);
+  float p = 1.98412698e-04f;
+  p = __fmaf_rn(p, r, 1.38888889e-03f);
+  p = __fmaf_rn(p, r, 8.33333333e-03f);
+  p = __fmaf_rn(p, r, 4.16666667e-02f);
+  p = __fmaf_rn(p, r, 1.66666667e-01f);
+  p = __fmaf_rn(p, r, 0.5f);
+  p = __fmaf_rn(p, r, 1.0f);
+  p = __fmaf_rn(p, r, 1.0f);
+  const float s = __int_as_float((static_cast<int>(k) + 127) << 23);
+  return __fmul_rn(p, s);
+}
+
+// Frequency encoding of one coordinate: 12 features -> 6 words.
+__device__ __forceinline__ void enc_freq12(float p, uint32_t* o) {
+#pragma unroll
+  for (int k = 0; k < 12; k += 2) {
+    o[k / 2] = pack_f16x2(enc_tri(p, static_cast<float>(1 << k)), enc_tri(p, static_cast<float>(1 << (k + 1))));
+  }
+}
+
+// NRCInputEncode (NRCRecord.glsl:78-95): 14 fp32 -> 64 fp16 as 32 words
+// (feature 2j in the low half of word j).
+__device__ __forceinline__ void encode_input(const float (&r)[kInFloats], uint32_t (&e)[32]) {
+  enc_freq12(r[0], e + 0);
+  enc_freq12(r[1], e + 6);
+  enc_freq12(r[2], e + 12);
+  enc_oneblob4(r[3], e[18], e[19]);
+  enc_oneblob4(r[4], e[20], e[21]);
+  enc_oneblob4(r[5], e[22], e[23]);
+  enc_oneblob4(r[6], e[24], e[25]);
+  enc_oneblob4(__fsub_rn(1.0f, enc_expf(-r[7])), e[26], e[27]);
+  e[28] = pack_f16x2(r[8], r[9]);
+  e[29] = pack_f16x2(r[10], r[11]);
+  e[30] = pack_f16x2(r[12], r[13]);
+  e[31] = pack_f16x2(1.0f, 1.0f);
+}
+
+// Device-side error word bits (read back by nrc_get_error).
+constexpr uint32_t kErrTimeout = 1u;
+
+}  // namespace nrc

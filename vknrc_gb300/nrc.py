@@ -1,0 +1,232 @@
+"""Python binding of libnrc.so (include/nrc.h) over ctypes.
+
+Thin glue for tests and benchmarks: device memory and streams come from
+PyTorch tensors, every call goes through the C ABI. There is no fallback: if
+libnrc.so is missing the import of a Cache fails loudly.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import build as _build
+
+P = 20672
+IN_FLOATS = 14
+TRAIN_FLOATS = 20
+TRAIN_BATCH_SIZE = 16384
+TRAIN_BATCH_COUNT = 4
+WEIGHTS_USE, WEIGHTS_TRAIN = 0, 1
+
+STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "no CUDA device", 4: "unsupported device",
+          5: "out of device memory", 6: "device timeout", 7: "misaligned buffer"}
+
+EXPORTS = [
+    "nrc_status_string", "nrc_default_config", "nrc_create", "nrc_destroy", "nrc_reset", "nrc_he_init_host",
+    "nrc_encode", "nrc_sph_encode", "nrc_infer", "nrc_infer_encoded", "nrc_train", "nrc_gradient", "nrc_frame",
+    "nrc_get_weights", "nrc_set_weights", "nrc_get_optimizer", "nrc_set_optimizer", "nrc_get_loss",
+    "nrc_get_error", "nrc_get_device_buffers",
+]
+
+
+class NRCError(RuntimeError):
+    def __init__(self, status: int, what: str):
+        super().__init__(f"{what}: {STATUS.get(status, status)} ({status})")
+        self.status = status
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("train_batch_size", ctypes.c_uint32), ("learning_rate", ctypes.c_float),
+                ("beta1", ctypes.c_float), ("beta2", ctypes.c_float), ("epsilon", ctypes.c_float),
+                ("ema_alpha", ctypes.c_float), ("loss_scale", ctypes.c_float),
+                ("use_ema_weights", ctypes.c_uint32), ("deterministic", ctypes.c_uint32),
+                ("track_loss", ctypes.c_uint32), ("seed", ctypes.c_uint64)]
+
+
+class OptState(ctypes.Structure):
+    _fields_ = [("t", ctypes.c_uint32), ("beta1_t", ctypes.c_float), ("beta2_t", ctypes.c_float),
+                ("alpha_t", ctypes.c_float), ("alpha_t_1", ctypes.c_float)]
+
+
+_lib: Optional[ctypes.CDLL] = None
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def lib(build_if_missing: bool = True) -> ctypes.CDLL:
+    """Load libnrc.so (building it in-tree first if it is absent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(_build.LIB):
+        if not build_if_missing:
+            raise RuntimeError(f"libnrc.so not built: {_build.LIB}")
+        _build.build()
+    L = ctypes.CDLL(_build.LIB)
+    vp, u32, i32, u64 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int, ctypes.c_uint64
+    L.nrc_status_string.restype = ctypes.c_char_p
+    L.nrc_status_string.argtypes = [i32]
+    L.nrc_default_config.argtypes = [ctypes.POINTER(Config)]
+    L.nrc_create.argtypes = [ctypes.POINTER(Config), ctypes.POINTER(vp)]
+    L.nrc_destroy.argtypes = [vp]
+    L.nrc_reset.argtypes = [vp, u64]
+    L.nrc_he_init_host.argtypes = [u64, vp]
+    L.nrc_encode.argtypes = [vp, vp, vp, u32, vp, vp]
+    L.nrc_sph_encode.argtypes = [vp, vp, u32, vp, vp]
+    L.nrc_infer.argtypes = [vp, vp, vp, u32, vp, i32, vp]
+    L.nrc_infer_encoded.argtypes = [vp, vp, vp, u32, vp, i32, vp]
+    L.nrc_train.argtypes = [vp, vp, vp, u32, i32, vp]
+    L.nrc_gradient.argtypes = [vp, vp, vp, u32, vp, vp]
+    L.nrc_frame.argtypes = [vp, vp, vp, u32, vp, ctypes.POINTER(vp), ctypes.POINTER(vp), u32, vp]
+    L.nrc_get_weights.argtypes = [vp, i32, vp]
+    L.nrc_set_weights.argtypes = [vp, vp]
+    L.nrc_get_optimizer.argtypes = [vp, ctypes.POINTER(OptState), vp]
+    L.nrc_set_optimizer.argtypes = [vp, ctypes.POINTER(OptState), vp]
+    L.nrc_get_loss.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_uint64)]
+    L.nrc_get_error.argtypes = [vp]
+    L.nrc_get_device_buffers.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp),
+                                         ctypes.POINTER(vp)]
+    _lib = L
+    return L
+
+
+def check(status: int, what: str) -> None:
+    if status != 0:
+        raise NRCError(status, what)
+
+
+def default_config(**overrides) -> Config:
+    c = Config()
+    check(lib().nrc_default_config(ctypes.byref(c)), "nrc_default_config")
+    for k, v in overrides.items():
+        if not hasattr(c, k):
+            raise KeyError(k)
+        setattr(c, k, v)
+    return c
+
+
+def he_init_host(seed: int) -> np.ndarray:
+    w = np.empty(P, np.float32)
+    check(lib().nrc_he_init_host(seed, w.ctypes.data_as(ctypes.c_void_p)), "nrc_he_init_host")
+    return w
+
+
+def _ptr(t) -> Optional[int]:
+    if t is None:
+        return None
+    return t.data_ptr()
+
+
+def _stream(stream) -> Optional[int]:
+    import torch
+
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return stream.cuda_stream
+
+
+class Cache:
+    """One neural radiance cache (an nrc_context): weights + Adam state on the GPU."""
+
+    def __init__(self, **cfg):
+        self.cfg = default_config(**cfg)
+        h = ctypes.c_void_p()
+        check(lib().nrc_create(ctypes.byref(self.cfg), ctypes.byref(h)), "nrc_create")
+        self.h = h
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            lib().nrc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ------------------------------------------------------------ compute --
+    def encode(self, inputs, count, out, capacity=None, stream=None):
+        cap = inputs.shape[0] if capacity is None else capacity
+        check(lib().nrc_encode(self.h, _ptr(inputs), _ptr(count), cap, _ptr(out), _stream(stream)), "nrc_encode")
+
+    def infer(self, inputs, count, out, capacity=None, weight_set=WEIGHTS_USE, stream=None):
+        cap = inputs.shape[0] if capacity is None else capacity
+        check(lib().nrc_infer(self.h, _ptr(inputs), _ptr(count), cap, _ptr(out), weight_set, _stream(stream)),
+              "nrc_infer")
+
+    def infer_encoded(self, enc, count, out, capacity=None, weight_set=WEIGHTS_USE, stream=None):
+        cap = enc.shape[0] if capacity is None else capacity
+        check(lib().nrc_infer_encoded(self.h, _ptr(enc), _ptr(count), cap, _ptr(out), weight_set,
+                                      _stream(stream)), "nrc_infer_encoded")
+
+    def train(self, records, count, capacity=None, write_use=False, stream=None):
+        cap = records.shape[0] if capacity is None else capacity
+        check(lib().nrc_train(self.h, _ptr(records), _ptr(count), cap, int(write_use), _stream(stream)), "nrc_train")
+
+    def gradient(self, records, count, grad, capacity=None, stream=None):
+        cap = records.shape[0] if capacity is None else capacity
+        check(lib().nrc_gradient(self.h, _ptr(records), _ptr(count), cap, _ptr(grad), _stream(stream)),
+              "nrc_gradient")
+
+    def frame(self, eval_inputs, eval_count, out, train_records: Sequence, train_counts: Sequence,
+              eval_capacity=None, train_capacity=None, stream=None):
+        ecap = eval_inputs.shape[0] if eval_capacity is None else eval_capacity
+        tcap = train_records[0].shape[0] if train_capacity is None else train_capacity
+        recs = (ctypes.c_void_p * TRAIN_BATCH_COUNT)(*[_ptr(r) for r in train_records])
+        cnts = (ctypes.c_void_p * TRAIN_BATCH_COUNT)(*[_ptr(c) for c in train_counts])
+        check(lib().nrc_frame(self.h, _ptr(eval_inputs), _ptr(eval_count), ecap, _ptr(out), recs, cnts, tcap,
+                              _stream(stream)), "nrc_frame")
+
+    # -------------------------------------------------------------- state --
+    def get_weights(self, which=WEIGHTS_TRAIN) -> np.ndarray:
+        w = np.empty(P, np.uint16)
+        check(lib().nrc_get_weights(self.h, which, w.ctypes.data_as(ctypes.c_void_p)), "nrc_get_weights")
+        return w
+
+    def set_weights(self, w16: np.ndarray) -> None:
+        w = np.ascontiguousarray(w16, np.uint16)
+        assert w.size == P
+        check(lib().nrc_set_weights(self.h, w.ctypes.data_as(ctypes.c_void_p)), "nrc_set_weights")
+
+    def get_optimizer(self):
+        st = OptState()
+        ent = np.empty((P, 4), np.float32)
+        check(lib().nrc_get_optimizer(self.h, ctypes.byref(st), ent.ctypes.data_as(ctypes.c_void_p)),
+              "nrc_get_optimizer")
+        return (st.t, st.beta1_t, st.beta2_t, st.alpha_t, st.alpha_t_1), ent
+
+    def set_optimizer(self, state=None, entries: Optional[np.ndarray] = None) -> None:
+        st = OptState(*state) if state is not None else None
+        ent = np.ascontiguousarray(entries, np.float32) if entries is not None else None
+        check(lib().nrc_set_optimizer(self.h, ctypes.byref(st) if st is not None else None,
+                                      ent.ctypes.data_as(ctypes.c_void_p) if ent is not None else None),
+              "nrc_set_optimizer")
+
+    def reset(self, seed: int) -> None:
+        check(lib().nrc_reset(self.h, seed), "nrc_reset")
+
+    def get_loss(self):
+        s, n = ctypes.c_double(), ctypes.c_uint64()
+        check(lib().nrc_get_loss(self.h, ctypes.byref(s), ctypes.byref(n)), "nrc_get_loss")
+        return s.value, n.value
+
+    def error(self) -> int:
+        return lib().nrc_get_error(self.h)
+
+    def device_buffers(self):
+        w, u, e, s = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+        check(lib().nrc_get_device_buffers(self.h, ctypes.byref(w), ctypes.byref(u), ctypes.byref(e), ctypes.byref(s)),
+              "nrc_get_device_buffers")
+        return w.value, u.value, e.value, s.value

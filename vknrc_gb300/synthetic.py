@@ -1,0 +1,75 @@
+"""Seeded synthetic path-vertex records with the distributions of the benchmark
+configurations (no dataset exists for this path: the reference's records come
+from its path tracer, shader/src/path_tracer.comp:159-166, 302-371).
+
+Inputs follow nrc_input / UnpackedNRCInput (shader/src/NRCRecord.glsl:40-45):
+position U[0,1]^3; scattered direction and normal uniform on the sphere, then
+sphere-encoded (NRCSphEncode), the direction quantised to unorm16 as the path
+tracer stores it (path_tracer.comp:164); roughness U(0,1); diffuse and specular
+albedo U(0,1)^3.
+
+Training records follow nrc_train_record: bias = target radiance, factor = 1.
+Targets: lognormal(0, 1.5) per channel, or a fixed smooth field of the inputs
+times lognormal noise (for loss curves that can be compared across runs).
+Per-frame redraws key a counter-based generator (Philox) by (seed, frame, stream).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+IN_FLOATS = 14
+TRAIN_FLOATS = 20
+
+
+def rng_for(seed: int, frame: int = 0, stream: int = 0) -> np.random.Generator:
+    return np.random.Generator(np.random.Philox(key=[seed & 0xFFFFFFFFFFFFFFFF, (frame << 16) | stream]))
+
+
+def sphere(rng: np.random.Generator, n: int) -> np.ndarray:
+    v = rng.standard_normal((n, 3))
+    v /= np.maximum(np.linalg.norm(v, axis=1, keepdims=True), 1e-30)
+    return v.astype(np.float32)
+
+
+def sph_encode(d: np.ndarray) -> np.ndarray:
+    """NRCSphEncode (NRCRecord.glsl:47-49) in float64, rounded to float32."""
+    d = d.astype(np.float64)
+    u = np.where((d[:, 0] == 0) & (d[:, 1] == 0), 0.5, 0.5 + np.arctan2(d[:, 1], d[:, 0]) / (2 * np.pi))
+    v = np.arccos(np.clip(d[:, 2], -1, 1)) / np.pi
+    return np.stack([u, v], 1).astype(np.float32)
+
+
+def inputs(rng: np.random.Generator, n: int) -> np.ndarray:
+    """(n, 14) float32 nrc_input records."""
+    r = np.empty((n, IN_FLOATS), np.float32)
+    r[:, 0:3] = rng.random((n, 3), dtype=np.float32)
+    r[:, 3:5] = np.round(sph_encode(sphere(rng, n)) * 65535.0) / 65535.0
+    r[:, 5:7] = sph_encode(sphere(rng, n))
+    r[:, 7] = rng.random(n, dtype=np.float32)
+    r[:, 8:14] = rng.random((n, 6), dtype=np.float32)
+    return r
+
+
+def smooth_field(x: np.ndarray) -> np.ndarray:
+    """A fixed smooth positive radiance field of the inputs, (n, 3) float32."""
+    p, d, nrm, rough = x[:, 0:3], x[:, 3:5], x[:, 5:7], x[:, 7]
+    diff, spec = x[:, 8:11], x[:, 11:14]
+    shade = 0.6 + 0.4 * np.sin(2 * np.pi * (p[:, 0] + 0.3 * p[:, 2])) * np.cos(np.pi * nrm[:, 1])
+    gloss = np.exp(-4.0 * rough) * (0.5 + 0.5 * np.cos(2 * np.pi * (p[:, 1] + d[:, 0])))
+    return (diff * shade[:, None] + spec * gloss[:, None] + 0.05).astype(np.float32)
+
+
+def train_records(rng: np.random.Generator, n: int, target: str = "lognormal", sigma: float = 1.5) -> np.ndarray:
+    """(n, 20) float32 nrc_train_record rows: bias[3], factor[3], input[14]."""
+    x = inputs(rng, n)
+    if target == "lognormal":
+        t = rng.lognormal(0.0, sigma, (n, 3)).astype(np.float32)
+    elif target == "field":
+        t = smooth_field(x) * rng.lognormal(0.0, sigma, (n, 3)).astype(np.float32)
+    else:
+        raise ValueError(target)
+    rec = np.empty((n, TRAIN_FLOATS), np.float32)
+    rec[:, 0:3] = t
+    rec[:, 3:6] = 1.0
+    rec[:, 6:20] = x
+    return rec
