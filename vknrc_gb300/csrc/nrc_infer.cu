@@ -7,15 +7,14 @@
 //   - the 42 KB of fp16 weights are staged once per CTA into shared memory as
 //     128-byte-swizzled K-major tiles (the MMA's B operand);
 //   - activations never leave the SM: each layer's fp16 input sits in tensor
-//     memory as the MMA's A operand (the TMEM-A form), its fp32 result lands in
-//     TMEM, and the epilogue threads convert it (ReLU + fp16) back into the A
-//     operand of the next layer;
-//   - kSlots independent 128-record tiles are in flight per CTA (128 TMEM
-//     columns each) so the single MMA-issuing thread always has a ready tile
-//     while the epilogue warps of the others convert.
-// Warp 0: TMEM allocator, lane 0 issues all MMAs. Warps 1..16: four epilogue
-// warpgroups, one per slot; thread <-> record row, warp w reads TMEM lanes
-// 32*(w%4)..+31.
+//     memory as the MMA's A operand (32 columns), its fp32 result lands in
+//     tensor memory (64 columns), and the epilogue threads convert it (ReLU +
+//     fp16) back into the A columns for the next layer;
+//   - kSlots independent 128-record tiles are in flight per CTA, one warpgroup
+//     each (thread <-> record row, warp k of a slot reads TMEM lanes 32k..+31).
+//     Every slot issues its own MMAs from its first warp (converged, one lane
+//     elected): a single issuing thread is bounded by its issue rate, several
+//     issuing warps keep the tensor pipe busy while other slots convert.
 #include "nrc_common.cuh"
 #include "nrc_kernels.h"
 
@@ -23,14 +22,16 @@ namespace nrc {
 
 namespace {
 
-constexpr int kSlots = 4;
-constexpr int kInferThreads = 32 + kSlots * 128;
-constexpr uint32_t kRecBytes = sizeof(nrc_input);   // 56
+constexpr int kSlots = 5;
+constexpr int kInferThreads = kSlots * 128;
+constexpr uint32_t kSlotCols = 96;                     // A: cols 0..31, D: cols 32..95
+constexpr uint32_t kRecBytes = sizeof(nrc_input);      // 56
 constexpr uint32_t kRecTileBytes = kTile * kRecBytes;  // 7168
 constexpr uint32_t kRecSmemOff = kWeightSmemBytes;     // 43008, 1024-aligned
 constexpr uint32_t kBarOff = kRecSmemOff + kSlots * 2 * kRecTileBytes;
-constexpr uint32_t kSmemBytes = kBarOff + 256 + 1024;  // + alignment slack
+constexpr uint32_t kSmemBytes = kBarOff + 512 + 1024;  // + alignment slack
 static_assert(kWeightSmemBytes % 1024 == 0, "weight tiles 1024-aligned");
+static_assert(kSlots * kSlotCols <= 512, "TMEM columns");
 
 struct SlotBars {
   uint64_t rec_full[2];   // bulk copy of a record tile landed (tx bytes)
@@ -38,7 +39,7 @@ struct SlotBars {
   uint64_t a_ready;       // 128 arrivals: A operand in TMEM for the next layer
   uint64_t d_ready;       // MMA commit: accumulator ready
 };
-static_assert(sizeof(SlotBars) * kSlots + 16 <= 256, "barrier area");
+static_assert(sizeof(SlotBars) * kSlots + 16 <= 512, "barrier area");
 
 __device__ __forceinline__ uint8_t* align1024(uint8_t* p) {
   return reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(p) + 1023) & ~uintptr_t(1023));
@@ -61,6 +62,16 @@ __device__ __forceinline__ void issue_record_tile(const nrc_input* __restrict__ 
 
 __device__ __forceinline__ bool warp_all(bool ok) { return __all_sync(0xffffffffu, ok); }
 
+// The four K-steps of one layer: D[128 x N] = A[128 x 64] (TMEM) * W^T.
+// bdesc0 addresses the layer's weight tile; each K-step advances 32 bytes
+// (2 in the descriptor's 16-byte address units).
+__device__ __forceinline__ void issue_layer(uint32_t d, uint32_t a, uint64_t bdesc0, uint32_t idesc) {
+  mma_ts(d, a + 0, bdesc0 + 0, idesc, 0u);
+  mma_ts(d, a + 8, bdesc0 + 2, idesc, 1u);
+  mma_ts(d, a + 16, bdesc0 + 4, idesc, 1u);
+  mma_ts(d, a + 24, bdesc0 + 6, idesc, 1u);
+}
+
 template <bool kEncoded>
 __global__ void __launch_bounds__(kInferThreads, 1)
     infer_kernel(const void* __restrict__ input, const uint32_t* __restrict__ d_count, uint32_t capacity,
@@ -70,8 +81,7 @@ __global__ void __launch_bounds__(kInferThreads, 1)
   uint8_t* smem_w = smem;
   uint8_t* smem_rec = smem + kRecSmemOff;
   SlotBars* bars = reinterpret_cast<SlotBars*>(smem + kBarOff);
-  uint64_t* drain = reinterpret_cast<uint64_t*>(bars + kSlots);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + kSlots);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t n = min(*d_count, capacity);
@@ -86,7 +96,6 @@ __global__ void __launch_bounds__(kInferThreads, 1)
       mbar_init(&bars[s].a_ready, 128);
       mbar_init(&bars[s].d_ready, 1);
     }
-    mbar_init(drain, 1);
     mbar_fence_init();
   }
   if (warp == 0) {
@@ -98,159 +107,135 @@ __global__ void __launch_bounds__(kInferThreads, 1)
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
-  const uint32_t tmem = *tmem_slot;
 
-  if (warp == 0) {
-    // ------------------------------------------------------ MMA issuer --
-    if (lane == 0) {
-      bool ok = true;
-      uint32_t ph_a[kSlots] = {0, 0, 0, 0};
-      const uint32_t id64 = idesc_f16_f32(128, 64, 0, 0);
-      const uint32_t id16 = idesc_f16_f32(128, 16, 0, 0);
-      const uint32_t sw = smem_u32(smem_w);
-      for (uint32_t it = 0; ok; ++it) {
-        const uint32_t tile0 = (it * gridDim.x + blockIdx.x) * kSlots;
-        if (tile0 >= num_tiles) break;
-        for (int l = 0; l < 6 && ok; ++l) {
-          for (int s = 0; s < kSlots; ++s) {
-            if (tile0 + s >= num_tiles) break;
-            if (!mbar_wait(&bars[s].a_ready, ph_a[s], kWaitLimitNs)) {
-              ok = false;
-              break;
-            }
-            ph_a[s] ^= 1u;
-            tc_fence_after();
-            const uint32_t base = tmem + s * 128;
-            const uint32_t a = base + ((l & 1) ? 64u : 0u);
-            const uint32_t d = base + ((l & 1) ? 0u : 64u);
-            const uint32_t wl = sw + l * 8192;
-#pragma unroll
-            for (int j = 0; j < 4; ++j)
-              mma_ts(d, a + 8 * j, sdesc_sw128(wl + 32 * j, 16, 1024), l < 5 ? id64 : id16, j > 0);
-            mma_commit(&bars[s].d_ready);
-          }
-        }
-      }
-      if (!ok) atomicOr(err, kErrTimeout);
-      // all issued MMAs must be complete before TMEM is released
-      mma_commit(drain);
-      if (!mbar_wait(drain, 0, kWaitLimitNs)) atomicOr(err, kErrTimeout);
-    }
-    __syncwarp();
-  } else {
-    // ------------------------------------------------ epilogue warpgroups --
-    const int ew = warp - 1;
-    const int s = ew >> 2;
-    const int q = warp & 3;  // TMEM lane quadrant accessible to this warp
-    const int row = q * 32 + lane;
-    const bool leader = (ew & 3) == 0 && lane == 0;
-    SlotBars& B = bars[s];
-    const uint32_t lane_base = tmem + (static_cast<uint32_t>(q * 32) << 16) + s * 128;
-    uint8_t* stage[2] = {smem_rec + (s * 2 + 0) * kRecTileBytes, smem_rec + (s * 2 + 1) * kRecTileBytes};
-    const nrc_input* rec_in = static_cast<const nrc_input*>(input);
-    auto tile_of = [&](uint32_t it) { return (it * gridDim.x + blockIdx.x) * kSlots + s; };
+  const int s = warp >> 2;  // slot
+  const int q = warp & 3;   // TMEM lane quadrant of this warp
+  const int row = q * 32 + lane;
+  const bool issuer = q == 0;
+  const bool leader = q == 0 && lane == 0;
+  SlotBars& B = bars[s];
+  const uint32_t tmem = __shfl_sync(0xffffffffu, *tmem_slot, 0);
+  const uint32_t a_col = tmem + s * kSlotCols, d_col = a_col + 32;  // lane-0 addresses of the slot
+  const uint32_t lane_off = static_cast<uint32_t>(q * 32) << 16;
+  const uint64_t wdesc = sdesc_sw128(smem_u32(smem_w), 16, 1024);  // layer l: + l * 512
+  const uint32_t id64 = idesc_f16_f32(128, 64, 0, 0), id16 = idesc_f16_f32(128, 16, 0, 0);
+  uint8_t* stage0 = smem_rec + (s * 2 + 0) * kRecTileBytes;
+  const nrc_input* rec_in = static_cast<const nrc_input*>(input);
+  auto tile_of = [&](uint32_t it) { return (it * gridDim.x + blockIdx.x) * kSlots + s; };
 
-    if (!kEncoded && leader) {
-      for (uint32_t b = 0; b < 2; ++b)
-        if (tile_of(b) < num_tiles) issue_record_tile(rec_in, tile_of(b), n, stage[b], &B.rec_full[b]);
-    }
-    bool ok = true;
-    uint32_t ph_d = 0;
-    for (uint32_t it = 0; ok; ++it) {
-      const uint32_t tile = tile_of(it);
-      if (tile >= num_tiles) break;
-      const uint32_t rows_valid = min(static_cast<uint32_t>(kTile), n - tile * kTile);
-      const size_t grow = static_cast<size_t>(tile) * kTile + row;
-      uint32_t e[32];
-      if (!kEncoded) {
-        const uint32_t b = it & 1;
-        ok = warp_all(mbar_wait(&B.rec_full[b], (it >> 1) & 1, kWaitLimitNs));
-        if (!ok) break;
-        const uint32_t bulk = rows_valid == kTile ? kRecTileBytes : ((rows_valid * kRecBytes) & ~15u);
-        float r[kInFloats];
-        if (row < static_cast<int>(rows_valid)) {
-          const float2* src = (static_cast<uint32_t>(row + 1) * kRecBytes <= bulk)
-                                  ? reinterpret_cast<const float2*>(stage[b] + row * kRecBytes)
-                                  : reinterpret_cast<const float2*>(rec_in + grow);
+  if (!kEncoded && leader) {
+    for (uint32_t b = 0; b < 2; ++b)
+      if (tile_of(b) < num_tiles)
+        issue_record_tile(rec_in, tile_of(b), n, stage0 + b * kRecTileBytes, &B.rec_full[b]);
+  }
+  bool ok = true;
+  uint32_t ph_d = 0, ph_a = 0;
+  for (uint32_t it = 0; ok; ++it) {
+    const uint32_t tile = tile_of(it);
+    if (tile >= num_tiles) break;
+    const uint32_t rows_valid = min(static_cast<uint32_t>(kTile), n - tile * kTile);
+    const size_t grow = static_cast<size_t>(tile) * kTile + row;
+    uint32_t e[32];
+    if (!kEncoded) {
+      const uint32_t b = it & 1;
+      uint8_t* stage = stage0 + b * kRecTileBytes;
+      ok = warp_all(mbar_wait(&B.rec_full[b], (it >> 1) & 1, kWaitLimitNs));
+      if (!ok) break;
+      const uint32_t bulk = rows_valid == kTile ? kRecTileBytes : ((rows_valid * kRecBytes) & ~15u);
+      float r[kInFloats];
+      if (row < static_cast<int>(rows_valid)) {
+        const float2* src = (static_cast<uint32_t>(row + 1) * kRecBytes <= bulk)
+                                ? reinterpret_cast<const float2*>(stage + row * kRecBytes)
+                                : reinterpret_cast<const float2*>(rec_in + grow);
 #pragma unroll
-          for (int k = 0; k < 7; ++k) {
-            const float2 v = src[k];
-            r[2 * k] = v.x;
-            r[2 * k + 1] = v.y;
-          }
-        } else {
-#pragma unroll
-          for (int k = 0; k < kInFloats; ++k) r[k] = 0.0f;
-        }
-        // the stage may be refilled once all 128 threads have read it
-        mbar_arrive(&B.rec_empty[b]);
-        encode_input(r, e);
-        if (leader && tile_of(it + 2) < num_tiles) {
-          if (!mbar_wait(&B.rec_empty[b], (it >> 1) & 1, kWaitLimitNs)) {
-            atomicOr(err, kErrTimeout);
-          } else {
-            issue_record_tile(rec_in, tile_of(it + 2), n, stage[b], &B.rec_full[b]);
-          }
+        for (int k = 0; k < 7; ++k) {
+          const float2 v = src[k];
+          r[2 * k] = v.x;
+          r[2 * k + 1] = v.y;
         }
       } else {
-        const uint16_t* enc_in = static_cast<const uint16_t*>(input);
-        if (row < static_cast<int>(rows_valid)) {
-          const uint4* src = reinterpret_cast<const uint4*>(enc_in + grow * 64);
 #pragma unroll
-          for (int c = 0; c < 8; ++c) {
-            const uint4 v = __ldg(src + c);
-            e[4 * c] = v.x;
-            e[4 * c + 1] = v.y;
-            e[4 * c + 2] = v.z;
-            e[4 * c + 3] = v.w;
+        for (int k = 0; k < kInFloats; ++k) r[k] = 0.0f;
+      }
+      // the stage may be refilled once all 128 threads have read it
+      mbar_arrive(&B.rec_empty[b]);
+      encode_input(r, e);
+      if (leader && tile_of(it + 2) < num_tiles) {
+        if (!mbar_wait(&B.rec_empty[b], (it >> 1) & 1, kWaitLimitNs))
+          atomicOr(err, kErrTimeout);
+        else
+          issue_record_tile(rec_in, tile_of(it + 2), n, stage, &B.rec_full[b]);
+      }
+    } else {
+      const uint16_t* enc_in = static_cast<const uint16_t*>(input);
+      if (row < static_cast<int>(rows_valid)) {
+        const uint4* src = reinterpret_cast<const uint4*>(enc_in + grow * 64);
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+          const uint4 v = __ldg(src + c);
+          e[4 * c] = v.x;
+          e[4 * c + 1] = v.y;
+          e[4 * c + 2] = v.z;
+          e[4 * c + 3] = v.w;
+        }
+      } else {
+#pragma unroll
+        for (int c = 0; c < 32; ++c) e[c] = 0u;
+      }
+    }
+    __syncwarp();  // reconverge before the warp-collective TMEM store
+    // layer-0 A operand: fp16 features, column pair (2j, 2j+1) in word j
+    tmem_st32(a_col + lane_off, e);
+    tc_fence_before();
+    mbar_arrive(&B.a_ready);
+#pragma unroll 1
+    for (int l = 0; l < 6; ++l) {
+      if (issuer) {
+        ok = warp_all(mbar_wait(&B.a_ready, ph_a, kWaitLimitNs));
+        if (ok) {
+          ph_a ^= 1u;  // counts issued layers; ph_d counts observed completions
+          tc_fence_after();
+          if (elect_one()) {
+            issue_layer(d_col, a_col, wdesc + static_cast<uint64_t>(l * 512), l < 5 ? id64 : id16);
+            mma_commit(&B.d_ready);
           }
-        } else {
-#pragma unroll
-          for (int c = 0; c < 32; ++c) e[c] = 0u;
+          __syncwarp();
         }
       }
-      __syncwarp();  // reconverge before the warp-collective TMEM store
-      // layer-0 A operand: fp16 features, column pair (2j, 2j+1) in word j
-      tmem_st32(lane_base, e);
-      tc_fence_before();
-      mbar_arrive(&B.a_ready);
-#pragma unroll 1
-      for (int l = 0; l < 5; ++l) {
-        ok = warp_all(mbar_wait(&B.d_ready, ph_d, kWaitLimitNs));
-        if (!ok) break;
-        ph_d ^= 1u;
-        tc_fence_after();
-        const uint32_t dcol = (l & 1) ? 0u : 64u;
-        uint32_t v[32], p[32];
-        tmem_ld32(lane_base + dcol, v);
-#pragma unroll
-        for (int j = 0; j < 16; ++j) p[j] = pack_relu_f16x2(__uint_as_float(v[2 * j]), __uint_as_float(v[2 * j + 1]));
-        tmem_ld32(lane_base + dcol + 32, v);
-#pragma unroll
-        for (int j = 0; j < 16; ++j)
-          p[16 + j] = pack_relu_f16x2(__uint_as_float(v[2 * j]), __uint_as_float(v[2 * j + 1]));
-        tmem_st32(lane_base + dcol, p);
-        tc_fence_before();
-        mbar_arrive(&B.a_ready);
-      }
-      if (!ok) break;
-      ok = warp_all(mbar_wait(&B.d_ready, ph_d, kWaitLimitNs));
+      ok = ok && warp_all(mbar_wait(&B.d_ready, ph_d, kWaitLimitNs));
       if (!ok) break;
       ph_d ^= 1u;
       tc_fence_after();
-      uint32_t o4[4];
-      tmem_ld4(lane_base + 0, o4);  // output layer (odd) accumulates at column 0
-      if (row < static_cast<int>(rows_valid)) {
-        float* dst = out + grow * 3;
+      if (l < 5) {
+        uint32_t v[32], p[32];
+        tmem_ld32(d_col + lane_off, v);
 #pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          const float v = __uint_as_float(o4[c]);
-          dst[c] = clamp_out ? fmaxf(v, 0.0f) : v;
+        for (int j = 0; j < 16; ++j) p[j] = pack_relu_f16x2(__uint_as_float(v[2 * j]), __uint_as_float(v[2 * j + 1]));
+        tmem_ld32(d_col + lane_off + 32, v);
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+          p[16 + j] = pack_relu_f16x2(__uint_as_float(v[2 * j]), __uint_as_float(v[2 * j + 1]));
+        tmem_st32(a_col + lane_off, p);
+        tc_fence_before();
+        mbar_arrive(&B.a_ready);
+      } else {
+        uint32_t o4[4];
+        tmem_ld4(d_col + lane_off, o4);
+        if (row < static_cast<int>(rows_valid)) {
+          float* dst = out + grow * 3;
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            const float v = __uint_as_float(o4[c]);
+            dst[c] = clamp_out ? fmaxf(v, 0.0f) : v;
+          }
         }
       }
     }
-    if (!ok && lane == 0) atomicOr(err, kErrTimeout);
   }
+  if (!ok && lane == 0) atomicOr(err, kErrTimeout);
+  // A slot that stopped early may still have MMAs in flight (issued, d_ready
+  // not yet observed): wait for them, bounded, before TMEM is released.
+  if (!ok && issuer && ph_a != ph_d) warp_all(mbar_wait(&B.d_ready, ph_d, kWaitLimitNs));
   tc_fence_before();
   __syncthreads();
   if (warp == 0) {

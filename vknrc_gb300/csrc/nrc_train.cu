@@ -145,57 +145,80 @@ __global__ void __launch_bounds__(kTrainThreads, 1)
 
   if (warp == 0) {
     // ------------------------------------------------------ MMA issuer --
-    if (lane == 0) {
-      bool ok = true;
-      uint32_t ph_a = 0;
-      const uint32_t sw = smem_u32(smem_w), sact = smem_u32(act), sg = smem_u32(gbuf);
-      const uint32_t id_fwd = idesc_f16_f32(128, 64, 0, 0);
-      const uint32_t id_out = idesc_f16_f32(128, 16, 0, 0);
-      const uint32_t id_dw = idesc_f16_f32(64, 64, 1, 1);
-      const uint32_t id_da = idesc_f16_f32(128, 64, 0, 1);
-      const uint32_t dcol = tmem + kDCol;
-      auto wait_a = [&]() {
-        if (!ok) return;
-        if (!mbar_wait(&B->a_ready, ph_a, kWaitLimitNs)) ok = false;
-        ph_a ^= 1u;
-        tc_fence_after();
-      };
-      uint32_t it = 0;
-      for (uint32_t tile = blockIdx.x; tile < num_tiles && ok; tile += gridDim.x, ++it) {
-        wait_a();  // act_0
-        for (int l = 0; l < 6 && ok; ++l) {
-          const uint32_t a_l = sact + l * kActBytes, w_l = sw + l * 8192;
-#pragma unroll
-          for (int j = 0; j < 4; ++j)
-            mma_ss(dcol, sdesc_sw128(a_l + 32 * j, 16, 1024), sdesc_sw128(w_l + 32 * j, 16, 1024),
-                   l < 5 ? id_fwd : id_out, j > 0);
+    // The whole warp runs the schedule (converged, so descriptors stay
+    // warp-uniform); one elected lane issues each group of MMAs.
+    bool ok = true;
+    uint32_t ph_a = 0;
+    const uint32_t tm = __shfl_sync(0xffffffffu, tmem, 0);
+    const uint32_t id_fwd = idesc_f16_f32(128, 64, 0, 0);
+    const uint32_t id_out = idesc_f16_f32(128, 16, 0, 0);
+    const uint32_t id_dw = idesc_f16_f32(64, 64, 1, 1);
+    const uint32_t id_da = idesc_f16_f32(128, 64, 0, 1);
+    const uint32_t dcol = tm + kDCol;
+    // descriptor bases; +1 in the address field = 16 bytes
+    const uint64_t dk_act = sdesc_sw128(smem_u32(act), 16, 1024);   // K-major act_l: + l*1024 + 2j
+    const uint64_t dk_w = sdesc_sw128(smem_u32(smem_w), 16, 1024);  // K-major W_l: + l*512 + 2j
+    const uint64_t dm_g = sdesc_sw128(smem_u32(gbuf), 8192, 1024);  // MN-major g: + buf*1024 + 128j
+    const uint64_t dk_g = sdesc_sw128(smem_u32(gbuf), 16, 1024);    // K-major g: + buf*1024 + 2j
+    const uint64_t dm_act = sdesc_sw128(smem_u32(act), 8192, 1024); // MN-major act_l: + l*1024 + 128j
+    const uint64_t dm_w = sdesc_sw128(smem_u32(smem_w), 8192, 1024); // MN-major W_l: + l*512 + 128j
+    auto wait_a = [&]() {
+      if (!ok) return;
+      ok = warp_all(mbar_wait(&B->a_ready, ph_a, kWaitLimitNs));
+      if (!ok) return;
+      ph_a ^= 1u;
+      tc_fence_after();
+    };
+    uint32_t it = 0;
+    for (uint32_t tile = blockIdx.x; tile < num_tiles && ok; tile += gridDim.x, ++it) {
+      wait_a();  // act_0
+      for (int l = 0; l < 6 && ok; ++l) {
+        if (elect_one()) {
+          const uint64_t a = dk_act + static_cast<uint64_t>(l * 1024), w = dk_w + static_cast<uint64_t>(l * 512);
+          const uint32_t id = l < 5 ? id_fwd : id_out;
+          mma_ss(dcol, a + 0, w + 0, id, 0u);
+          mma_ss(dcol, a + 2, w + 2, id, 1u);
+          mma_ss(dcol, a + 4, w + 4, id, 1u);
+          mma_ss(dcol, a + 6, w + 6, id, 1u);
           mma_commit(&B->d_ready);
-          wait_a();  // act_{l+1}, or g_6 after the output layer
         }
-        // backward: g_{l+1} lives in gbuf[(5 - l) & 1]
-        for (int l = 5; l >= 0 && ok; --l) {
-          const uint32_t g = sg + ((5 - l) & 1) * kActBytes;
-          const uint32_t a_l = sact + l * kActBytes, w_l = sw + l * 8192;
-          // dW_l += g^T act_l   (M = 64 outputs, N = 64 inputs, K = 128 records)
-#pragma unroll
-          for (int j = 0; j < 8; ++j)
-            mma_ss(tmem + 64 * l, sdesc_sw128(g + 2048 * j, 8192, 1024), sdesc_sw128(a_l + 2048 * j, 8192, 1024),
-                   id_dw, (it > 0 || j > 0) ? 1u : 0u);
-          if (l == 0) break;
-          // dA_l = g W_l  (K = 64 outputs, or 16 for the padded output layer)
-          const int ksteps = l == 5 ? 1 : 4;
-          for (int j = 0; j < ksteps; ++j)
-            mma_ss(dcol, sdesc_sw128(g + 32 * j, 16, 1024), sdesc_sw128(w_l + 2048 * j, 8192, 1024), id_da, j > 0);
-          mma_commit(&B->d_ready);
-          wait_a();  // g_l
-        }
-        mma_commit(&B->tile_done);
+        __syncwarp();
+        wait_a();  // act_{l+1}, or g_6 after the output layer
       }
-      if (!ok) atomicOr(err, kErrTimeout);
-      mma_commit(&B->drain);
-      if (!mbar_wait(&B->drain, 0, kWaitLimitNs)) atomicOr(err, kErrTimeout);
+      // backward: g_{l+1} lives in gradient buffer (5 - l) & 1
+      for (int l = 5; l >= 0 && ok; --l) {
+        const uint64_t gb = static_cast<uint64_t>(((5 - l) & 1) * 1024);
+        if (elect_one()) {
+          // dW_l += g^T act_l   (M = 64 outputs, N = 64 inputs, K = 128 records)
+          const uint64_t ga = dm_g + gb, ab = dm_act + static_cast<uint64_t>(l * 1024);
+          const uint32_t acc0 = it > 0 ? 1u : 0u;
+          const uint32_t dw = tm + 64 * l;
+          mma_ss(dw, ga + 0, ab + 0, id_dw, acc0);
+#pragma unroll
+          for (int j = 1; j < 8; ++j) mma_ss(dw, ga + 128 * j, ab + 128 * j, id_dw, 1u);
+          if (l > 0) {
+            // dA_l = g W_l  (K = 64 outputs, or 16 for the padded output layer)
+            const uint64_t gk = dk_g + gb, wm = dm_w + static_cast<uint64_t>(l * 512);
+            mma_ss(dcol, gk + 0, wm + 0, id_da, 0u);
+            if (l < 5) {
+              mma_ss(dcol, gk + 2, wm + 128, id_da, 1u);
+              mma_ss(dcol, gk + 4, wm + 256, id_da, 1u);
+              mma_ss(dcol, gk + 6, wm + 384, id_da, 1u);
+            }
+            mma_commit(&B->d_ready);
+          } else {
+            mma_commit(&B->tile_done);
+          }
+        }
+        __syncwarp();
+        if (l > 0) wait_a();  // g_l
+      }
     }
+    if (!ok && lane == 0) atomicOr(err, kErrTimeout);
+    // all issued MMAs must be complete before TMEM is released
+    if (elect_one()) mma_commit(&B->drain);
     __syncwarp();
+    if (!warp_all(mbar_wait(&B->drain, 0, kWaitLimitNs)) && lane == 0) atomicOr(err, kErrTimeout);
   } else {
     // ------------------------------------------------ epilogue warpgroup --
     const int q = warp & 3;

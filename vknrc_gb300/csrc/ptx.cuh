@@ -216,6 +216,17 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
                : "memory");
 }
 
+// One lane of a converged warp returns true (elect.sync).
+__device__ __forceinline__ bool elect_one() {
+  uint32_t pred = 0;
+  asm volatile(
+      "{\n\t.reg .pred P;\n\t"
+      "elect.sync _|P, 0xffffffff;\n\t"
+      "selp.u32 %0, 1, 0, P;\n\t}"
+      : "=r"(pred));
+  return pred != 0;
+}
+
 // ------------------------------------------------------------- packing --
 // fp32 pair -> f16x2 with ReLU, round to nearest even; `lo` lands in bits 0..15.
 __device__ __forceinline__ uint32_t pack_relu_f16x2(float lo, float hi) {
