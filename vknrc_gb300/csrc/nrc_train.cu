@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(kTrainThreads, 1)
   // the clamped value, and both clamp to the same n.
   if (do_prepare && blockIdx.x == 0 && threadIdx.x == 0) {
     *d_count = clamped;
-    if (clamped > 0) {
+    if (n > 0) {  // the optimizer kernel updates exactly when records were processed
       nrc_optimizer_state st = *state;
       st.t += 1;
       st.beta1_t *= beta1;
