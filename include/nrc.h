@@ -101,7 +101,8 @@ typedef enum nrc_status {
   NRC_ERROR_UNSUPPORTED_DEVICE = 4, /* not an sm_103 (GB300) device */
   NRC_ERROR_OUT_OF_MEMORY = 5,
   NRC_ERROR_DEVICE_TIMEOUT = 6, /* a kernel's bounded wait ran out (latched) */
-  NRC_ERROR_MISALIGNED = 7
+  NRC_ERROR_MISALIGNED = 7,
+  NRC_ERROR_TOO_LARGE = 8 /* more records than nrc_train_noalloc's fixed scratch holds */
 } nrc_status;
 
 /* Which fp16 weight vector a query uses. The reference renders with
@@ -176,6 +177,28 @@ NRC_API int nrc_gradient(nrc_context* ctx, const nrc_train_record* d_records, co
 NRC_API int nrc_frame(nrc_context* ctx, const nrc_input* d_eval_inputs, const uint32_t* d_eval_count, uint32_t eval_capacity,
               float* d_out_rgb, const nrc_train_record* const* d_train_records, uint32_t* const* d_train_counts,
               uint32_t train_capacity, void* stream);
+
+/* One training step with nrc_train's semantics that allocates no device memory.
+ * No counterpart in the reference: it serves callers that cannot call cudaMalloc,
+ * such as a renderer that sub-allocates every device buffer from its own heaps or
+ * a process held to a fixed device-memory budget. The caller owns the parameter
+ * buffers in the layouts above (fp16 weights, optional fp16 use_weights, Adam
+ * entries, step state) as well as the records and the count; `cfg` supplies the
+ * hyper-parameters (seed, deterministic and track_loss are ignored).
+ * Scratch: the per-CTA weight-gradient partials live in a fixed array compiled
+ * into the library, 5,292,288 bytes held by every GPU that loads it until the
+ * process exits; it bounds one call to 16,384 records: if min(capacity,
+ * cfg->train_batch_size) is larger the call returns NRC_ERROR_TOO_LARGE and does
+ * nothing. The gradient is summed in a fixed order.
+ * The first call on a device performs a one-time set-up (it resolves the
+ * scratch's device address); make that first call before any stream capture.
+ * Every call uses the same scratch: calls that may overlap on the GPU (other
+ * streams, no ordering) race; order them. d_error (may be NULL) receives the
+ * device-timeout flag; when NULL a word in the scratch is used, cleared on each
+ * call. */
+NRC_API int nrc_train_noalloc(uint16_t* d_weights, uint16_t* d_use_weights, nrc_optimizer_entry* d_entries,
+                              nrc_optimizer_state* d_state, const nrc_train_record* d_records, uint32_t* d_count,
+                              uint32_t capacity, const nrc_config* cfg, uint32_t* d_error, void* stream);
 
 /* Host copies of the parameter state (synchronous). `which` selects
  * NRC_WEIGHTS_USE or NRC_WEIGHTS_TRAIN for the fp16 vectors. */

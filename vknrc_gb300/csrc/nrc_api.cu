@@ -112,6 +112,7 @@ const char* nrc_status_string(int s) {
     case NRC_ERROR_OUT_OF_MEMORY: return "out of device memory";
     case NRC_ERROR_DEVICE_TIMEOUT: return "a kernel's bounded wait timed out";
     case NRC_ERROR_MISALIGNED: return "device buffer not 16-byte aligned";
+    case NRC_ERROR_TOO_LARGE: return "more records than the fixed no-allocation scratch holds (16,384)";
     default: return "unknown status";
   }
 }

@@ -1,0 +1,112 @@
+// nrc_train_noalloc: one training step that allocates no device memory.
+//
+// Some callers cannot call cudaMalloc: a renderer that sub-allocates every
+// device buffer from its own heaps (as the reference's Vulkan side does through
+// its allocator), or a process that runs under a fixed device-memory budget
+// imposed before this library is loaded. nrc_create allocates the cache's
+// buffers, so those callers pass their own parameter buffers to this entry
+// point instead, and the one piece of scratch the step needs, the per-CTA
+// weight-gradient partials, lives in a fixed array compiled into the library.
+#include <mutex>
+
+#include "nrc_common.cuh"
+#include "nrc_kernels.h"
+
+namespace {
+
+// One gradient partial per CTA; a CTA handles at most two 128-record tiles, so
+// the array bounds one call at kNoAllocSlots * 256 = 16,384 records.
+constexpr int kNoAllocSlots = 64;
+constexpr uint32_t kNoAllocMaxRecords = kNoAllocSlots * 2 * nrc::kTile;
+constexpr size_t kScratchFloats = size_t(kNoAllocSlots) * nrc::kParams + 64;  // + error word
+
+// Held by every GPU that loads the library until the process exits:
+// 64 x 20,672 x 4 B + 256 B = 5,292,288 bytes.
+static __device__ __align__(256) float g_noalloc_scratch[kScratchFloats];
+
+struct DeviceSetup {
+  bool ready = false;
+  int status = NRC_OK;
+  float* scratch = nullptr;  // device address of g_noalloc_scratch on that device
+  int num_sms = 0;
+};
+
+std::mutex g_setup_mutex;
+DeviceSetup g_setup[64];
+
+// Once per device, with that device current: check the architecture, raise the
+// kernels' shared-memory limit and resolve the scratch array's device address.
+// In host code the array's name only stands for the symbol; a kernel must be
+// given the address that cudaGetSymbolAddress returns.
+int setup_current_device(DeviceSetup** out) {
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return NRC_ERROR_NO_DEVICE;
+  if (dev >= 64) return NRC_ERROR_UNSUPPORTED_DEVICE;
+  std::lock_guard<std::mutex> lock(g_setup_mutex);
+  DeviceSetup& s = g_setup[dev];
+  if (!s.ready) {
+    int major = 0, minor = 0, sms = 0;
+    if (cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+      s.status = NRC_ERROR_CUDA;
+    } else if (!(major == 10 && minor == 3)) {
+      s.status = NRC_ERROR_UNSUPPORTED_DEVICE;
+    } else if (nrc::configure_train_kernels() != cudaSuccess) {
+      s.status = NRC_ERROR_CUDA;
+    } else {
+      void* p = nullptr;
+      const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+      if (e != cudaSuccess || p == nullptr) {
+        s.status = NRC_ERROR_CUDA;
+      } else {
+        s.scratch = static_cast<float*>(p);
+        s.num_sms = sms;
+        s.status = NRC_OK;
+      }
+    }
+    s.ready = true;
+  }
+  *out = &s;
+  return s.status;
+}
+
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+}  // namespace
+
+extern "C" NRC_API int nrc_train_noalloc(uint16_t* d_weights, uint16_t* d_use_weights,
+                                         nrc_optimizer_entry* d_entries, nrc_optimizer_state* d_state,
+                                         const nrc_train_record* d_records, uint32_t* d_count, uint32_t capacity,
+                                         const nrc_config* cfg, uint32_t* d_error, void* stream) {
+  if (cfg == nullptr || d_weights == nullptr || d_entries == nullptr || d_state == nullptr || d_count == nullptr ||
+      (capacity > 0 && d_records == nullptr) || cfg->train_batch_size == 0 || !(cfg->loss_scale != 0.0f))
+    return NRC_ERROR_INVALID_ARGUMENT;
+  if (!aligned16(d_weights) || !aligned16(d_entries) || (d_records && !aligned16(d_records)) ||
+      (d_use_weights && (reinterpret_cast<uintptr_t>(d_use_weights) & 1u)))
+    return NRC_ERROR_MISALIGNED;
+  const uint32_t records = capacity < cfg->train_batch_size ? capacity : cfg->train_batch_size;
+  if (records > kNoAllocMaxRecords) return NRC_ERROR_TOO_LARGE;
+  DeviceSetup* s = nullptr;
+  const int st = setup_current_device(&s);
+  if (st != NRC_OK) return st;
+  cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  uint32_t* err = d_error;
+  if (err == nullptr) {
+    err = reinterpret_cast<uint32_t*>(s->scratch + size_t(kNoAllocSlots) * nrc::kParams);
+    if (cudaMemsetAsync(err, 0, sizeof(uint32_t), cs) != cudaSuccess) return NRC_ERROR_CUDA;
+  }
+  // At most kNoAllocSlots CTAs, one gradient partial each, summed in CTA order.
+  const int max_ctas = s->num_sms < kNoAllocSlots ? s->num_sms : kNoAllocSlots;
+  cudaError_t e = nrc::launch_train_grad(
+      d_records, d_count, capacity, cfg->train_batch_size, reinterpret_cast<const __half*>(d_weights), nullptr,
+      s->scratch, d_state, cfg->loss_scale, cfg->beta1, cfg->beta2, cfg->ema_alpha, true, nullptr, nullptr, err,
+      max_ctas, cs);
+  if (e != cudaSuccess) return NRC_ERROR_CUDA;
+  const uint32_t ctas = nrc::train_grid(capacity, cfg->train_batch_size, max_ctas);
+  e = nrc::launch_adam(d_count, capacity, cfg->train_batch_size, nullptr, s->scratch, ctas, d_entries, d_state,
+                       reinterpret_cast<__half*>(d_weights), reinterpret_cast<__half*>(d_use_weights),
+                       cfg->learning_rate, cfg->beta1, cfg->beta2, cfg->epsilon, cfg->ema_alpha, cfg->loss_scale,
+                       cfg->use_ema_weights != 0, cs);
+  return e == cudaSuccess ? NRC_OK : NRC_ERROR_CUDA;
+}

@@ -22,13 +22,13 @@ TRAIN_BATCH_COUNT = 4
 WEIGHTS_USE, WEIGHTS_TRAIN = 0, 1
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "no CUDA device", 4: "unsupported device",
-          5: "out of device memory", 6: "device timeout", 7: "misaligned buffer"}
+          5: "out of device memory", 6: "device timeout", 7: "misaligned buffer", 8: "too large"}
 
 EXPORTS = [
     "nrc_status_string", "nrc_default_config", "nrc_create", "nrc_destroy", "nrc_reset", "nrc_he_init_host",
     "nrc_encode", "nrc_sph_encode", "nrc_infer", "nrc_infer_encoded", "nrc_train", "nrc_gradient", "nrc_frame",
     "nrc_get_weights", "nrc_set_weights", "nrc_get_optimizer", "nrc_set_optimizer", "nrc_get_loss",
-    "nrc_get_error", "nrc_get_device_buffers",
+    "nrc_get_error", "nrc_get_device_buffers", "nrc_train_noalloc",
 ]
 
 
@@ -89,6 +89,7 @@ def lib(build_if_missing: bool = True) -> ctypes.CDLL:
     L.nrc_set_optimizer.argtypes = [vp, ctypes.POINTER(OptState), vp]
     L.nrc_get_loss.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_uint64)]
     L.nrc_get_error.argtypes = [vp]
+    L.nrc_train_noalloc.argtypes = [vp, vp, vp, vp, vp, vp, u32, ctypes.POINTER(Config), vp, vp]
     L.nrc_get_device_buffers.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp),
                                          ctypes.POINTER(vp)]
     _lib = L
