@@ -50,6 +50,8 @@ def parse_args():
     p.add_argument("--e2e-steps", type=int, default=100)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-plain", action="store_true")
+    p.add_argument("--deterministic", type=int, default=1,
+                   help="1: fixed-order gradient reduction (per-CTA partials); 0: fp32 atomics")
     return p.parse_args()
 
 
@@ -287,16 +289,14 @@ def ours_arm(args, world, rank, local):
 
     stream = torch.cuda.current_stream()
     evals, trains = make_pools(args, rank)
-    cache = Cache(seed=1234 + rank, learning_rate=1e-3, beta1=0.9, beta2=0.99, epsilon=1e-8)
+    cache = Cache(seed=1234 + rank, learning_rate=1e-3, beta1=0.9, beta2=0.99, epsilon=1e-8,
+                  deterministic=args.deterministic)
     out = torch.empty((Q, 3), dtype=torch.float32, device="cuda")
     eval_cnt = torch.tensor([Q], dtype=torch.int32, device="cuda")
     train_cnt = [torch.tensor([R], dtype=torch.int32, device="cuda") for _ in range(B)]
 
     def frame(k, ev=None):
-        cache.infer(evals[k % len(evals)], eval_cnt, out)
-        tb = trains[k % len(trains)]
-        for b in range(B):
-            cache.train(tb[b], train_cnt[b], write_use=(b == B - 1))
+        cache.frame(evals[k % len(evals)], eval_cnt, out, trains[k % len(trains)], train_cnt)
 
     for k in range(args.warmup):
         frame(k)
@@ -313,11 +313,10 @@ def ours_arm(args, world, rank, local):
     t_host0 = time.perf_counter()
     ev_frame[0].record(stream)
     for k in range(K):
+        # nrc_frame = nrc_infer + nrc_train_batches; called apart to time the query kernel
         cache.infer(evals[k % len(evals)], eval_cnt, out)
         ev_inf[k].record(stream)
-        tb = trains[k % len(trains)]
-        for b in range(B):
-            cache.train(tb[b], train_cnt[b], write_use=(b == B - 1))
+        cache.train_batches(trains[k % len(trains)], train_cnt, write_use_last=True)
         ev_frame[k + 1].record(stream)
     torch.cuda.synchronize()
     t_host = time.perf_counter() - t_host0
@@ -346,9 +345,7 @@ def ours_arm(args, world, rank, local):
         d_eval.copy_(h_eval[k % len(h_eval)], non_blocking=True)
         for b in range(B):
             d_train[b].copy_(h_train[k % len(h_train)][b], non_blocking=True)
-        cache.infer(d_eval, eval_cnt, out)
-        for b in range(B):
-            cache.train(d_train[b], train_cnt[b], write_use=(b == B - 1))
+        cache.frame(d_eval, eval_cnt, out, d_train, train_cnt)
         h_out.copy_(out, non_blocking=True)
 
     for k in range(3):
@@ -390,13 +387,14 @@ def ours_arm(args, world, rank, local):
             "records": "seeded synthetic; 4 distinct eval frames (464 MB) and 8 distinct train frames rotated",
             "l2": "inputs larger than L2: each frame's 116 MB of records is cold (4-frame rotation)",
             "hyper": "lr 1e-3, beta 0.9/0.99, eps 1e-8",
+            "gradient_reduction": "deterministic per-CTA partials" if args.deterministic else "fp32 atomics",
             "parallelism": f"replicas x{world}",
         },
         "train_records_per_s": world * B * R * K / total_s,
         "frame_ms": {"p50": statistics.median(frame_ms), "p99": float(np.quantile(frame_ms, 0.99)),
                      "mean": statistics.mean(frame_ms)},
         "infer_ms": {"mean": statistics.mean(infer_ms), "p50": statistics.median(infer_ms)},
-        "gpu_launches": K * (1 + 2 * B),
+        "gpu_launches": K * 2,  # query kernel + one persistent training launch per frame
         "host_s": t_host,
         "roofline": {
             "bound": "tensor", "kernel": "infer_kernel<records> (nrc_infer)",

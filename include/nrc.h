@@ -164,6 +164,14 @@ NRC_API int nrc_infer_encoded(nrc_context* ctx, const uint16_t* d_encoded, const
 NRC_API int nrc_train(nrc_context* ctx, const nrc_train_record* d_records, uint32_t* d_count, uint32_t capacity,
               int write_use_weights, void* stream);
 
+/* The reference's chained train passes of one frame
+ * (src/rg/NRCRenderGraph.cpp:57-80) in one call: nbatches (1..4) training steps
+ * as nrc_train does them, batch b on d_records[b] / d_counts[b], each using the
+ * weights the previous one produced; the last also writes use_weights when
+ * write_use_last != 0. One persistent launch runs all of them. */
+NRC_API int nrc_train_batches(nrc_context* ctx, const nrc_train_record* const* d_records, uint32_t* const* d_counts,
+                              uint32_t capacity, int nbatches, int write_use_last, void* stream);
+
 /* Weight-gradient pass alone (no optimizer step): d_grad receives the
  * NRC_PARAM_COUNT fp32 gradient sums over min(*d_count, capacity) records
  * (the reference's gradients buffer, src/rg/NNTrain.hpp:96-98), computed with

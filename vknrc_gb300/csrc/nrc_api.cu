@@ -2,6 +2,7 @@
 // kernel launches. Host code only; kernels live in nrc_infer.cu, nrc_train.cu
 // and nrc_encode.cu.
 #include <cmath>
+#include <cudaTypedefs.h>
 #include <cstring>
 #include <new>
 #include <random>
@@ -19,12 +20,39 @@ struct nrc_context {
   __half* use16 = nullptr;  // rendering weights (reference: use_weights)
   nrc_optimizer_entry* entries = nullptr;
   nrc_optimizer_state* state = nullptr;
-  float* grad = nullptr;      // atomic gradient accumulator, zero between steps
-  float* partials = nullptr;  // deterministic mode: one gradient vector per CTA
+  float* partials = nullptr;  // one weight-gradient vector per training CTA
+  uint32_t* sync = nullptr;   // grid-barrier counter of the trainer
   uint32_t* err = nullptr;
   double* loss_acc = nullptr;
   unsigned long long* loss_count = nullptr;
+  CUtensorMap map_w16;    // TMA views of the two fp16 weight vectors
+  CUtensorMap map_use16;
 };
+
+namespace nrc {
+
+cudaError_t make_weight_map(CUtensorMap* map, const void* w16) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  if (encode == nullptr) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    const cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+    if (e != cudaSuccess || fn == nullptr || q != cudaDriverEntryPointSuccess) return cudaErrorNotSupported;
+    encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }
+  // 323 rows of 64 fp16 (128-byte rows); boxes of 64 x 16, 128-byte swizzle;
+  // rows past 322 read as zero.
+  const cuuint64_t dims[2] = {static_cast<cuuint64_t>(kWidth), static_cast<cuuint64_t>(kWeightRows)};
+  const cuuint64_t strides[1] = {static_cast<cuuint64_t>(kWidth) * 2};
+  const cuuint32_t box[2] = {static_cast<cuuint32_t>(kWidth), 16};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<void*>(w16), dims, strides, box, estr,
+                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+}  // namespace nrc
 
 namespace {
 
@@ -86,7 +114,6 @@ int upload_init(nrc_context* c, uint64_t seed) {
       cudaSuccess)
     return from_cuda(e);
   if ((e = cudaMemcpy(c->state, &st, sizeof(st), cudaMemcpyHostToDevice)) != cudaSuccess) return from_cuda(e);
-  if ((e = cudaMemset(c->grad, 0, kParams * sizeof(float))) != cudaSuccess) return from_cuda(e);
   return NRC_OK;
 }
 
@@ -167,11 +194,10 @@ int nrc_create(const nrc_config* cfg_in, nrc_context** out) {
   const size_t o_use = o_w16 + up256(kParams * 2);
   const size_t o_ent = o_use + up256(kParams * 2);
   const size_t o_st = o_ent + up256(kParams * sizeof(nrc_optimizer_entry));
-  const size_t o_grad = o_st + up256(sizeof(nrc_optimizer_state));
-  const size_t o_err = o_grad + up256(kParams * sizeof(float));
+  const size_t o_err = o_st + up256(sizeof(nrc_optimizer_state));
   const size_t o_loss = o_err + 256;
   const size_t o_part = o_loss + 256;
-  const size_t part_bytes = cfg.deterministic ? up256(size_t(c->num_sms) * kParams * sizeof(float)) : 0;
+  const size_t part_bytes = up256(size_t(c->num_sms) * kParams * sizeof(float));
   const size_t total = o_part + part_bytes;
   if ((e = cudaMalloc(&c->block, total)) != cudaSuccess) {
     delete c;
@@ -182,12 +208,14 @@ int nrc_create(const nrc_config* cfg_in, nrc_context** out) {
   c->use16 = reinterpret_cast<__half*>(b + o_use);
   c->entries = reinterpret_cast<nrc_optimizer_entry*>(b + o_ent);
   c->state = reinterpret_cast<nrc_optimizer_state*>(b + o_st);
-  c->grad = reinterpret_cast<float*>(b + o_grad);
   c->err = reinterpret_cast<uint32_t*>(b + o_err);
   c->loss_acc = reinterpret_cast<double*>(b + o_loss);
   c->loss_count = reinterpret_cast<unsigned long long*>(b + o_loss + 8);
-  c->partials = cfg.deterministic ? reinterpret_cast<float*>(b + o_part) : nullptr;
-  if ((e = cudaMemset(c->err, 0, 256 + 256)) != cudaSuccess) {
+  c->sync = reinterpret_cast<uint32_t*>(b + o_err + 64);
+  c->partials = reinterpret_cast<float*>(b + o_part);
+  if ((e = nrc::make_weight_map(&c->map_w16, c->w16)) != cudaSuccess ||
+      (e = nrc::make_weight_map(&c->map_use16, c->use16)) != cudaSuccess ||
+      (e = cudaMemset(c->err, 0, 256 + 256)) != cudaSuccess) {
     cudaFree(c->block);
     delete c;
     return from_cuda(e);
@@ -250,6 +278,10 @@ static const __half* weights_of(nrc_context* c, int which) {
   return which == NRC_WEIGHTS_TRAIN ? c->w16 : c->use16;
 }
 
+static const CUtensorMap* weight_map_of(nrc_context* c, int which) {
+  return which == NRC_WEIGHTS_TRAIN ? &c->map_w16 : &c->map_use16;
+}
+
 int nrc_infer(nrc_context* c, const nrc_input* in, const uint32_t* d_count, uint32_t capacity, float* out,
               int weight_set, void* stream) {
   int s = check_ctx(c);
@@ -258,7 +290,7 @@ int nrc_infer(nrc_context* c, const nrc_input* in, const uint32_t* d_count, uint
   if (capacity == 0) return NRC_OK;
   if (in == nullptr || d_count == nullptr || out == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
   if (!aligned16(in) || (reinterpret_cast<uintptr_t>(out) & 3u)) return NRC_ERROR_MISALIGNED;
-  return from_cuda(nrc::launch_infer(in, false, d_count, capacity, weights_of(c, weight_set), out, true, c->err,
+  return from_cuda(nrc::launch_infer(in, false, d_count, capacity, weight_map_of(c, weight_set), out, true, c->err,
                                      c->num_sms, static_cast<cudaStream_t>(stream)));
 }
 
@@ -270,23 +302,33 @@ int nrc_infer_encoded(nrc_context* c, const uint16_t* enc, const uint32_t* d_cou
   if (capacity == 0) return NRC_OK;
   if (enc == nullptr || d_count == nullptr || out == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
   if (!aligned16(enc) || (reinterpret_cast<uintptr_t>(out) & 3u)) return NRC_ERROR_MISALIGNED;
-  return from_cuda(nrc::launch_infer(enc, true, d_count, capacity, weights_of(c, weight_set), out, false, c->err,
+  return from_cuda(nrc::launch_infer(enc, true, d_count, capacity, weight_map_of(c, weight_set), out, false, c->err,
                                      c->num_sms, static_cast<cudaStream_t>(stream)));
 }
 
-static int train_step(nrc_context* c, const nrc_train_record* rec, uint32_t* d_count, uint32_t capacity,
-                      bool write_use, cudaStream_t st) {
+static nrc::TrainParams train_params(nrc_context* c, int steps, int mode) {
   const nrc_config& g = c->cfg;
-  cudaError_t e = nrc::launch_train_grad(rec, d_count, capacity, g.train_batch_size, c->w16, c->grad, c->partials,
-                                         c->state, g.loss_scale, g.beta1, g.beta2, g.ema_alpha, true,
-                                         g.track_loss ? c->loss_acc : nullptr,
-                                         g.track_loss ? c->loss_count : nullptr, c->err, c->num_sms, st);
-  if (e != cudaSuccess) return from_cuda(e);
-  const uint32_t grad_ctas = nrc::train_grid(capacity, g.train_batch_size, c->num_sms);
-  e = nrc::launch_adam(d_count, capacity, g.train_batch_size, c->grad, c->partials, grad_ctas, c->entries, c->state,
-                       c->w16, write_use ? c->use16 : nullptr, g.learning_rate, g.beta1, g.beta2, g.epsilon,
-                       g.ema_alpha, g.loss_scale, g.use_ema_weights != 0, st);
-  return from_cuda(e);
+  nrc::TrainParams p = {};
+  p.steps = steps;
+  p.mode = mode;
+  p.batch_cap = mode == nrc::kTrainStep ? g.train_batch_size : 0xFFFFFFFFu;
+  p.lr = g.learning_rate;
+  p.beta1 = g.beta1;
+  p.beta2 = g.beta2;
+  p.eps = g.epsilon;
+  p.ema_alpha = g.ema_alpha;
+  p.loss_scale = g.loss_scale;
+  p.use_ema = g.use_ema_weights != 0;
+  p.entries = c->entries;
+  p.state = c->state;
+  p.w16 = c->w16;
+  p.use16 = c->use16;
+  p.partials = c->partials;
+  p.sync = c->sync;
+  p.loss_acc = (g.track_loss && mode == nrc::kTrainStep) ? c->loss_acc : nullptr;
+  p.loss_count = (g.track_loss && mode == nrc::kTrainStep) ? c->loss_count : nullptr;
+  p.err = c->err;
+  return p;
 }
 
 int nrc_train(nrc_context* c, const nrc_train_record* rec, uint32_t* d_count, uint32_t capacity,
@@ -295,7 +337,9 @@ int nrc_train(nrc_context* c, const nrc_train_record* rec, uint32_t* d_count, ui
   if (s != NRC_OK) return s;
   if (d_count == nullptr || (capacity > 0 && rec == nullptr)) return NRC_ERROR_INVALID_ARGUMENT;
   if (rec != nullptr && !aligned16(rec)) return NRC_ERROR_MISALIGNED;
-  return train_step(c, rec, d_count, capacity, write_use_weights != 0, static_cast<cudaStream_t>(stream));
+  nrc::TrainParams p = train_params(c, 1, nrc::kTrainStep);
+  p.batch[0] = nrc::TrainBatch{rec, d_count, capacity, write_use_weights != 0};
+  return from_cuda(nrc::launch_train(p, &c->map_w16, c->num_sms, static_cast<cudaStream_t>(stream)));
 }
 
 int nrc_gradient(nrc_context* c, const nrc_train_record* rec, const uint32_t* d_count, uint32_t capacity,
@@ -304,15 +348,28 @@ int nrc_gradient(nrc_context* c, const nrc_train_record* rec, const uint32_t* d_
   if (s != NRC_OK) return s;
   if (d_count == nullptr || d_grad == nullptr || (capacity > 0 && rec == nullptr)) return NRC_ERROR_INVALID_ARGUMENT;
   if ((rec != nullptr && !aligned16(rec)) || !aligned16(d_grad)) return NRC_ERROR_MISALIGNED;
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
-  // the reference clears its gradient buffer before the pass (src/rg/NNTrain.hpp:96-98)
-  cudaError_t e = cudaMemsetAsync(d_grad, 0, kParams * sizeof(float), st);
-  if (e != cudaSuccess) return from_cuda(e);
-  if (capacity == 0) return NRC_OK;
-  e = nrc::launch_train_grad(rec, const_cast<uint32_t*>(d_count), capacity, 0xFFFFFFFFu, c->w16, d_grad, nullptr,
-                             c->state, c->cfg.loss_scale, c->cfg.beta1, c->cfg.beta2, c->cfg.ema_alpha, false, nullptr,
-                             nullptr, c->err, c->num_sms, st);
-  return from_cuda(e);
+  // The whole gradient vector is written (zero for an empty batch), as the
+  // reference's cleared gradient buffer would read (src/rg/NNTrain.hpp:96-98).
+  nrc::TrainParams p = train_params(c, 1, nrc::kGradientOnly);
+  p.batch[0] = nrc::TrainBatch{rec, const_cast<uint32_t*>(d_count), capacity, 0};
+  p.grad_out = d_grad;
+  return from_cuda(nrc::launch_train(p, &c->map_w16, c->num_sms, static_cast<cudaStream_t>(stream)));
+}
+
+int nrc_train_batches(nrc_context* c, const nrc_train_record* const* recs, uint32_t* const* counts, uint32_t capacity,
+                      int nbatches, int write_use_last, void* stream) {
+  int s = check_ctx(c);
+  if (s != NRC_OK) return s;
+  if (recs == nullptr || counts == nullptr || nbatches < 1 || nbatches > NRC_TRAIN_BATCH_COUNT)
+    return NRC_ERROR_INVALID_ARGUMENT;
+  for (int b = 0; b < nbatches; ++b) {
+    if (counts[b] == nullptr || (capacity > 0 && recs[b] == nullptr)) return NRC_ERROR_INVALID_ARGUMENT;
+    if (recs[b] != nullptr && !aligned16(recs[b])) return NRC_ERROR_MISALIGNED;
+  }
+  nrc::TrainParams p = train_params(c, nbatches, nrc::kTrainStep);
+  for (int b = 0; b < nbatches; ++b)
+    p.batch[b] = nrc::TrainBatch{recs[b], counts[b], capacity, (write_use_last != 0 && b == nbatches - 1) ? 1 : 0};
+  return from_cuda(nrc::launch_train(p, &c->map_w16, c->num_sms, static_cast<cudaStream_t>(stream)));
 }
 
 int nrc_frame(nrc_context* c, const nrc_input* eval_in, const uint32_t* d_eval_count, uint32_t eval_capacity,
@@ -323,11 +380,7 @@ int nrc_frame(nrc_context* c, const nrc_input* eval_in, const uint32_t* d_eval_c
   if (train_rec == nullptr || train_counts == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
   s = nrc_infer(c, eval_in, d_eval_count, eval_capacity, out, NRC_WEIGHTS_USE, stream);
   if (s != NRC_OK) return s;
-  for (int b = 0; b < NRC_TRAIN_BATCH_COUNT; ++b) {
-    s = nrc_train(c, train_rec[b], train_counts[b], train_capacity, b == NRC_TRAIN_BATCH_COUNT - 1, stream);
-    if (s != NRC_OK) return s;
-  }
-  return NRC_OK;
+  return nrc_train_batches(c, train_rec, train_counts, train_capacity, NRC_TRAIN_BATCH_COUNT, 1, stream);
 }
 
 int nrc_get_weights(nrc_context* c, int which, uint16_t* host) {

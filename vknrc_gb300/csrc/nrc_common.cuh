@@ -1,8 +1,9 @@
 // Shared constants and device code for the neural-radiance-cache kernels:
-// record layouts, the fp32 input encoding, and the weight staging into
+// record layouts, the fp32 input encoding, and the weight staging (TMA) into
 // shared memory in the tensor-core operand layout.
 #pragma once
 #include <cstdint>
+#include <cuda.h>
 #include <cuda_fp16.h>
 
 #include "../../include/nrc.h"
@@ -28,25 +29,24 @@ static_assert(sizeof(nrc_train_record) == kTrainFloats * 4, "nrc_train_record la
 // output layer as 16 rows (3 real, 13 zero) x 128 B.
 constexpr uint32_t kWeightSmemBytes = kHidden * 8192 + kOutPad * 128;
 
-// Copy the fp16 parameter vector (reference layout: layer l row-major [out][in] at
-// l*4096; output layer [3][64] at 5*4096) into shared memory as 128-byte-swizzled
-// K-major tiles: layer l at smem_w + l*8192, output layer at smem_w + 5*8192.
-__device__ __forceinline__ void stage_weights(uint8_t* smem_w, const __half* __restrict__ w16) {
-  constexpr int kHiddenChunks = kHidden * kWidth * 8;  // 16-byte chunks
-  constexpr int kOutChunks = kOutPad * 8;
-  const uint4* src = reinterpret_cast<const uint4*>(w16);
-  for (int idx = threadIdx.x; idx < kHiddenChunks + kOutChunks; idx += blockDim.x) {
-    if (idx < kHiddenChunks) {
-      const int l = idx >> 9, row = (idx >> 3) & 63, c = idx & 7;
-      const uint4 v = __ldg(src + idx);  // (l*4096 + row*64 + c*8) / 8 == idx
-      *reinterpret_cast<uint4*>(smem_w + l * 8192 + sw128_offset(row, c)) = v;
-    } else {
-      const int j = idx - kHiddenChunks, row = j >> 3, c = j & 7;
-      uint4 v = make_uint4(0, 0, 0, 0);
-      if (row < kOut) v = __ldg(src + (kHidden * kLayerElems) / 8 + row * 8 + c);
-      *reinterpret_cast<uint4*>(smem_w + kHidden * 8192 + sw128_offset(row, c)) = v;
-    }
-  }
+// Weight staging by TMA. The parameter vector is viewed as a 2-D tensor of
+// 323 rows x 64 fp16 (row r = output row r%64 of layer r/64; rows 320..322 are
+// the output layer) with the 128-byte swizzle; 21 boxes of 16 rows land as the
+// same swizzled K-major tiles as stage_weights() writes. The last box covers
+// rows 320..335, and the tensor map zero-fills rows 323..335: the output
+// layer's padding to 16 rows (NN_nv.glsl:77-82). One thread issues; `bar`
+// completes when all 43,008 bytes have landed.
+constexpr int kWeightRows = kHidden * kWidth + kOut;  // 323
+constexpr uint32_t kWeightTmaBytes = (kHidden * 4 + 1) * 16 * 128;
+static_assert(kWeightTmaBytes == kWeightSmemBytes, "weight staging size");
+
+__device__ __forceinline__ void stage_weights_tma(uint8_t* smem_w, const CUtensorMap* map, uint64_t* bar) {
+  mbar_arrive_expect_tx(bar, kWeightTmaBytes);
+#pragma unroll
+  for (int l = 0; l < kHidden; ++l)
+#pragma unroll
+    for (int k = 0; k < 4; ++k) tma_load_2d(smem_w + l * 8192 + k * 2048, map, 0, l * kWidth + k * 16, bar);
+  tma_load_2d(smem_w + kHidden * 8192, map, 0, kHidden * kWidth, bar);
 }
 
 // ------------------------------------------------------------- encoding --
@@ -99,29 +99,46 @@ __device__ __forceinline__ float enc_expf(float x) {
   return __fmul_rn(p, s);
 }
 
-// Frequency encoding of one coordinate: 12 features -> 6 words.
-__device__ __forceinline__ void enc_freq12(float p, uint32_t* o) {
+// Frequency features k0 .. k0+2n-1 of one coordinate -> n words.
+template <int K0, int N>
+__device__ __forceinline__ void enc_freq(float p, uint32_t* o) {
 #pragma unroll
-  for (int k = 0; k < 12; k += 2) {
-    o[k / 2] = pack_f16x2(enc_tri(p, static_cast<float>(1 << k)), enc_tri(p, static_cast<float>(1 << (k + 1))));
+  for (int i = 0; i < N; ++i) {
+    constexpr int kBase = K0;
+    o[i] = pack_f16x2(enc_tri(p, static_cast<float>(1 << (kBase + 2 * i))),
+                      enc_tri(p, static_cast<float>(1 << (kBase + 2 * i + 1))));
   }
 }
 
-// NRCInputEncode (NRCRecord.glsl:78-95): 14 fp32 -> 64 fp16 as 32 words
-// (feature 2j in the low half of word j).
+// NRCInputEncode (NRCRecord.glsl:78-95) split at feature 32, a 16-byte chunk
+// boundary of the 128-byte row, so two threads can encode one record:
+// features 0..31 = pos.x and pos.y frequencies, pos.z frequencies 0..7;
+// features 32..63 = pos.z frequencies 8..11, the five one-blob groups, diffuse,
+// specular and the two constant ones. Word j holds features 2j (low half) and
+// 2j+1 of its half.
+__device__ __forceinline__ void encode_half0(const float (&r)[kInFloats], uint32_t* e) {
+  enc_freq<0, 6>(r[0], e + 0);
+  enc_freq<0, 6>(r[1], e + 6);
+  enc_freq<0, 4>(r[2], e + 12);
+}
+
+__device__ __forceinline__ void encode_half1(const float (&r)[kInFloats], uint32_t* e) {
+  enc_freq<8, 2>(r[2], e + 0);
+  enc_oneblob4(r[3], e[2], e[3]);
+  enc_oneblob4(r[4], e[4], e[5]);
+  enc_oneblob4(r[5], e[6], e[7]);
+  enc_oneblob4(r[6], e[8], e[9]);
+  enc_oneblob4(__fsub_rn(1.0f, enc_expf(-r[7])), e[10], e[11]);
+  e[12] = pack_f16x2(r[8], r[9]);
+  e[13] = pack_f16x2(r[10], r[11]);
+  e[14] = pack_f16x2(r[12], r[13]);
+  e[15] = pack_f16x2(1.0f, 1.0f);
+}
+
+// The whole record: 14 fp32 -> 64 fp16 as 32 words.
 __device__ __forceinline__ void encode_input(const float (&r)[kInFloats], uint32_t (&e)[32]) {
-  enc_freq12(r[0], e + 0);
-  enc_freq12(r[1], e + 6);
-  enc_freq12(r[2], e + 12);
-  enc_oneblob4(r[3], e[18], e[19]);
-  enc_oneblob4(r[4], e[20], e[21]);
-  enc_oneblob4(r[5], e[22], e[23]);
-  enc_oneblob4(r[6], e[24], e[25]);
-  enc_oneblob4(__fsub_rn(1.0f, enc_expf(-r[7])), e[26], e[27]);
-  e[28] = pack_f16x2(r[8], r[9]);
-  e[29] = pack_f16x2(r[10], r[11]);
-  e[30] = pack_f16x2(r[12], r[13]);
-  e[31] = pack_f16x2(1.0f, 1.0f);
+  encode_half0(r, e);
+  encode_half1(r, e + 16);
 }
 
 // Device-side error word bits (read back by nrc_get_error).

@@ -4,8 +4,8 @@
 // Follows shader/src/nrc_inference.comp:30-48 with NN_nv.glsl's forward
 // (NNLoadInput :84-97, NNForward64_ReLU :99-127, NNForward3/NNOutput3 :129-158),
 // re-laid out for tcgen05:
-//   - the 42 KB of fp16 weights are staged once per CTA into shared memory as
-//     128-byte-swizzled K-major tiles (the MMA's B operand);
+//   - the 42 KB of fp16 weights are staged once per CTA by TMA (tensor map,
+//     128-byte swizzle) into shared memory as K-major tiles (the MMA's B operand);
 //   - activations never leave the SM: each layer's fp16 input sits in tensor
 //     memory as the MMA's A operand (32 columns), its fp32 result lands in
 //     tensor memory (64 columns), and the epilogue threads convert it (ReLU +
@@ -39,7 +39,7 @@ struct SlotBars {
   uint64_t a_ready;       // 128 arrivals: A operand in TMEM for the next layer
   uint64_t d_ready;       // MMA commit: accumulator ready
 };
-static_assert(sizeof(SlotBars) * kSlots + 16 <= 512, "barrier area");
+static_assert(sizeof(SlotBars) * kSlots + 16 <= 512, "barrier area (+ weight barrier, TMEM slot)");
 
 __device__ __forceinline__ uint8_t* align1024(uint8_t* p) {
   return reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(p) + 1023) & ~uintptr_t(1023));
@@ -75,17 +75,16 @@ __device__ __forceinline__ void issue_layer(uint32_t d, uint32_t a, uint64_t bde
 template <bool kEncoded>
 __global__ void __launch_bounds__(kInferThreads, 1)
     infer_kernel(const void* __restrict__ input, const uint32_t* __restrict__ d_count, uint32_t capacity,
-                 const __half* __restrict__ w16, float* __restrict__ out, int clamp_out, uint32_t* err) {
+                 const __grid_constant__ CUtensorMap wmap, float* __restrict__ out, int clamp_out, uint32_t* err) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
   uint8_t* smem_w = smem;
   uint8_t* smem_rec = smem + kRecSmemOff;
   SlotBars* bars = reinterpret_cast<SlotBars*>(smem + kBarOff);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + kSlots);
+  uint64_t* w_full = reinterpret_cast<uint64_t*>(bars + kSlots);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(w_full + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const uint32_t n = min(*d_count, capacity);
-  const uint32_t num_tiles = (n + kTile - 1) / kTile;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kSlots; ++s) {
@@ -96,14 +95,19 @@ __global__ void __launch_bounds__(kInferThreads, 1)
       mbar_init(&bars[s].a_ready, 128);
       mbar_init(&bars[s].d_ready, 1);
     }
+    mbar_init(w_full, 1);
     mbar_fence_init();
   }
+  // Everything below may read what the preceding kernel in the stream wrote.
+  griddep_wait();
+  griddep_launch_dependents();
+  const uint32_t n = min(*d_count, capacity);
+  const uint32_t num_tiles = (n + kTile - 1) / kTile;
   if (warp == 0) {
     tmem_alloc(tmem_slot, 512);
     tmem_relinquish();
   }
-  stage_weights(smem_w, w16);
-  fence_proxy_async_smem();
+  if (threadIdx.x == 0) stage_weights_tma(smem_w, &wmap, w_full);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
@@ -130,6 +134,7 @@ __global__ void __launch_bounds__(kInferThreads, 1)
   }
   bool ok = true;
   uint32_t ph_d = 0, ph_a = 0;
+  if (issuer) ok = warp_all(mbar_wait(w_full, 0, kWaitLimitNs));  // before this slot's first MMA
   for (uint32_t it = 0; ok; ++it) {
     const uint32_t tile = tile_of(it);
     if (tile >= num_tiles) break;
@@ -258,19 +263,25 @@ int infer_threads() { return kInferThreads; }
 int infer_tiles_per_cta() { return kSlots; }
 
 cudaError_t launch_infer(const void* input, bool encoded, const uint32_t* d_count, uint32_t capacity,
-                         const __half* w16, float* out, bool clamp_out, uint32_t* err, int num_sms,
+                         const CUtensorMap* wmap, float* out, bool clamp_out, uint32_t* err, int num_sms,
                          cudaStream_t stream) {
   const uint32_t tiles = (capacity + kTile - 1) / kTile;
   const uint32_t want = (tiles + kSlots - 1) / kSlots;
   const uint32_t grid = want < static_cast<uint32_t>(num_sms) ? want : static_cast<uint32_t>(num_sms);
   if (grid == 0) return cudaSuccess;
-  if (encoded)
-    infer_kernel<true><<<grid, kInferThreads, kSmemBytes, stream>>>(input, d_count, capacity, w16, out, clamp_out,
-                                                                     err);
-  else
-    infer_kernel<false><<<grid, kInferThreads, kSmemBytes, stream>>>(input, d_count, capacity, w16, out, clamp_out,
-                                                                      err);
-  return cudaGetLastError();
+  cudaLaunchAttribute attr;
+  attr.id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr.val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(kInferThreads);
+  cfg.dynamicSmemBytes = kSmemBytes;
+  cfg.stream = stream;
+  cfg.attrs = &attr;
+  cfg.numAttrs = 1;
+  const int clamp = clamp_out ? 1 : 0;
+  if (encoded) return cudaLaunchKernelEx(&cfg, infer_kernel<true>, input, d_count, capacity, *wmap, out, clamp, err);
+  return cudaLaunchKernelEx(&cfg, infer_kernel<false>, input, d_count, capacity, *wmap, out, clamp, err);
 }
 
 }  // namespace nrc

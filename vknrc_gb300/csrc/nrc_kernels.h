@@ -1,6 +1,7 @@
 // Kernel launchers shared between the kernel translation units and the C ABI.
 #pragma once
 #include <cstdint>
+#include <cuda.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
@@ -8,27 +9,55 @@
 
 namespace nrc {
 
+// Tensor map over an fp16 parameter vector (323 rows x 64, 128-byte swizzle,
+// 64 x 16 boxes) for stage_weights_tma(). Host only; allocates nothing.
+cudaError_t make_weight_map(CUtensorMap* map, const void* w16);
+
 cudaError_t configure_infer_kernels();
 cudaError_t configure_train_kernels();
 uint32_t infer_smem_bytes();
 int infer_threads();
 int infer_tiles_per_cta();
 cudaError_t launch_infer(const void* input, bool encoded, const uint32_t* d_count, uint32_t capacity,
-                         const __half* w16, float* out, bool clamp_out, uint32_t* err, int num_sms,
+                         const CUtensorMap* wmap, float* out, bool clamp_out, uint32_t* err, int num_sms,
                          cudaStream_t stream);
 
+// One launch of the persistent trainer: up to NRC_TRAIN_BATCH_COUNT chained
+// batches, each a fused gradient pass followed by the optimizer step (mode
+// kTrainStep), or one gradient pass whose fixed-order sum is written to
+// grad_out (kGradientOnly).
+constexpr int kTrainStep = 0;
+constexpr int kGradientOnly = 1;
+
+struct TrainBatch {
+  const nrc_train_record* records;
+  uint32_t* d_count;
+  uint32_t capacity;
+  int write_use;  // the optimizer step also writes use_weights
+};
+
+struct TrainParams {
+  TrainBatch batch[NRC_TRAIN_BATCH_COUNT];
+  int steps;
+  int mode;
+  uint32_t batch_cap;
+  float lr, beta1, beta2, eps, ema_alpha, loss_scale;
+  int use_ema;
+  nrc_optimizer_entry* entries;
+  nrc_optimizer_state* state;
+  __half* w16;
+  __half* use16;
+  float* partials;   // one gradient vector per CTA (grid <= the slots given)
+  float* grad_out;   // kGradientOnly
+  uint32_t* sync;    // grid-barrier counter (zeroed by launch_train)
+  double* loss_acc;  // optional check-path loss sum
+  unsigned long long* loss_count;
+  uint32_t* err;
+};
+
 uint32_t train_smem_bytes();
-uint32_t train_grid(uint32_t capacity, uint32_t batch_cap, int num_sms);
-cudaError_t launch_train_grad(const nrc_train_record* records, uint32_t* d_count, uint32_t capacity,
-                              uint32_t batch_cap, const __half* w16, float* grad, float* partials,
-                              nrc_optimizer_state* state, float loss_scale, float beta1, float beta2,
-                              float ema_alpha, bool do_prepare, double* loss_acc, unsigned long long* loss_count,
-                              uint32_t* err, int num_sms, cudaStream_t stream);
-cudaError_t launch_adam(const uint32_t* d_count, uint32_t capacity, uint32_t batch_cap, float* grad,
-                        const float* partials, uint32_t grad_ctas, nrc_optimizer_entry* entries,
-                        const nrc_optimizer_state* state, __half* w16, __half* use16, float lr, float beta1,
-                        float beta2, float eps, float ema_alpha, float loss_scale, bool use_ema,
-                        cudaStream_t stream);
+uint32_t train_grid(const TrainParams& p, int max_ctas);
+cudaError_t launch_train(const TrainParams& p, const CUtensorMap* wmap, int max_ctas, cudaStream_t stream);
 
 cudaError_t launch_encode(const nrc_input* in, const uint32_t* d_count, uint32_t capacity, uint16_t* out,
                           int num_sms, cudaStream_t stream);

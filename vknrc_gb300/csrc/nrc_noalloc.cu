@@ -18,7 +18,7 @@ namespace {
 // the array bounds one call at kNoAllocSlots * 256 = 16,384 records.
 constexpr int kNoAllocSlots = 64;
 constexpr uint32_t kNoAllocMaxRecords = kNoAllocSlots * 2 * nrc::kTile;
-constexpr size_t kScratchFloats = size_t(kNoAllocSlots) * nrc::kParams + 64;  // + error word
+constexpr size_t kScratchFloats = size_t(kNoAllocSlots) * nrc::kParams + 64;  // + error word, barrier counter
 
 // Held by every GPU that loads the library until the process exits:
 // 64 x 20,672 x 4 B + 256 B = 5,292,288 bytes.
@@ -98,15 +98,27 @@ extern "C" NRC_API int nrc_train_noalloc(uint16_t* d_weights, uint16_t* d_use_we
   }
   // At most kNoAllocSlots CTAs, one gradient partial each, summed in CTA order.
   const int max_ctas = s->num_sms < kNoAllocSlots ? s->num_sms : kNoAllocSlots;
-  cudaError_t e = nrc::launch_train_grad(
-      d_records, d_count, capacity, cfg->train_batch_size, reinterpret_cast<const __half*>(d_weights), nullptr,
-      s->scratch, d_state, cfg->loss_scale, cfg->beta1, cfg->beta2, cfg->ema_alpha, true, nullptr, nullptr, err,
-      max_ctas, cs);
-  if (e != cudaSuccess) return NRC_ERROR_CUDA;
-  const uint32_t ctas = nrc::train_grid(capacity, cfg->train_batch_size, max_ctas);
-  e = nrc::launch_adam(d_count, capacity, cfg->train_batch_size, nullptr, s->scratch, ctas, d_entries, d_state,
-                       reinterpret_cast<__half*>(d_weights), reinterpret_cast<__half*>(d_use_weights),
-                       cfg->learning_rate, cfg->beta1, cfg->beta2, cfg->epsilon, cfg->ema_alpha, cfg->loss_scale,
-                       cfg->use_ema_weights != 0, cs);
+  CUtensorMap wmap;  // host-side descriptor of the caller's weights; no device memory
+  if (nrc::make_weight_map(&wmap, d_weights) != cudaSuccess) return NRC_ERROR_CUDA;
+  nrc::TrainParams p = {};
+  p.steps = 1;
+  p.mode = nrc::kTrainStep;
+  p.batch[0] = nrc::TrainBatch{d_records, d_count, capacity, d_use_weights != nullptr};
+  p.batch_cap = cfg->train_batch_size;
+  p.lr = cfg->learning_rate;
+  p.beta1 = cfg->beta1;
+  p.beta2 = cfg->beta2;
+  p.eps = cfg->epsilon;
+  p.ema_alpha = cfg->ema_alpha;
+  p.loss_scale = cfg->loss_scale;
+  p.use_ema = cfg->use_ema_weights != 0;
+  p.entries = d_entries;
+  p.state = d_state;
+  p.w16 = reinterpret_cast<__half*>(d_weights);
+  p.use16 = reinterpret_cast<__half*>(d_use_weights);
+  p.partials = s->scratch;
+  p.sync = reinterpret_cast<uint32_t*>(s->scratch + size_t(kNoAllocSlots) * nrc::kParams) + 16;
+  p.err = err;
+  const cudaError_t e = nrc::launch_train(p, &wmap, max_ctas, cs);
   return e == cudaSuccess ? NRC_OK : NRC_ERROR_CUDA;
 }

@@ -1,24 +1,36 @@
-// Fused training step: record tile (bulk copy) -> encode -> forward keeping all
-// six activations -> relative-L2 loss gradient -> backward -> weight gradients,
-// then the Adam/EMA update.
+// Fused training: for each of up to four chained batches, record tiles (bulk
+// copy) -> encode -> forward keeping all six activations -> relative-L2 loss
+// gradient -> backward -> weight gradients, then the Adam/EMA update, all in
+// one persistent cooperative kernel.
 //
 // Follows shader/src/nrc_gradient.comp:26-58 with NN_nv.glsl's backward
 // (NNLoadDA3_RelativeL2LuminanceLoss :178-196, NNBackwardDA3/64_ReLU :222-278,
 // NNUpdateDW3/64 :280-367), nrc_train_prepare.comp:16-29 and
-// nrc_optimize.comp:32-54, re-laid out for tcgen05:
+// nrc_optimize.comp:32-54, and the chaining of the four train passes of one
+// frame (src/rg/NRCRenderGraph.cpp:57-80), re-laid out for tcgen05:
+//   - the weights arrive by TMA (tensor map, 128-byte swizzle) as the MMA's B
+//     operand tiles, again after every optimizer step;
 //   - activations act_0..act_5 (fp16, 128 x 64 per tile) stay in shared memory
-//     as 128-byte-swizzled rows; the same tile is the K-major A operand of the
-//     next forward layer and the MN-major B operand of that layer's weight
-//     gradient, so nothing is transposed or copied;
+//     as 128-byte-swizzled rows and serve as the MN-major B operand of each
+//     layer's weight gradient; the forward and dA MMAs take their A operand
+//     (act_l, or the gradient g_{l+1}) from tensor memory, where the epilogue
+//     writes it beside the shared-memory copy (the shared-memory form would be
+//     bound by shared-memory bandwidth at this width);
 //   - dA = (g W) masked by act > 0 uses the weight tile itself as an MN-major B
-//     operand (the reference's NaN-mask trick becomes a select in the epilogue);
+//     operand (the reference's NaN-mask trick becomes a bit mask on packed
+//     halves); it is issued before the layer's weight-gradient MMAs so the
+//     epilogue, which needs only dA, is not held up by them;
 //   - dW_l += g^T act_l is an M=64 MMA (K = records) accumulated in TMEM across
-//     every tile the CTA processes, so the cross-CTA reduction happens once per
-//     CTA: fp32 vector atomics, or per-CTA partials summed in a fixed order by
-//     the optimizer kernel (deterministic mode);
-//   - the count clamp and step-state advance (the reference's prepare pass) run
-//     in CTA 0 of the gradient kernel; the optimizer kernel zeroes the gradient
-//     accumulator after reading it, replacing the reference's clear pass.
+//     the CTA's tiles of a batch; on its last tile each layer's dW is written
+//     to the CTA's slot of a per-CTA partial-gradient array as soon as it is
+//     final, overlapping that write with the rest of the backward chain;
+//   - a grid-wide barrier (cooperative launch, bounded waits) then lets every
+//     CTA update one slice of the parameters: it sums the partials of its slice
+//     in CTA order (run-to-run identical) and applies Adam + EMA; a second
+//     barrier publishes the new weights, which the next batch reloads by TMA.
+//     The reference's prepare pass (count clamp, step state) runs in CTA 0.
+//   - the epilogue runs on eight warps: the two warps that share a TMEM lane
+//     quadrant split each 64-wide row between them.
 #include "nrc_common.cuh"
 #include "nrc_kernels.h"
 
@@ -26,7 +38,9 @@ namespace nrc {
 
 namespace {
 
-constexpr int kTrainThreads = 32 + 128;
+constexpr int kEpiWarps = 8;
+constexpr int kEpiThreads = kEpiWarps * 32;
+constexpr int kTrainThreads = 32 + kEpiThreads;
 constexpr uint32_t kTRecBytes = sizeof(nrc_train_record);  // 80
 constexpr uint32_t kTRecTileBytes = kTile * kTRecBytes;     // 10240
 constexpr uint32_t kActBytes = kTile * 128;                 // 16384: 128 rows x 64 fp16
@@ -38,17 +52,29 @@ constexpr uint32_t kTrainSmemBytes = kTBarOff + 128 + 1024;
 static_assert(kActOff % 1024 == 0 && kGOff % 1024 == 0 && kStageOff % 16 == 0, "alignment");
 static_assert(kTrainSmemBytes <= 227 * 1024, "shared memory");
 
-// TMEM columns: dW_l accumulators (M=64 layout) at 64*l, l = 0..5; scratch D at 384.
+// TMEM columns: dW_l accumulators (M=64 layout) at 64*l, l = 0..5; scratch D at
+// 384..447; the A operand of the forward / dA MMAs (fp16 pairs) at 448..479.
 constexpr uint32_t kDCol = 384;
+constexpr uint32_t kACol = 448;
+
+// Parameter slices of the optimizer phase: float4 columns of the gradient.
+constexpr int kCols4 = kParams / 4;  // 5168
+constexpr uint32_t kMaxTrainCtas = 160;  // bounds the staged gradient slice (slice x CTAs <= kCols4 + grid)
+static_assert(kParams % 4 == 0, "parameters in float4 columns");
 
 struct TrainBars {
   uint64_t rec_full[2];
   uint64_t rec_empty[2];
-  uint64_t a_ready;    // 128 arrivals: the next operand tile is in shared memory
+  uint64_t a_ready;    // 256 arrivals: the next operand rows are in shared memory / TMEM
   uint64_t d_ready;    // MMA commit: scratch accumulator ready
   uint64_t tile_done;  // MMA commit after the tile's last weight-gradient MMA
   uint64_t drain;
+  uint64_t w_full;     // weights landed (TMA)
+  uint64_t p_full;     // partial-gradient slice landed (bulk copies)
+  uint32_t tmem_base;
+  uint32_t sync_ok;
 };
+static_assert(sizeof(TrainBars) <= 128, "barrier area");
 
 __device__ __forceinline__ uint8_t* align1024(uint8_t* p) {
   return reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(p) + 1023) & ~uintptr_t(1023));
@@ -64,20 +90,18 @@ __device__ __forceinline__ void issue_train_tile(const nrc_train_record* __restr
   bulk_g2s(dst, reinterpret_cast<const uint8_t*>(in) + static_cast<size_t>(tile) * kTRecTileBytes, bytes, full);
 }
 
-// fp16 bit pattern strictly positive (finite or +inf), i.e. act > 0 in the reference.
-__device__ __forceinline__ bool h_pos(uint32_t bits16) { return ((bits16 - 1u) & 0xFFFFu) < 0x7C00u; }
-
-// Store one 128-byte row (32 words) of a swizzled operand tile.
-__device__ __forceinline__ void store_row(uint8_t* tile, int row, const uint32_t (&w)[32]) {
+// Half h (16 words = chunks 4h..4h+3) of one 128-byte row of a swizzled operand tile.
+__device__ __forceinline__ void store_half(uint8_t* tile, int row, int h, const uint32_t* w) {
 #pragma unroll
-  for (int c = 0; c < 8; ++c)
-    *reinterpret_cast<uint4*>(tile + sw128_offset(row, c)) = make_uint4(w[4 * c], w[4 * c + 1], w[4 * c + 2], w[4 * c + 3]);
+  for (int c = 0; c < 4; ++c)
+    *reinterpret_cast<uint4*>(tile + sw128_offset(row, 4 * h + c)) =
+        make_uint4(w[4 * c], w[4 * c + 1], w[4 * c + 2], w[4 * c + 3]);
 }
 
-__device__ __forceinline__ void load_row(const uint8_t* tile, int row, uint32_t (&w)[32]) {
+__device__ __forceinline__ void load_half(const uint8_t* tile, int row, int h, uint32_t* w) {
 #pragma unroll
-  for (int c = 0; c < 8; ++c) {
-    const uint4 v = *reinterpret_cast<const uint4*>(tile + sw128_offset(row, c));
+  for (int c = 0; c < 4; ++c) {
+    const uint4 v = *reinterpret_cast<const uint4*>(tile + sw128_offset(row, 4 * h + c));
     w[4 * c] = v.x;
     w[4 * c + 1] = v.y;
     w[4 * c + 2] = v.z;
@@ -85,12 +109,101 @@ __device__ __forceinline__ void load_row(const uint8_t* tile, int row, uint32_t 
   }
 }
 
+// ReLU backward on packed halves: keep g where act > 0, and zero NaN sums as
+// the reference's NaN-mask trick does (NN_nv.glsl:240-243, 272-277).
+__device__ __forceinline__ uint32_t relu_mask_f16x2(uint32_t g, uint32_t a) {
+  const __half2 g2 = *reinterpret_cast<const __half2*>(&g);
+  const __half2 a2 = *reinterpret_cast<const __half2*>(&a);
+  return g & __hgt2_mask(a2, __float2half2_rn(0.0f)) & ~__hneu2_mask(g2, g2);
+}
+
+// Write half h (32 inputs) of one layer's final weight gradient from TMEM to the
+// CTA's partial slot. M=64 accumulator layout: output row 16q+t lives in TMEM
+// lane 32q+t (t < 16), so lanes 0..15 of each warp own one output row.
+__device__ __forceinline__ void drain_dw(uint32_t lane_base, int layer, int q, int h, int lane, float* dst) {
+  const int o = q * 16 + lane;
+  const bool keep = lane < 16 && (layer < kHidden || o < kOut);
+  uint32_t v[32];
+  tmem_ld32(lane_base + 64 * layer + 32 * h, v);
+  if (keep) {
+    float4* g4 = reinterpret_cast<float4*>(dst + layer * kLayerElems + o * 64 + 32 * h);
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+      g4[j] = make_float4(__uint_as_float(v[4 * j]), __uint_as_float(v[4 * j + 1]), __uint_as_float(v[4 * j + 2]),
+                          __uint_as_float(v[4 * j + 3]));
+  }
+}
+
+__device__ __forceinline__ uint32_t ld_acquire_gpu(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void fence_proxy_async_global() {
+  asm volatile("fence.proxy.async.global;" ::: "memory");
+}
+
+// Grid-wide barrier of a cooperative launch: every CTA adds one to the counter
+// and waits (bounded) until it reaches `target`. Writes before the barrier,
+// generic or read later by TMA, are visible after it. Returns false on timeout.
+__device__ __forceinline__ bool grid_sync(uint32_t* counter, uint32_t target, uint32_t* sync_ok) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    fence_proxy_async_global();
+    __threadfence();
+    atomicAdd(counter, 1u);
+    bool ok = true;
+    if (ld_acquire_gpu(counter) < target) {
+      const uint64_t t0 = globaltimer_ns();
+      while (ld_acquire_gpu(counter) < target) {
+        if (globaltimer_ns() - t0 > kWaitLimitNs) {
+          ok = false;
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+    __threadfence();
+    fence_proxy_async_global();
+    *sync_ok = ok ? 1u : 0u;
+  }
+  __syncthreads();
+  return *reinterpret_cast<volatile uint32_t*>(sync_ok) != 0;
+}
+
+// One optimizer update (nrc_optimize.comp:32-54) of parameter i from its
+// gradient sum; exactly the CPU oracle's operation order.
+struct AdamHyper {
+  float lr, beta1, beta2, eps, ema_alpha, loss_scale;
+  int use_ema;
+};
+
+__device__ __forceinline__ void adam_one(int i, float gsum, uint32_t n, const nrc_optimizer_state& st,
+                                         const AdamHyper& hp, nrc_optimizer_entry* __restrict__ entries,
+                                         __half* __restrict__ w16, __half* __restrict__ use16) {
+  float g = __fdiv_rn(__fdiv_rn(gsum, static_cast<float>(n)), hp.loss_scale);
+  if (isnan(g) || isinf(g)) g = 0.0f;
+  nrc_optimizer_entry e = entries[i];
+  const float m = __fmaf_rn(hp.beta1, e.m, __fmul_rn(__fsub_rn(1.0f, hp.beta1), g));
+  const float v = __fmaf_rn(hp.beta2, e.v, __fmul_rn(__fsub_rn(1.0f, hp.beta2), __fmul_rn(g, g)));
+  const float hm = __fdiv_rn(m, __fsub_rn(1.0f, st.beta1_t));
+  const float hv = __fdiv_rn(v, __fsub_rn(1.0f, st.beta2_t));
+  const float w = __fsub_rn(e.weight, __fdiv_rn(__fmul_rn(hp.lr, hm), __fadd_rn(__fsqrt_rn(hv), hp.eps)));
+  const float eta_t = __fsub_rn(1.0f, st.alpha_t), eta_t1 = __fsub_rn(1.0f, st.alpha_t_1);
+  const float ea = __fdiv_rn(__fsub_rn(1.0f, hp.ema_alpha), eta_t), eb = __fmul_rn(hp.ema_alpha, eta_t1);
+  const float ema = __fmaf_rn(ea, w, __fmul_rn(eb, e.ema_weight));
+  e.m = m;
+  e.v = v;
+  e.weight = w;
+  e.ema_weight = ema;
+  entries[i] = e;
+  w16[i] = __float2half_rn(w);
+  if (use16 != nullptr) use16[i] = __float2half_rn(hp.use_ema ? ema : w);
+}
+
 __global__ void __launch_bounds__(kTrainThreads, 1)
-    train_grad_kernel(const nrc_train_record* __restrict__ records, uint32_t* __restrict__ d_count,
-                      uint32_t capacity, uint32_t batch_cap, const __half* __restrict__ w16, float* __restrict__ grad,
-                      float* __restrict__ partials, nrc_optimizer_state* __restrict__ state, float loss_scale,
-                      float beta1, float beta2, float ema_alpha, int do_prepare, double* loss_acc,
-                      unsigned long long* loss_count, uint32_t* err) {
+    train_steps_kernel(const __grid_constant__ TrainParams P, const __grid_constant__ CUtensorMap wmap) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
   uint8_t* smem_w = smem;
@@ -98,311 +211,398 @@ __global__ void __launch_bounds__(kTrainThreads, 1)
   uint8_t* gbuf = smem + kGOff;
   uint8_t* stage = smem + kStageOff;
   TrainBars* B = reinterpret_cast<TrainBars*>(smem + kTBarOff);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(B + 1);
-
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const uint32_t raw = *d_count;
-  const uint32_t clamped = min(raw, batch_cap);
-  const uint32_t n = min(clamped, capacity);
-  const uint32_t num_tiles = (n + kTile - 1) / kTile;
 
   if (threadIdx.x == 0) {
     mbar_init(&B->rec_full[0], 1);
     mbar_init(&B->rec_full[1], 1);
-    mbar_init(&B->rec_empty[0], 128);
-    mbar_init(&B->rec_empty[1], 128);
-    mbar_init(&B->a_ready, 128);
+    mbar_init(&B->rec_empty[0], kEpiThreads);
+    mbar_init(&B->rec_empty[1], kEpiThreads);
+    mbar_init(&B->a_ready, kEpiThreads);
     mbar_init(&B->d_ready, 1);
     mbar_init(&B->tile_done, 1);
     mbar_init(&B->drain, 1);
+    mbar_init(&B->w_full, 1);
+    mbar_init(&B->p_full, 1);
     mbar_fence_init();
   }
   if (warp == 0) {
-    tmem_alloc(tmem_slot, 512);
+    tmem_alloc(&B->tmem_base, 512);
     tmem_relinquish();
   }
-  stage_weights(smem_w, w16);
-  fence_proxy_async_smem();
+  // Everything below may read what the preceding kernel in the stream wrote.
+  griddep_wait();
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
-  const uint32_t tmem = *tmem_slot;
-  // Every CTA has read the count above; CTA 0 now plays nrc_train_prepare.comp.
-  // Other CTAs may still read the count concurrently: they see either the raw or
-  // the clamped value, and both clamp to the same n.
-  if (do_prepare && blockIdx.x == 0 && threadIdx.x == 0) {
-    *d_count = clamped;
-    if (n > 0) {  // the optimizer kernel updates exactly when records were processed
-      nrc_optimizer_state st = *state;
-      st.t += 1;
-      st.beta1_t *= beta1;
-      st.beta2_t *= beta2;
-      st.alpha_t_1 = st.alpha_t;
-      st.alpha_t *= ema_alpha;
-      *state = st;
+  const uint32_t tmem = __shfl_sync(0xffffffffu, B->tmem_base, 0);
+  float* const my_partial = P.partials + static_cast<size_t>(blockIdx.x) * kParams;
+
+  // Role state that persists across the batches (mbarrier phases).
+  const int ew = warp - 1;   // epilogue warp index (warps 1..8)
+  const int h = ew >> 2;     // column half of the epilogue warp
+  const int q = warp & 3;    // TMEM lane quadrant
+  const int row = q * 32 + lane;
+  const bool leader = ew == 0 && lane == 0;
+  const uint32_t lane_base = tmem + (static_cast<uint32_t>(q * 32) << 16);
+  const uint32_t a_lane = lane_base + kACol + 16 * h;
+  const uint32_t d_lane = lane_base + kDCol + 32 * h;
+  uint32_t ph_a = 0, ph_d = 0;  // MMA warp / epilogue d_ready phases
+  uint32_t ct = 0;              // tiles this CTA has processed over all batches
+  uint32_t wloads = 0;          // weight loads issued to this CTA
+  uint32_t barriers = 0;        // grid barriers passed
+  uint32_t pstages = 0;         // partial-gradient slices staged
+  bool ok = true;
+  double loss_local = 0.0;
+  uint32_t loss_n = 0;
+  const AdamHyper hp{P.lr, P.beta1, P.beta2, P.eps, P.ema_alpha, P.loss_scale, P.use_ema};
+
+  for (int step = 0; step < P.steps && ok; ++step) {
+    const TrainBatch bt = P.batch[step];
+    const uint32_t raw = *reinterpret_cast<volatile const uint32_t*>(bt.d_count);
+    const uint32_t clamped = min(raw, P.batch_cap);
+    const uint32_t n = min(clamped, bt.capacity);
+    const uint32_t num_tiles = (n + kTile - 1) / kTile;
+    const uint32_t my_tiles = blockIdx.x < num_tiles ? (num_tiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
+    __syncthreads();  // every thread has read the count before CTA 0 may rewrite it
+    if (P.mode == kTrainStep && blockIdx.x == 0 && threadIdx.x == 0) {
+      // nrc_train_prepare.comp; other CTAs read either the raw or the clamped
+      // count, and both clamp to the same n.
+      *bt.d_count = clamped;
+      if (n > 0) {  // the optimizer phase below updates exactly when records were processed
+        nrc_optimizer_state st = *P.state;
+        st.t += 1;
+        st.beta1_t *= P.beta1;
+        st.beta2_t *= P.beta2;
+        st.alpha_t_1 = st.alpha_t;
+        st.alpha_t *= P.ema_alpha;
+        *P.state = st;
+      }
+    }
+    if (threadIdx.x == 0 && my_tiles > 0) stage_weights_tma(smem_w, &wmap, &B->w_full);
+
+    if (warp == 0) {
+      // ---------------------------------------------------- MMA issuer --
+      // The whole warp runs the schedule (converged, so descriptors stay
+      // warp-uniform); one elected lane issues each group of MMAs.
+      const uint32_t id_fwd = idesc_f16_f32(128, 64, 0, 0);
+      const uint32_t id_out = idesc_f16_f32(128, 16, 0, 0);
+      const uint32_t id_dw = idesc_f16_f32(64, 64, 1, 1);
+      const uint32_t id_da = idesc_f16_f32(128, 64, 0, 1);
+      const uint32_t dcol = tmem + kDCol, acol = tmem + kACol;
+      // descriptor bases; +1 in the address field = 16 bytes
+      const uint64_t dk_w = sdesc_sw128(smem_u32(smem_w), 16, 1024);    // K-major W_l: + l*512 + 2j
+      const uint64_t dm_g = sdesc_sw128(smem_u32(gbuf), 8192, 1024);    // MN-major g: + buf*1024 + 128j
+      const uint64_t dm_act = sdesc_sw128(smem_u32(act), 8192, 1024);   // MN-major act_l: + l*1024 + 128j
+      const uint64_t dm_w = sdesc_sw128(smem_u32(smem_w), 8192, 1024);  // MN-major W_l: + l*512 + 128j
+      auto wait_a = [&]() {
+        if (!ok) return;
+        ok = warp_all(mbar_wait(&B->a_ready, ph_a, kWaitLimitNs));
+        if (!ok) return;
+        ph_a ^= 1u;
+        tc_fence_after();
+      };
+      if (my_tiles > 0) ok = ok && warp_all(mbar_wait(&B->w_full, wloads & 1, kWaitLimitNs));
+      for (uint32_t it = 0; it < my_tiles && ok; ++it) {
+        wait_a();  // act_0
+        for (int l = 0; l < 6 && ok; ++l) {
+          if (elect_one()) {
+            const uint64_t w = dk_w + static_cast<uint64_t>(l * 512);
+            const uint32_t id = l < 5 ? id_fwd : id_out;
+            mma_ts(dcol, acol + 0, w + 0, id, 0u);
+            mma_ts(dcol, acol + 8, w + 2, id, 1u);
+            mma_ts(dcol, acol + 16, w + 4, id, 1u);
+            mma_ts(dcol, acol + 24, w + 6, id, 1u);
+            mma_commit(&B->d_ready);
+          }
+          __syncwarp();
+          wait_a();  // act_{l+1}, or g_6 after the output layer
+        }
+        // backward: g_{l+1} lives in gradient buffer (5 - l) & 1
+        for (int l = 5; l >= 0 && ok; --l) {
+          const uint64_t gb = static_cast<uint64_t>(((5 - l) & 1) * 1024);
+          if (elect_one()) {
+            if (l > 0) {
+              // dA_l = g W_l  (K = 64 outputs, or 16 for the padded output layer)
+              const uint64_t wm = dm_w + static_cast<uint64_t>(l * 512);
+              mma_ts(dcol, acol + 0, wm + 0, id_da, 0u);
+              if (l < 5) {
+                mma_ts(dcol, acol + 8, wm + 128, id_da, 1u);
+                mma_ts(dcol, acol + 16, wm + 256, id_da, 1u);
+                mma_ts(dcol, acol + 24, wm + 384, id_da, 1u);
+              }
+              mma_commit(&B->d_ready);
+            }
+            // dW_l += g^T act_l   (M = 64 outputs, N = 64 inputs, K = 128 records);
+            // complete by the next d_ready (or tile_done for l = 0)
+            const uint64_t ga = dm_g + gb, ab = dm_act + static_cast<uint64_t>(l * 1024);
+            const uint32_t dw = tmem + 64 * l;
+            mma_ss(dw, ga + 0, ab + 0, id_dw, it > 0 ? 1u : 0u);
+#pragma unroll
+            for (int j = 1; j < 8; ++j) mma_ss(dw, ga + 128 * j, ab + 128 * j, id_dw, 1u);
+            if (l == 0) mma_commit(&B->tile_done);
+          }
+          __syncwarp();
+          if (l > 0) wait_a();  // g_l
+        }
+      }
+      ct += my_tiles;
+    } else {
+      // ------------------------------------------------------ epilogue --
+      auto wait_d = [&]() -> bool {
+        ok = ok && warp_all(mbar_wait(&B->d_ready, ph_d, kWaitLimitNs));
+        ph_d ^= 1u;
+        tc_fence_after();
+        return ok;
+      };
+      auto publish = [&]() {  // operand rows written: hand them to the tensor core
+        fence_proxy_async_smem();
+        tc_fence_before();
+        mbar_arrive(&B->a_ready);
+      };
+      // The record stages are free: every tile of the previous batch was read
+      // before the grid barrier this batch starts after.
+      if (leader) {
+        for (uint32_t k = 0; k < 2 && k < my_tiles; ++k) {
+          const uint32_t s = (ct + k) & 1;
+          issue_train_tile(bt.records, blockIdx.x + k * gridDim.x, n, stage + s * kTRecTileBytes, &B->rec_full[s]);
+        }
+      }
+      for (uint32_t it = 0; it < my_tiles && ok; ++it, ++ct) {
+        const uint32_t tile = blockIdx.x + it * gridDim.x;
+        const uint32_t rows_valid = min(static_cast<uint32_t>(kTile), n - tile * kTile);
+        const bool valid = row < static_cast<int>(rows_valid);
+        const bool last = it + 1 == my_tiles;
+        const uint32_t s = ct & 1, use = ct >> 1;  // stage and its use count
+        ok = warp_all(mbar_wait(&B->rec_full[s], use & 1, kWaitLimitNs));
+        if (!ok) break;
+        float r[kInFloats], target[3];
+        {
+          const float4* src = reinterpret_cast<const float4*>(stage + s * kTRecTileBytes + row * kTRecBytes);
+          float f[20];
+#pragma unroll
+          for (int k = 0; k < 5; ++k) {
+            const float4 v = valid ? src[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+            f[4 * k] = v.x;
+            f[4 * k + 1] = v.y;
+            f[4 * k + 2] = v.z;
+            f[4 * k + 3] = v.w;
+          }
+          target[0] = f[0];
+          target[1] = f[1];
+          target[2] = f[2];
+#pragma unroll
+          for (int k = 0; k < kInFloats; ++k) r[k] = f[6 + k];
+        }
+        mbar_arrive(&B->rec_empty[s]);
+        if (leader && it + 2 < my_tiles) {
+          if (mbar_wait(&B->rec_empty[s], use & 1, kWaitLimitNs))
+            issue_train_tile(bt.records, tile + 2 * gridDim.x, n, stage + s * kTRecTileBytes, &B->rec_full[s]);
+          else
+            atomicOr(P.err, kErrTimeout);
+        }
+        __syncwarp();
+        // the previous tile's last MMAs read act_0 and the gradient buffers
+        if (it > 0) {
+          ok = warp_all(mbar_wait(&B->tile_done, (ct - 1) & 1, kWaitLimitNs));
+          if (!ok) break;
+          tc_fence_after();
+        }
+        {
+          uint32_t e[16];
+          if (h == 0)
+            encode_half0(r, e);
+          else
+            encode_half1(r, e);
+          if (!valid) {
+#pragma unroll
+            for (int k = 0; k < 16; ++k) e[k] = 0u;
+          }
+          tmem_st16(a_lane, e);
+          store_half(act, row, h, e);
+        }
+        publish();
+        // forward: act_{l+1} = fp16(relu(W_l act_l))
+        for (int l = 0; l < 5; ++l) {
+          if (!wait_d()) break;
+          uint32_t v[32], p[16];
+          tmem_ld32(d_lane, v);
+#pragma unroll
+          for (int j = 0; j < 16; ++j)
+            p[j] = pack_relu_f16x2(__uint_as_float(v[2 * j]), __uint_as_float(v[2 * j + 1]));
+          tmem_st16(a_lane, p);
+          store_half(act + (l + 1) * kActBytes, row, h, p);
+          publish();
+        }
+        if (!ok) break;
+        // output + relative-L2 luminance loss gradient (NN_nv.glsl:178-196), fp16;
+        // outputs 3..63 of the gradient row are zero (the output layer's padding)
+        if (!wait_d()) break;
+        {
+          uint32_t gw[16];
+#pragma unroll
+          for (int k = 0; k < 16; ++k) gw[k] = 0u;
+          if (h == 0) {
+            uint32_t o4[4];
+            tmem_ld4(lane_base + kDCol, o4);
+            const float p0 = __uint_as_float(o4[0]), p1 = __uint_as_float(o4[1]), p2 = __uint_as_float(o4[2]);
+            const float lum = __fmaf_rn(0.114f, fmaxf(p2, 0.0f),
+                                        __fmaf_rn(0.587f, fmaxf(p1, 0.0f), __fmul_rn(0.299f, fmaxf(p0, 0.0f))));
+            const float den = __fmaf_rn(lum, lum, 0.01f);
+            const float s2 = __fmul_rn(2.0f, P.loss_scale);
+            const float d0 = __fdiv_rn(__fmul_rn(s2, __fsub_rn(p0, target[0])), den);
+            const float d1 = __fdiv_rn(__fmul_rn(s2, __fsub_rn(p1, target[1])), den);
+            const float d2 = __fdiv_rn(__fmul_rn(s2, __fsub_rn(p2, target[2])), den);
+            if (valid) {
+              gw[0] = pack_f16x2(d0, d1);
+              gw[1] = pack_f16x2(d2, 0.0f);
+              if (P.loss_acc != nullptr) {
+                const double dd = static_cast<double>(den);
+                const double e0 = static_cast<double>(p0) - target[0], e1 = static_cast<double>(p1) - target[1],
+                             e2 = static_cast<double>(p2) - target[2];
+                loss_local += (e0 * e0 + e1 * e1 + e2 * e2) / dd;
+                ++loss_n;
+              }
+            }
+            tmem_st16(a_lane, gw);  // dA_5 reads K = 16 (A words 0..7)
+          }
+          store_half(gbuf, row, h, gw);
+          publish();
+        }
+        // backward: g_l = fp16((g_{l+1} W_l) masked by act_l > 0), l = 5..1
+        for (int l = 5; l >= 1; --l) {
+          if (!wait_d()) break;
+          uint32_t aw[16], gw[16], v[32];
+          load_half(act + l * kActBytes, row, h, aw);
+          tmem_ld32(d_lane, v);
+#pragma unroll
+          for (int j = 0; j < 16; ++j)
+            gw[j] = relu_mask_f16x2(pack_f16x2(__uint_as_float(v[2 * j]), __uint_as_float(v[2 * j + 1])), aw[j]);
+          tmem_st16(a_lane, gw);
+          store_half(gbuf + ((6 - l) & 1) * kActBytes, row, h, gw);
+          publish();
+          // dA_l completing means dW_{l+1} (issued before it) is complete too;
+          // on the CTA's last tile it is final: write it out while the chain goes on.
+          if (last && l <= 4) drain_dw(lane_base, l + 1, q, h, lane, my_partial);
+        }
+        if (!ok) break;
+        if (last) {
+          ok = warp_all(mbar_wait(&B->tile_done, ct & 1, kWaitLimitNs));
+          if (!ok) break;
+          tc_fence_after();
+          drain_dw(lane_base, 1, q, h, lane, my_partial);
+          drain_dw(lane_base, 0, q, h, lane, my_partial);
+        }
+      }
+    }
+    if (my_tiles > 0) ++wloads;
+    if (!ok && lane == 0) atomicOr(P.err, kErrTimeout);
+    ok = __syncthreads_and(ok) != 0;  // one decision per CTA from here on
+
+    // ------------------------------------------- reduction + optimizer --
+    if (!grid_sync(P.sync, ++barriers * gridDim.x, &B->sync_ok)) {
+      ok = false;
+      if (threadIdx.x == 0) atomicOr(P.err, kErrTimeout);
+      break;
+    }
+    {
+      // This CTA's slice [c0, c1) of float4 gradient columns. The slice of every
+      // partial (one contiguous run per CTA that had tiles) is staged into the
+      // free activation buffers with bulk copies, summed over the partials in a
+      // fixed order (run-to-run identical), and the parameters are updated.
+      const uint32_t active = min(gridDim.x, num_tiles);
+      const uint32_t per = (kCols4 + gridDim.x - 1) / gridDim.x;
+      const uint32_t c0 = min(static_cast<uint32_t>(kCols4), blockIdx.x * per);
+      const uint32_t c1 = min(static_cast<uint32_t>(kCols4), c0 + per);
+      const uint32_t ncols = c1 - c0;
+      float4* stg = reinterpret_cast<float4*>(act);   // [active][ncols], <= 85 KB of the 96 KB
+      float4* red = reinterpret_cast<float4*>(gbuf);  // 8 x 32
+      static_assert(6 * kActBytes >= (kCols4 + kMaxTrainCtas) * 16, "staged slice fits the activation buffers");
+      if (n > 0 && ncols > 0) {
+        if (threadIdx.x == 0) {
+          const uint32_t row_bytes = ncols * 16;
+          mbar_arrive_expect_tx(&B->p_full, row_bytes * active);
+          for (uint32_t r = 0; r < active; ++r)
+            bulk_g2s(stg + static_cast<size_t>(r) * ncols, P.partials + static_cast<size_t>(r) * kParams + 4 * c0,
+                     row_bytes, &B->p_full);
+        }
+        if (!mbar_wait(&B->p_full, pstages & 1, kWaitLimitNs)) {
+          ok = false;
+          atomicOr(P.err, kErrTimeout);
+        }
+        ++pstages;
+        const int col = threadIdx.x & 31, rg = threadIdx.x >> 5;  // 8 row groups (threads 0..255)
+        for (uint32_t cb = 0; cb < ncols; cb += 32) {
+          const uint32_t cc = cb + col;
+          if (rg < 8) {
+            float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (ok && cc < ncols) {
+              for (uint32_t r = rg; r < active; r += 8) {
+                const float4 v = stg[static_cast<size_t>(r) * ncols + cc];
+                acc.x += v.x;
+                acc.y += v.y;
+                acc.z += v.z;
+                acc.w += v.w;
+              }
+            }
+            red[rg * 32 + col] = acc;
+          }
+          __syncthreads();
+          if (rg == 0 && cc < ncols) {  // row 0 of the staged slice now holds the sums
+            float4 g = red[col];
+#pragma unroll
+            for (int k = 1; k < 8; ++k) {
+              const float4 v = red[k * 32 + col];
+              g.x += v.x;
+              g.y += v.y;
+              g.z += v.z;
+              g.w += v.w;
+            }
+            stg[cc] = g;
+          }
+          __syncthreads();
+        }
+        if (P.mode == kTrainStep) {
+          const nrc_optimizer_state st = *P.state;
+          __half* use16 = bt.write_use ? P.use16 : nullptr;
+          const float* sums = reinterpret_cast<const float*>(stg);
+          for (uint32_t k = threadIdx.x; k < 4 * ncols; k += blockDim.x)
+            adam_one(4 * c0 + k, sums[k], n, st, hp, P.entries, P.w16, use16);
+        } else {
+          for (uint32_t k = threadIdx.x; k < ncols; k += blockDim.x)
+            reinterpret_cast<float4*>(P.grad_out)[c0 + k] = stg[k];
+        }
+      } else if (P.mode == kGradientOnly) {
+        for (uint32_t k = threadIdx.x; k < ncols; k += blockDim.x)
+          reinterpret_cast<float4*>(P.grad_out)[c0 + k] = make_float4(0.f, 0.f, 0.f, 0.f);  // no records
+      }
+      ok = __syncthreads_and(ok) != 0;
+    }
+    if (step + 1 < P.steps) {  // publish the new weights before the next batch loads them
+      if (!grid_sync(P.sync, ++barriers * gridDim.x, &B->sync_ok)) {
+        ok = false;
+        if (threadIdx.x == 0) atomicOr(P.err, kErrTimeout);
+        break;
+      }
     }
   }
 
-  if (warp == 0) {
-    // ------------------------------------------------------ MMA issuer --
-    // The whole warp runs the schedule (converged, so descriptors stay
-    // warp-uniform); one elected lane issues each group of MMAs.
-    bool ok = true;
-    uint32_t ph_a = 0;
-    const uint32_t tm = __shfl_sync(0xffffffffu, tmem, 0);
-    const uint32_t id_fwd = idesc_f16_f32(128, 64, 0, 0);
-    const uint32_t id_out = idesc_f16_f32(128, 16, 0, 0);
-    const uint32_t id_dw = idesc_f16_f32(64, 64, 1, 1);
-    const uint32_t id_da = idesc_f16_f32(128, 64, 0, 1);
-    const uint32_t dcol = tm + kDCol;
-    // descriptor bases; +1 in the address field = 16 bytes
-    const uint64_t dk_act = sdesc_sw128(smem_u32(act), 16, 1024);   // K-major act_l: + l*1024 + 2j
-    const uint64_t dk_w = sdesc_sw128(smem_u32(smem_w), 16, 1024);  // K-major W_l: + l*512 + 2j
-    const uint64_t dm_g = sdesc_sw128(smem_u32(gbuf), 8192, 1024);  // MN-major g: + buf*1024 + 128j
-    const uint64_t dk_g = sdesc_sw128(smem_u32(gbuf), 16, 1024);    // K-major g: + buf*1024 + 2j
-    const uint64_t dm_act = sdesc_sw128(smem_u32(act), 8192, 1024); // MN-major act_l: + l*1024 + 128j
-    const uint64_t dm_w = sdesc_sw128(smem_u32(smem_w), 8192, 1024); // MN-major W_l: + l*512 + 128j
-    auto wait_a = [&]() {
-      if (!ok) return;
-      ok = warp_all(mbar_wait(&B->a_ready, ph_a, kWaitLimitNs));
-      if (!ok) return;
-      ph_a ^= 1u;
-      tc_fence_after();
-    };
-    uint32_t it = 0;
-    for (uint32_t tile = blockIdx.x; tile < num_tiles && ok; tile += gridDim.x, ++it) {
-      wait_a();  // act_0
-      for (int l = 0; l < 6 && ok; ++l) {
-        if (elect_one()) {
-          const uint64_t a = dk_act + static_cast<uint64_t>(l * 1024), w = dk_w + static_cast<uint64_t>(l * 512);
-          const uint32_t id = l < 5 ? id_fwd : id_out;
-          mma_ss(dcol, a + 0, w + 0, id, 0u);
-          mma_ss(dcol, a + 2, w + 2, id, 1u);
-          mma_ss(dcol, a + 4, w + 4, id, 1u);
-          mma_ss(dcol, a + 6, w + 6, id, 1u);
-          mma_commit(&B->d_ready);
-        }
-        __syncwarp();
-        wait_a();  // act_{l+1}, or g_6 after the output layer
-      }
-      // backward: g_{l+1} lives in gradient buffer (5 - l) & 1
-      for (int l = 5; l >= 0 && ok; --l) {
-        const uint64_t gb = static_cast<uint64_t>(((5 - l) & 1) * 1024);
-        if (elect_one()) {
-          // dW_l += g^T act_l   (M = 64 outputs, N = 64 inputs, K = 128 records)
-          const uint64_t ga = dm_g + gb, ab = dm_act + static_cast<uint64_t>(l * 1024);
-          const uint32_t acc0 = it > 0 ? 1u : 0u;
-          const uint32_t dw = tm + 64 * l;
-          mma_ss(dw, ga + 0, ab + 0, id_dw, acc0);
+  if (P.loss_acc != nullptr && warp > 0) {
 #pragma unroll
-          for (int j = 1; j < 8; ++j) mma_ss(dw, ga + 128 * j, ab + 128 * j, id_dw, 1u);
-          if (l > 0) {
-            // dA_l = g W_l  (K = 64 outputs, or 16 for the padded output layer)
-            const uint64_t gk = dk_g + gb, wm = dm_w + static_cast<uint64_t>(l * 512);
-            mma_ss(dcol, gk + 0, wm + 0, id_da, 0u);
-            if (l < 5) {
-              mma_ss(dcol, gk + 2, wm + 128, id_da, 1u);
-              mma_ss(dcol, gk + 4, wm + 256, id_da, 1u);
-              mma_ss(dcol, gk + 6, wm + 384, id_da, 1u);
-            }
-            mma_commit(&B->d_ready);
-          } else {
-            mma_commit(&B->tile_done);
-          }
-        }
-        __syncwarp();
-        if (l > 0) wait_a();  // g_l
-      }
+    for (int off = 16; off > 0; off >>= 1) {
+      loss_local += __shfl_xor_sync(0xffffffffu, loss_local, off);
+      loss_n += __shfl_xor_sync(0xffffffffu, loss_n, off);
     }
-    if (!ok && lane == 0) atomicOr(err, kErrTimeout);
-    // all issued MMAs must be complete before TMEM is released
+    if (lane == 0 && loss_n > 0) {
+      atomicAdd(P.loss_acc, loss_local);
+      atomicAdd(P.loss_count, static_cast<unsigned long long>(loss_n));
+    }
+  }
+  // all issued MMAs must be complete before TMEM is released
+  if (warp == 0) {
     if (elect_one()) mma_commit(&B->drain);
     __syncwarp();
-    if (!warp_all(mbar_wait(&B->drain, 0, kWaitLimitNs)) && lane == 0) atomicOr(err, kErrTimeout);
-  } else {
-    // ------------------------------------------------ epilogue warpgroup --
-    const int q = warp & 3;
-    const int row = q * 32 + lane;
-    const bool leader = warp == 1 && lane == 0;
-    const uint32_t lane_base = tmem + (static_cast<uint32_t>(q * 32) << 16);
-    bool ok = true;
-    uint32_t ph_d = 0;
-    double loss_local = 0.0;
-    uint32_t loss_n = 0;
-    if (leader) {
-      for (uint32_t b = 0; b < 2; ++b) {
-        const uint32_t t = blockIdx.x + b * gridDim.x;
-        if (t < num_tiles) issue_train_tile(records, t, n, stage + b * kTRecTileBytes, &B->rec_full[b]);
-      }
-    }
-    auto wait_d = [&]() -> bool {
-      ok = ok && warp_all(mbar_wait(&B->d_ready, ph_d, kWaitLimitNs));
-      ph_d ^= 1u;
-      tc_fence_after();
-      return ok;
-    };
-    auto publish = [&]() {  // operand tile rows written: hand them to the tensor core
-      fence_proxy_async_smem();
-      tc_fence_before();
-      mbar_arrive(&B->a_ready);
-    };
-    uint32_t it = 0;
-    for (uint32_t tile = blockIdx.x; tile < num_tiles && ok; tile += gridDim.x, ++it) {
-      const uint32_t rows_valid = min(static_cast<uint32_t>(kTile), n - tile * kTile);
-      const bool valid = row < static_cast<int>(rows_valid);
-      const uint32_t b = it & 1;
-      ok = warp_all(mbar_wait(&B->rec_full[b], (it >> 1) & 1, kWaitLimitNs));
-      if (!ok) break;
-      float r[kInFloats], target[3];
-      {
-        const float4* src = reinterpret_cast<const float4*>(stage + b * kTRecTileBytes + row * kTRecBytes);
-        float f[20];
-#pragma unroll
-        for (int k = 0; k < 5; ++k) {
-          const float4 v = valid ? src[k] : make_float4(0.f, 0.f, 0.f, 0.f);
-          f[4 * k] = v.x;
-          f[4 * k + 1] = v.y;
-          f[4 * k + 2] = v.z;
-          f[4 * k + 3] = v.w;
-        }
-        target[0] = f[0];
-        target[1] = f[1];
-        target[2] = f[2];
-#pragma unroll
-        for (int k = 0; k < kInFloats; ++k) r[k] = f[6 + k];
-      }
-      mbar_arrive(&B->rec_empty[b]);
-      if (leader && blockIdx.x + (it + 2) * gridDim.x < num_tiles) {
-        if (mbar_wait(&B->rec_empty[b], (it >> 1) & 1, kWaitLimitNs))
-          issue_train_tile(records, blockIdx.x + (it + 2) * gridDim.x, n, stage + b * kTRecTileBytes,
-                           &B->rec_full[b]);
-        else
-          atomicOr(err, kErrTimeout);
-      }
-      __syncwarp();
-      // the previous tile's last MMAs read act_0 and the gradient buffers
-      if (it > 0) {
-        ok = warp_all(mbar_wait(&B->tile_done, (it - 1) & 1, kWaitLimitNs));
-        if (!ok) break;
-        tc_fence_after();
-      }
-      {
-        uint32_t e[32];
-        encode_input(r, e);
-        if (!valid) {
-#pragma unroll
-          for (int k = 0; k < 32; ++k) e[k] = 0u;
-        }
-        store_row(act, row, e);
-      }
-      publish();
-      // forward: act_{l+1} = fp16(relu(W_l act_l))
-      for (int l = 0; l < 5; ++l) {
-        if (!wait_d()) break;
-        uint32_t v[32], p[32];
-        tmem_ld32(lane_base + kDCol, v);
-#pragma unroll
-        for (int j = 0; j < 16; ++j) p[j] = pack_relu_f16x2(__uint_as_float(v[2 * j]), __uint_as_float(v[2 * j + 1]));
-        tmem_ld32(lane_base + kDCol + 32, v);
-#pragma unroll
-        for (int j = 0; j < 16; ++j)
-          p[16 + j] = pack_relu_f16x2(__uint_as_float(v[2 * j]), __uint_as_float(v[2 * j + 1]));
-        store_row(act + (l + 1) * kActBytes, row, p);
-        publish();
-      }
-      if (!ok) break;
-      // output + relative-L2 luminance loss gradient (NN_nv.glsl:178-196), fp16
-      if (!wait_d()) break;
-      {
-        uint32_t o4[4];
-        tmem_ld4(lane_base + kDCol, o4);
-        const float p0 = __uint_as_float(o4[0]), p1 = __uint_as_float(o4[1]), p2 = __uint_as_float(o4[2]);
-        const float lum = __fmaf_rn(0.114f, fmaxf(p2, 0.0f), __fmaf_rn(0.587f, fmaxf(p1, 0.0f), __fmul_rn(0.299f, fmaxf(p0, 0.0f))));
-        const float den = __fmaf_rn(lum, lum, 0.01f);
-        const float s2 = __fmul_rn(2.0f, loss_scale);
-        const float d0 = __fdiv_rn(__fmul_rn(s2, __fsub_rn(p0, target[0])), den);
-        const float d1 = __fdiv_rn(__fmul_rn(s2, __fsub_rn(p1, target[1])), den);
-        const float d2 = __fdiv_rn(__fmul_rn(s2, __fsub_rn(p2, target[2])), den);
-        uint32_t gw[32];
-#pragma unroll
-        for (int k = 0; k < 32; ++k) gw[k] = 0u;
-        if (valid) {
-          gw[0] = pack_f16x2(d0, d1);
-          gw[1] = pack_f16x2(d2, 0.0f);
-          if (loss_acc != nullptr) {
-            const double dd = static_cast<double>(den);
-            const double e0 = static_cast<double>(p0) - target[0], e1 = static_cast<double>(p1) - target[1],
-                         e2 = static_cast<double>(p2) - target[2];
-            loss_local += (e0 * e0 + e1 * e1 + e2 * e2) / dd;
-            ++loss_n;
-          }
-        }
-        store_row(gbuf, row, gw);
-        publish();
-      }
-      // backward: g_l = fp16((g_{l+1} W_l) masked by act_l > 0), l = 5..1
-      for (int l = 5; l >= 1; --l) {
-        if (!wait_d()) break;
-        uint32_t aw[32], gw[32], v[32];
-        load_row(act + l * kActBytes, row, aw);
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          tmem_ld32(lane_base + kDCol + 32 * h, v);
-#pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            const uint32_t a2 = aw[16 * h + j];
-            float x0 = __uint_as_float(v[2 * j]), x1 = __uint_as_float(v[2 * j + 1]);
-            x0 = (h_pos(a2 & 0xFFFFu) && !isnan(x0)) ? x0 : 0.0f;
-            x1 = (h_pos(a2 >> 16) && !isnan(x1)) ? x1 : 0.0f;
-            gw[16 * h + j] = pack_f16x2(x0, x1);
-          }
-        }
-        store_row(gbuf + ((6 - l) & 1) * kActBytes, row, gw);
-        publish();
-      }
-    }
-    // cross-CTA reduction of this CTA's weight gradients
-    if (ok && it > 0) {
-      ok = warp_all(mbar_wait(&B->tile_done, (it - 1) & 1, kWaitLimitNs));
-      tc_fence_after();
-      if (ok) {
-        const bool has_row = lane < 16;  // M=64 layout: rows 16q+t live in lanes 32q+t, t < 16
-        const int o = q * 16 + lane;
-        float* dst = partials ? partials + static_cast<size_t>(blockIdx.x) * kParams : grad;
-        for (int l = 0; l < 6; ++l) {
-          uint32_t v[32];
-#pragma unroll
-          for (int h = 0; h < 2; ++h) {
-            tmem_ld32(lane_base + 64 * l + 32 * h, v);
-            const bool keep = has_row && (l < 5 || o < kOut);
-            if (keep) {
-              float4* g4 = reinterpret_cast<float4*>(dst + l * kLayerElems + o * 64 + 32 * h);
-#pragma unroll
-              for (int j = 0; j < 8; ++j) {
-                const float4 val = make_float4(__uint_as_float(v[4 * j]), __uint_as_float(v[4 * j + 1]),
-                                               __uint_as_float(v[4 * j + 2]), __uint_as_float(v[4 * j + 3]));
-                if (partials)
-                  g4[j] = val;
-                else
-                  atomicAdd(g4 + j, val);
-              }
-            }
-          }
-        }
-      }
-    }
-    if (loss_acc != nullptr) {
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) {
-        loss_local += __shfl_xor_sync(0xffffffffu, loss_local, off);
-        loss_n += __shfl_xor_sync(0xffffffffu, loss_n, off);
-      }
-      if (lane == 0 && loss_n > 0) {
-        atomicAdd(loss_acc, loss_local);
-        atomicAdd(loss_count, static_cast<unsigned long long>(loss_n));
-      }
-    }
-    if (!ok && lane == 0) atomicOr(err, kErrTimeout);
+    if (!warp_all(mbar_wait(&B->drain, 0, kWaitLimitNs)) && lane == 0) atomicOr(P.err, kErrTimeout);
   }
   tc_fence_before();
   __syncthreads();
@@ -412,88 +612,43 @@ __global__ void __launch_bounds__(kTrainThreads, 1)
   }
 }
 
-// nrc_optimize.comp:32-54 over all parameters (one thread each). In
-// deterministic mode the per-CTA partial gradients are summed in CTA order;
-// otherwise the atomic accumulator is read and zeroed for the next step.
-__global__ void __launch_bounds__(256) adam_kernel(const uint32_t* __restrict__ d_count, uint32_t capacity,
-                                                   uint32_t batch_cap, float* __restrict__ grad,
-                                                   const float* __restrict__ partials, uint32_t grad_ctas,
-                                                   nrc_optimizer_entry* __restrict__ entries,
-                                                   const nrc_optimizer_state* __restrict__ state,
-                                                   __half* __restrict__ w16, __half* __restrict__ use16, float lr,
-                                                   float beta1, float beta2, float eps, float ema_alpha,
-                                                   float loss_scale, int use_ema) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= kParams) return;
-  const uint32_t n = min(min(*d_count, batch_cap), capacity);
-  if (n == 0) return;
-  float gsum;
-  if (partials != nullptr) {
-    const uint32_t active = min(grad_ctas, (n + kTile - 1) / kTile);
-    gsum = 0.0f;
-    for (uint32_t b = 0; b < active; ++b) gsum += partials[static_cast<size_t>(b) * kParams + i];
-  } else {
-    gsum = grad[i];
-    grad[i] = 0.0f;
-  }
-  const nrc_optimizer_state st = *state;
-  float g = __fdiv_rn(__fdiv_rn(gsum, static_cast<float>(n)), loss_scale);
-  if (isnan(g) || isinf(g)) g = 0.0f;
-  nrc_optimizer_entry e = entries[i];
-  const float m = __fmaf_rn(beta1, e.m, __fmul_rn(__fsub_rn(1.0f, beta1), g));
-  const float v = __fmaf_rn(beta2, e.v, __fmul_rn(__fsub_rn(1.0f, beta2), __fmul_rn(g, g)));
-  const float hm = __fdiv_rn(m, __fsub_rn(1.0f, st.beta1_t));
-  const float hv = __fdiv_rn(v, __fsub_rn(1.0f, st.beta2_t));
-  const float w = __fsub_rn(e.weight, __fdiv_rn(__fmul_rn(lr, hm), __fadd_rn(__fsqrt_rn(hv), eps)));
-  const float eta_t = __fsub_rn(1.0f, st.alpha_t), eta_t1 = __fsub_rn(1.0f, st.alpha_t_1);
-  const float ea = __fdiv_rn(__fsub_rn(1.0f, ema_alpha), eta_t), eb = __fmul_rn(ema_alpha, eta_t1);
-  const float ema = __fmaf_rn(ea, w, __fmul_rn(eb, e.ema_weight));
-  e.m = m;
-  e.v = v;
-  e.weight = w;
-  e.ema_weight = ema;
-  entries[i] = e;
-  w16[i] = __float2half_rn(w);
-  if (use16 != nullptr) use16[i] = __float2half_rn(use_ema ? ema : w);
-}
-
 }  // namespace
 
 cudaError_t configure_train_kernels() {
-  return cudaFuncSetAttribute(train_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTrainSmemBytes);
+  return cudaFuncSetAttribute(train_steps_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTrainSmemBytes);
 }
 
 uint32_t train_smem_bytes() { return kTrainSmemBytes; }
 
-uint32_t train_grid(uint32_t capacity, uint32_t batch_cap, int num_sms) {
-  const uint32_t cap = capacity < batch_cap ? capacity : batch_cap;
-  const uint32_t tiles = (cap + kTile - 1) / kTile;
-  return tiles < static_cast<uint32_t>(num_sms) ? tiles : static_cast<uint32_t>(num_sms);
+uint32_t train_grid(const TrainParams& p, int max_ctas) {
+  uint32_t tiles = 0;
+  for (int s = 0; s < p.steps; ++s) {
+    const uint32_t cap = p.batch[s].capacity < p.batch_cap ? p.batch[s].capacity : p.batch_cap;
+    const uint32_t t = (cap + kTile - 1) / kTile;
+    tiles = t > tiles ? t : tiles;
+  }
+  if (tiles == 0) tiles = 1;  // the prepare step still runs on an empty batch
+  uint32_t grid = tiles < static_cast<uint32_t>(max_ctas) ? tiles : static_cast<uint32_t>(max_ctas);
+  return grid < kMaxTrainCtas ? grid : kMaxTrainCtas;
 }
 
-cudaError_t launch_train_grad(const nrc_train_record* records, uint32_t* d_count, uint32_t capacity,
-                              uint32_t batch_cap, const __half* w16, float* grad, float* partials,
-                              nrc_optimizer_state* state, float loss_scale, float beta1, float beta2,
-                              float ema_alpha, bool do_prepare, double* loss_acc, unsigned long long* loss_count,
-                              uint32_t* err, int num_sms, cudaStream_t stream) {
-  uint32_t grid = train_grid(capacity, batch_cap, num_sms);
-  if (grid == 0) grid = 1;  // the prepare step still runs on an empty batch
-  train_grad_kernel<<<grid, kTrainThreads, kTrainSmemBytes, stream>>>(
-      records, d_count, capacity, batch_cap, w16, grad, partials, state, loss_scale, beta1, beta2, ema_alpha,
-      do_prepare ? 1 : 0, loss_acc, loss_count, err);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_adam(const uint32_t* d_count, uint32_t capacity, uint32_t batch_cap, float* grad,
-                        const float* partials, uint32_t grad_ctas, nrc_optimizer_entry* entries,
-                        const nrc_optimizer_state* state, __half* w16, __half* use16, float lr, float beta1,
-                        float beta2, float eps, float ema_alpha, float loss_scale, bool use_ema,
-                        cudaStream_t stream) {
-  const int threads = 256, blocks = (kParams + threads - 1) / threads;
-  adam_kernel<<<blocks, threads, 0, stream>>>(d_count, capacity, batch_cap, grad, partials, grad_ctas, entries, state,
-                                              w16, use16, lr, beta1, beta2, eps, ema_alpha, loss_scale,
-                                              use_ema ? 1 : 0);
-  return cudaGetLastError();
+cudaError_t launch_train(const TrainParams& p, const CUtensorMap* wmap, int max_ctas, cudaStream_t stream) {
+  if (p.steps < 1 || p.steps > NRC_TRAIN_BATCH_COUNT) return cudaErrorInvalidValue;
+  const uint32_t grid = train_grid(p, max_ctas);
+  // the grid barrier counts from zero in every launch
+  cudaError_t e = cudaMemsetAsync(p.sync, 0, sizeof(uint32_t), stream);
+  if (e != cudaSuccess) return e;
+  cudaLaunchAttribute attr;
+  attr.id = cudaLaunchAttributeCooperative;
+  attr.val.cooperative = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(kTrainThreads);
+  cfg.dynamicSmemBytes = kTrainSmemBytes;
+  cfg.stream = stream;
+  cfg.attrs = &attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, train_steps_kernel, p, *wmap);
 }
 
 }  // namespace nrc

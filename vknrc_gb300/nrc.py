@@ -28,7 +28,7 @@ EXPORTS = [
     "nrc_status_string", "nrc_default_config", "nrc_create", "nrc_destroy", "nrc_reset", "nrc_he_init_host",
     "nrc_encode", "nrc_sph_encode", "nrc_infer", "nrc_infer_encoded", "nrc_train", "nrc_gradient", "nrc_frame",
     "nrc_get_weights", "nrc_set_weights", "nrc_get_optimizer", "nrc_set_optimizer", "nrc_get_loss",
-    "nrc_get_error", "nrc_get_device_buffers", "nrc_train_noalloc",
+    "nrc_get_error", "nrc_get_device_buffers", "nrc_train_noalloc", "nrc_train_batches",
 ]
 
 
@@ -82,6 +82,7 @@ def lib(build_if_missing: bool = True) -> ctypes.CDLL:
     L.nrc_infer_encoded.argtypes = [vp, vp, vp, u32, vp, i32, vp]
     L.nrc_train.argtypes = [vp, vp, vp, u32, i32, vp]
     L.nrc_gradient.argtypes = [vp, vp, vp, u32, vp, vp]
+    L.nrc_train_batches.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), u32, i32, i32, vp]
     L.nrc_frame.argtypes = [vp, vp, vp, u32, vp, ctypes.POINTER(vp), ctypes.POINTER(vp), u32, vp]
     L.nrc_get_weights.argtypes = [vp, i32, vp]
     L.nrc_set_weights.argtypes = [vp, vp]
@@ -180,6 +181,14 @@ class Cache:
         cap = records.shape[0] if capacity is None else capacity
         check(lib().nrc_gradient(self.h, _ptr(records), _ptr(count), cap, _ptr(grad), _stream(stream)),
               "nrc_gradient")
+
+    def train_batches(self, records: Sequence, counts: Sequence, capacity=None, write_use_last=True, stream=None):
+        cap = records[0].shape[0] if capacity is None else capacity
+        nb = len(records)
+        recs = (ctypes.c_void_p * nb)(*[_ptr(r) for r in records])
+        cnts = (ctypes.c_void_p * nb)(*[_ptr(c) for c in counts])
+        check(lib().nrc_train_batches(self.h, recs, cnts, cap, nb, int(write_use_last), _stream(stream)),
+              "nrc_train_batches")
 
     def frame(self, eval_inputs, eval_count, out, train_records: Sequence, train_counts: Sequence,
               eval_capacity=None, train_capacity=None, stream=None):
