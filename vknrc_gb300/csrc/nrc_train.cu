@@ -48,19 +48,28 @@ constexpr uint32_t kActOff = kWeightSmemBytes;              // 43008
 constexpr uint32_t kGOff = kActOff + 6 * kActBytes;         // two gradient buffers
 constexpr uint32_t kStageOff = kGOff + 2 * kActBytes;
 constexpr uint32_t kTBarOff = kStageOff + 2 * kTRecTileBytes;
-constexpr uint32_t kTrainSmemBytes = kTBarOff + 128 + 1024;
+constexpr uint32_t kECacheOff = kTBarOff + 128;
 static_assert(kActOff % 1024 == 0 && kGOff % 1024 == 0 && kStageOff % 16 == 0, "alignment");
-static_assert(kTrainSmemBytes <= 227 * 1024, "shared memory");
 
 // TMEM columns: dW_l accumulators (M=64 layout) at 64*l, l = 0..5; scratch D at
 // 384..447; the A operand of the forward / dA MMAs (fp16 pairs) at 448..479.
 constexpr uint32_t kDCol = 384;
 constexpr uint32_t kACol = 448;
 
-// Parameter slices of the optimizer phase: float4 columns of the gradient.
+// Parameter slices of the optimizer phase: float4 columns of the gradient. The
+// grid has between kMinTrainCtas and kMaxTrainCtas CTAs: the first bounds a
+// CTA's slice (its optimizer entries stay in shared memory for the whole
+// launch), the second the staged partials (slice x CTAs <= kCols4 + grid).
 constexpr int kCols4 = kParams / 4;  // 5168
-constexpr uint32_t kMaxTrainCtas = 160;  // bounds the staged gradient slice (slice x CTAs <= kCols4 + grid)
+constexpr uint32_t kMinTrainCtas = 32;
+constexpr uint32_t kMaxTrainCtas = 160;
+constexpr uint32_t kMaxSlice4 = (kCols4 + kMinTrainCtas - 1) / kMinTrainCtas;  // 162
+constexpr uint32_t kTrainSmemBytes = kECacheOff + kMaxSlice4 * 4 * sizeof(nrc_optimizer_entry) + 1024;
 static_assert(kParams % 4 == 0, "parameters in float4 columns");
+static_assert(kTrainSmemBytes <= 227 * 1024, "shared memory");
+// The partials are staged behind act_0, which the next batch's first tile may
+// already be encoded into.
+static_assert(5 * kActBytes + 2 * kActBytes >= (kCols4 + kMaxTrainCtas) * 16, "staged slice fits");
 
 struct TrainBars {
   uint64_t rec_full[2];
@@ -70,9 +79,10 @@ struct TrainBars {
   uint64_t tile_done;  // MMA commit after the tile's last weight-gradient MMA
   uint64_t drain;
   uint64_t w_full;     // weights landed (TMA)
-  uint64_t p_full;     // partial-gradient slice landed (bulk copies)
   uint32_t tmem_base;
   uint32_t sync_ok;
+  uint32_t count[NRC_TRAIN_BATCH_COUNT];  // record counts as read at launch
+  nrc_optimizer_state st;                 // optimizer step state as read at launch
 };
 static_assert(sizeof(TrainBars) <= 128, "barrier area");
 
@@ -173,18 +183,19 @@ __device__ __forceinline__ bool grid_sync(uint32_t* counter, uint32_t target, ui
 }
 
 // One optimizer update (nrc_optimize.comp:32-54) of parameter i from its
-// gradient sum; exactly the CPU oracle's operation order.
+// gradient sum; exactly the CPU oracle's operation order. `e` is the CTA's
+// shared-memory copy of the entry; the entry is also written back to memory.
 struct AdamHyper {
   float lr, beta1, beta2, eps, ema_alpha, loss_scale;
   int use_ema;
 };
 
 __device__ __forceinline__ void adam_one(int i, float gsum, uint32_t n, const nrc_optimizer_state& st,
-                                         const AdamHyper& hp, nrc_optimizer_entry* __restrict__ entries,
-                                         __half* __restrict__ w16, __half* __restrict__ use16) {
+                                         const AdamHyper& hp, nrc_optimizer_entry& e,
+                                         nrc_optimizer_entry* __restrict__ entries, __half* __restrict__ w16,
+                                         __half* __restrict__ use16) {
   float g = __fdiv_rn(__fdiv_rn(gsum, static_cast<float>(n)), hp.loss_scale);
   if (isnan(g) || isinf(g)) g = 0.0f;
-  nrc_optimizer_entry e = entries[i];
   const float m = __fmaf_rn(hp.beta1, e.m, __fmul_rn(__fsub_rn(1.0f, hp.beta1), g));
   const float v = __fmaf_rn(hp.beta2, e.v, __fmul_rn(__fsub_rn(1.0f, hp.beta2), __fmul_rn(g, g)));
   const float hm = __fdiv_rn(m, __fsub_rn(1.0f, st.beta1_t));
@@ -211,6 +222,7 @@ __global__ void __launch_bounds__(kTrainThreads, 1)
   uint8_t* gbuf = smem + kGOff;
   uint8_t* stage = smem + kStageOff;
   TrainBars* B = reinterpret_cast<TrainBars*>(smem + kTBarOff);
+  nrc_optimizer_entry* ecache = reinterpret_cast<nrc_optimizer_entry*>(smem + kECacheOff);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   if (threadIdx.x == 0) {
@@ -223,7 +235,6 @@ __global__ void __launch_bounds__(kTrainThreads, 1)
     mbar_init(&B->tile_done, 1);
     mbar_init(&B->drain, 1);
     mbar_init(&B->w_full, 1);
-    mbar_init(&B->p_full, 1);
     mbar_fence_init();
   }
   if (warp == 0) {
@@ -232,11 +243,37 @@ __global__ void __launch_bounds__(kTrainThreads, 1)
   }
   // Everything below may read what the preceding kernel in the stream wrote.
   griddep_wait();
+
+  // This CTA's slice [c0, c1) of float4 gradient columns in the optimizer phase;
+  // its optimizer entries stay in shared memory for the whole launch (only this
+  // CTA updates them).
+  const uint32_t per = (kCols4 + gridDim.x - 1) / gridDim.x;  // <= kMaxSlice4
+  const uint32_t c0 = min(static_cast<uint32_t>(kCols4), blockIdx.x * per);
+  const uint32_t ncols = min(static_cast<uint32_t>(kCols4), c0 + per) - c0;
+  if (P.mode == kTrainStep) {
+    for (uint32_t k = threadIdx.x; k < 4 * ncols; k += blockDim.x) cp_async16(ecache + k, P.entries + 4 * c0 + k);
+    cp_async_commit();
+  }
+  // Every batch's record count and the optimizer step state, read once before
+  // CTA 0 writes them back (nrc_train_prepare.comp:16-29).
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < P.steps; ++s) B->count[s] = *reinterpret_cast<volatile const uint32_t*>(P.batch[s].d_count);
+    if (P.mode == kTrainStep) B->st = *P.state;
+  }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = __shfl_sync(0xffffffffu, B->tmem_base, 0);
   float* const my_partial = P.partials + static_cast<size_t>(blockIdx.x) * kParams;
+  nrc_optimizer_state st = B->st;  // advanced per batch in every CTA alike
+  if (P.mode == kTrainStep && blockIdx.x == 0 && threadIdx.x == 0) {
+    // Other CTAs read either the raw or the clamped count; both clamp to the same n.
+    for (int s = 0; s < P.steps; ++s) *P.batch[s].d_count = min(B->count[s], P.batch_cap);
+  }
+  auto batch_records = [&](int s) { return min(min(B->count[s], P.batch_cap), P.batch[s].capacity); };
+  auto tiles_of = [&](uint32_t num_tiles) {
+    return blockIdx.x < num_tiles ? (num_tiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0u;
+  };
 
   // Role state that persists across the batches (mbarrier phases).
   const int ew = warp - 1;   // epilogue warp index (warps 1..8)
@@ -251,33 +288,94 @@ __global__ void __launch_bounds__(kTrainThreads, 1)
   uint32_t ct = 0;              // tiles this CTA has processed over all batches
   uint32_t wloads = 0;          // weight loads issued to this CTA
   uint32_t barriers = 0;        // grid barriers passed
-  uint32_t pstages = 0;         // partial-gradient slices staged
   bool ok = true;
+  bool prefetched = false;      // the batch's first tile is already encoded and published
+  float target[3] = {0.f, 0.f, 0.f};
   double loss_local = 0.0;
   uint32_t loss_n = 0;
   const AdamHyper hp{P.lr, P.beta1, P.beta2, P.eps, P.ema_alpha, P.loss_scale, P.use_ema};
 
+  // Bulk copies of a batch's first two record tiles into the two stages.
+  auto issue_first_tiles = [&](const TrainBatch& bt, uint32_t n, uint32_t my_tiles) {
+    for (uint32_t k = 0; k < 2 && k < my_tiles; ++k) {
+      const uint32_t s = (ct + k) & 1;
+      issue_train_tile(bt.records, blockIdx.x + k * gridDim.x, n, stage + s * kTRecTileBytes, &B->rec_full[s]);
+    }
+  };
+  auto publish = [&]() {  // operand rows written: hand them to the tensor core
+    fence_proxy_async_smem();
+    tc_fence_before();
+    mbar_arrive(&B->a_ready);
+  };
+  // Epilogue warps: records of the CTA's tile `it` -> target, and the encoded
+  // input act_0 in shared memory and TMEM, published to the MMA warp.
+  auto prep_tile = [&](const TrainBatch& bt, uint32_t n, uint32_t it, uint32_t my_tiles) -> bool {
+    const uint32_t tile = blockIdx.x + it * gridDim.x;
+    const bool valid = row < static_cast<int>(min(static_cast<uint32_t>(kTile), n - tile * kTile));
+    const uint32_t s = ct & 1, use = ct >> 1;  // stage and its use count
+    if (!warp_all(mbar_wait(&B->rec_full[s], use & 1, kWaitLimitNs))) return false;
+    float r[kInFloats];
+    {
+      const float4* src = reinterpret_cast<const float4*>(stage + s * kTRecTileBytes + row * kTRecBytes);
+      float f[20];
+#pragma unroll
+      for (int k = 0; k < 5; ++k) {
+        const float4 v = valid ? src[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+        f[4 * k] = v.x;
+        f[4 * k + 1] = v.y;
+        f[4 * k + 2] = v.z;
+        f[4 * k + 3] = v.w;
+      }
+      target[0] = f[0];
+      target[1] = f[1];
+      target[2] = f[2];
+#pragma unroll
+      for (int k = 0; k < kInFloats; ++k) r[k] = f[6 + k];
+    }
+    mbar_arrive(&B->rec_empty[s]);
+    if (leader && it + 2 < my_tiles) {
+      if (mbar_wait(&B->rec_empty[s], use & 1, kWaitLimitNs))
+        issue_train_tile(bt.records, tile + 2 * gridDim.x, n, stage + s * kTRecTileBytes, &B->rec_full[s]);
+      else
+        atomicOr(P.err, kErrTimeout);
+    }
+    __syncwarp();
+    // the previous tile's last MMAs read act_0 and the gradient buffers
+    if (it > 0) {
+      if (!warp_all(mbar_wait(&B->tile_done, (ct - 1) & 1, kWaitLimitNs))) return false;
+      tc_fence_after();
+    }
+    uint32_t e[16];
+    if (h == 0)
+      encode_half0(r, e);
+    else
+      encode_half1(r, e);
+    if (!valid) {
+#pragma unroll
+      for (int k = 0; k < 16; ++k) e[k] = 0u;
+    }
+    tmem_st16(a_lane, e);
+    store_half(act, row, h, e);
+    publish();
+    return true;
+  };
+
+  if (leader && P.steps > 0) {
+    const uint32_t n0 = batch_records(0);
+    issue_first_tiles(P.batch[0], n0, tiles_of((n0 + kTile - 1) / kTile));
+  }
+
   for (int step = 0; step < P.steps && ok; ++step) {
     const TrainBatch bt = P.batch[step];
-    const uint32_t raw = *reinterpret_cast<volatile const uint32_t*>(bt.d_count);
-    const uint32_t clamped = min(raw, P.batch_cap);
-    const uint32_t n = min(clamped, bt.capacity);
+    const uint32_t n = batch_records(step);
     const uint32_t num_tiles = (n + kTile - 1) / kTile;
-    const uint32_t my_tiles = blockIdx.x < num_tiles ? (num_tiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
-    __syncthreads();  // every thread has read the count before CTA 0 may rewrite it
-    if (P.mode == kTrainStep && blockIdx.x == 0 && threadIdx.x == 0) {
-      // nrc_train_prepare.comp; other CTAs read either the raw or the clamped
-      // count, and both clamp to the same n.
-      *bt.d_count = clamped;
-      if (n > 0) {  // the optimizer phase below updates exactly when records were processed
-        nrc_optimizer_state st = *P.state;
-        st.t += 1;
-        st.beta1_t *= P.beta1;
-        st.beta2_t *= P.beta2;
-        st.alpha_t_1 = st.alpha_t;
-        st.alpha_t *= P.ema_alpha;
-        *P.state = st;
-      }
+    const uint32_t my_tiles = tiles_of(num_tiles);
+    if (P.mode == kTrainStep && n > 0) {  // the optimizer phase updates exactly when records were processed
+      st.t += 1;
+      st.beta1_t *= P.beta1;
+      st.beta2_t *= P.beta2;
+      st.alpha_t_1 = st.alpha_t;
+      st.alpha_t *= P.ema_alpha;
     }
     if (threadIdx.x == 0 && my_tiles > 0) stage_weights_tma(smem_w, &wmap, &B->w_full);
 
@@ -355,73 +453,16 @@ __global__ void __launch_bounds__(kTrainThreads, 1)
         tc_fence_after();
         return ok;
       };
-      auto publish = [&]() {  // operand rows written: hand them to the tensor core
-        fence_proxy_async_smem();
-        tc_fence_before();
-        mbar_arrive(&B->a_ready);
-      };
-      // The record stages are free: every tile of the previous batch was read
-      // before the grid barrier this batch starts after.
-      if (leader) {
-        for (uint32_t k = 0; k < 2 && k < my_tiles; ++k) {
-          const uint32_t s = (ct + k) & 1;
-          issue_train_tile(bt.records, blockIdx.x + k * gridDim.x, n, stage + s * kTRecTileBytes, &B->rec_full[s]);
-        }
-      }
       for (uint32_t it = 0; it < my_tiles && ok; ++it, ++ct) {
         const uint32_t tile = blockIdx.x + it * gridDim.x;
         const uint32_t rows_valid = min(static_cast<uint32_t>(kTile), n - tile * kTile);
         const bool valid = row < static_cast<int>(rows_valid);
         const bool last = it + 1 == my_tiles;
-        const uint32_t s = ct & 1, use = ct >> 1;  // stage and its use count
-        ok = warp_all(mbar_wait(&B->rec_full[s], use & 1, kWaitLimitNs));
-        if (!ok) break;
-        float r[kInFloats], target[3];
-        {
-          const float4* src = reinterpret_cast<const float4*>(stage + s * kTRecTileBytes + row * kTRecBytes);
-          float f[20];
-#pragma unroll
-          for (int k = 0; k < 5; ++k) {
-            const float4 v = valid ? src[k] : make_float4(0.f, 0.f, 0.f, 0.f);
-            f[4 * k] = v.x;
-            f[4 * k + 1] = v.y;
-            f[4 * k + 2] = v.z;
-            f[4 * k + 3] = v.w;
-          }
-          target[0] = f[0];
-          target[1] = f[1];
-          target[2] = f[2];
-#pragma unroll
-          for (int k = 0; k < kInFloats; ++k) r[k] = f[6 + k];
-        }
-        mbar_arrive(&B->rec_empty[s]);
-        if (leader && it + 2 < my_tiles) {
-          if (mbar_wait(&B->rec_empty[s], use & 1, kWaitLimitNs))
-            issue_train_tile(bt.records, tile + 2 * gridDim.x, n, stage + s * kTRecTileBytes, &B->rec_full[s]);
-          else
-            atomicOr(P.err, kErrTimeout);
-        }
-        __syncwarp();
-        // the previous tile's last MMAs read act_0 and the gradient buffers
-        if (it > 0) {
-          ok = warp_all(mbar_wait(&B->tile_done, (ct - 1) & 1, kWaitLimitNs));
+        if (!(it == 0 && prefetched)) {
+          ok = prep_tile(bt, n, it, my_tiles);
           if (!ok) break;
-          tc_fence_after();
         }
-        {
-          uint32_t e[16];
-          if (h == 0)
-            encode_half0(r, e);
-          else
-            encode_half1(r, e);
-          if (!valid) {
-#pragma unroll
-            for (int k = 0; k < 16; ++k) e[k] = 0u;
-          }
-          tmem_st16(a_lane, e);
-          store_half(act, row, h, e);
-        }
-        publish();
+        prefetched = false;
         // forward: act_{l+1} = fp16(relu(W_l act_l))
         for (int l = 0; l < 5; ++l) {
           if (!wait_d()) break;
@@ -499,86 +540,80 @@ __global__ void __launch_bounds__(kTrainThreads, 1)
     if (!ok && lane == 0) atomicOr(P.err, kErrTimeout);
     ok = __syncthreads_and(ok) != 0;  // one decision per CTA from here on
 
+    // The record stages are free again: the next batch's first tiles land
+    // during the grid barrier and the optimizer phase.
+    const bool has_next = step + 1 < P.steps;
+    const uint32_t n_next = has_next ? batch_records(step + 1) : 0u;
+    const uint32_t tiles_next = tiles_of((n_next + kTile - 1) / kTile);
+    if (ok && leader && tiles_next > 0) issue_first_tiles(P.batch[step + 1], n_next, tiles_next);
+
     // ------------------------------------------- reduction + optimizer --
     if (!grid_sync(P.sync, ++barriers * gridDim.x, &B->sync_ok)) {
       ok = false;
       if (threadIdx.x == 0) atomicOr(P.err, kErrTimeout);
       break;
     }
-    {
-      // This CTA's slice [c0, c1) of float4 gradient columns. The slice of every
-      // partial (one contiguous run per CTA that had tiles) is staged into the
-      // free activation buffers with bulk copies, summed over the partials in a
-      // fixed order (run-to-run identical), and the parameters are updated.
-      const uint32_t active = min(gridDim.x, num_tiles);
-      const uint32_t per = (kCols4 + gridDim.x - 1) / gridDim.x;
-      const uint32_t c0 = min(static_cast<uint32_t>(kCols4), blockIdx.x * per);
-      const uint32_t c1 = min(static_cast<uint32_t>(kCols4), c0 + per);
-      const uint32_t ncols = c1 - c0;
-      float4* stg = reinterpret_cast<float4*>(act);   // [active][ncols], <= 85 KB of the 96 KB
-      float4* red = reinterpret_cast<float4*>(gbuf);  // 8 x 32
-      static_assert(6 * kActBytes >= (kCols4 + kMaxTrainCtas) * 16, "staged slice fits the activation buffers");
-      if (n > 0 && ncols > 0) {
-        if (threadIdx.x == 0) {
-          const uint32_t row_bytes = ncols * 16;
-          mbar_arrive_expect_tx(&B->p_full, row_bytes * active);
-          for (uint32_t r = 0; r < active; ++r)
-            bulk_g2s(stg + static_cast<size_t>(r) * ncols, P.partials + static_cast<size_t>(r) * kParams + 4 * c0,
-                     row_bytes, &B->p_full);
-        }
-        if (!mbar_wait(&B->p_full, pstages & 1, kWaitLimitNs)) {
-          ok = false;
-          atomicOr(P.err, kErrTimeout);
-        }
-        ++pstages;
-        const int col = threadIdx.x & 31, rg = threadIdx.x >> 5;  // 8 row groups (threads 0..255)
-        for (uint32_t cb = 0; cb < ncols; cb += 32) {
-          const uint32_t cc = cb + col;
-          if (rg < 8) {
-            float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (ok && cc < ncols) {
-              for (uint32_t r = rg; r < active; r += 8) {
-                const float4 v = stg[static_cast<size_t>(r) * ncols + cc];
-                acc.x += v.x;
-                acc.y += v.y;
-                acc.z += v.z;
-                acc.w += v.w;
-              }
-            }
-            red[rg * 32 + col] = acc;
-          }
-          __syncthreads();
-          if (rg == 0 && cc < ncols) {  // row 0 of the staged slice now holds the sums
-            float4 g = red[col];
-#pragma unroll
-            for (int k = 1; k < 8; ++k) {
-              const float4 v = red[k * 32 + col];
-              g.x += v.x;
-              g.y += v.y;
-              g.z += v.z;
-              g.w += v.w;
-            }
-            stg[cc] = g;
-          }
-          __syncthreads();
-        }
-        if (P.mode == kTrainStep) {
-          const nrc_optimizer_state st = *P.state;
-          __half* use16 = bt.write_use ? P.use16 : nullptr;
-          const float* sums = reinterpret_cast<const float*>(stg);
-          for (uint32_t k = threadIdx.x; k < 4 * ncols; k += blockDim.x)
-            adam_one(4 * c0 + k, sums[k], n, st, hp, P.entries, P.w16, use16);
-        } else {
-          for (uint32_t k = threadIdx.x; k < ncols; k += blockDim.x)
-            reinterpret_cast<float4*>(P.grad_out)[c0 + k] = stg[k];
-        }
-      } else if (P.mode == kGradientOnly) {
-        for (uint32_t k = threadIdx.x; k < ncols; k += blockDim.x)
-          reinterpret_cast<float4*>(P.grad_out)[c0 + k] = make_float4(0.f, 0.f, 0.f, 0.f);  // no records
+    // Gather this CTA's slice of every partial (one per CTA that had tiles)
+    // behind act_0, many 16-byte copies in flight per thread.
+    float4* stg = reinterpret_cast<float4*>(act + kActBytes);  // [active][ncols]
+    const uint32_t active = min(gridDim.x, num_tiles);
+    const bool reduce = n > 0 && ncols > 0;
+    if (reduce) {
+      const uint32_t total = active * ncols;
+      for (uint32_t i = threadIdx.x; i < total; i += blockDim.x) {
+        const uint32_t r = i / ncols, cc = i - r * ncols;
+        cp_async16(stg + i, P.partials + static_cast<size_t>(r) * kParams + 4 * (c0 + cc));
       }
-      ok = __syncthreads_and(ok) != 0;
+      cp_async_commit();
     }
-    if (step + 1 < P.steps) {  // publish the new weights before the next batch loads them
+    // Meanwhile the epilogue warps encode the next batch's first tile into act_0.
+    if (ok && warp > 0 && tiles_next > 0) {
+      prefetched = prep_tile(P.batch[step + 1], n_next, 0, tiles_next);
+      if (!prefetched) {
+        ok = false;
+        if (lane == 0) atomicOr(P.err, kErrTimeout);
+      }
+    }
+    if (reduce) cp_async_wait_all();
+    ok = __syncthreads_and(ok) != 0;
+    if (ok && reduce) {
+      // Four threads per float4 column sum every fourth partial, then combine
+      // as (s0 + s1) + (s2 + s3): a fixed order, so runs are identical. Thread
+      // `part` then owns parameter 4 * column + part.
+      const uint32_t part = threadIdx.x & 3;
+      __half* use16 = bt.write_use ? P.use16 : nullptr;
+      for (uint32_t cb = 0; cb < ncols; cb += kTrainThreads / 4) {
+        const uint32_t cc = cb + (threadIdx.x >> 2);
+        float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (cc < ncols) {
+          for (uint32_t r = part; r < active; r += 4) {
+            const float4 v = stg[static_cast<size_t>(r) * ncols + cc];
+            acc.x += v.x;
+            acc.y += v.y;
+            acc.z += v.z;
+            acc.w += v.w;
+          }
+        }
+#pragma unroll
+        for (int off = 1; off <= 2; off <<= 1) {
+          acc.x += __shfl_xor_sync(0xffffffffu, acc.x, off);
+          acc.y += __shfl_xor_sync(0xffffffffu, acc.y, off);
+          acc.z += __shfl_xor_sync(0xffffffffu, acc.z, off);
+          acc.w += __shfl_xor_sync(0xffffffffu, acc.w, off);
+        }
+        if (cc < ncols) {
+          const float gsum = part == 0 ? acc.x : part == 1 ? acc.y : part == 2 ? acc.z : acc.w;
+          const uint32_t k = 4 * cc + part;  // parameter index within the slice
+          if (P.mode == kTrainStep)
+            adam_one(4 * c0 + k, gsum, n, st, hp, ecache[k], P.entries, P.w16, use16);
+          else
+            P.grad_out[4 * c0 + k] = gsum;
+        }
+      }
+    } else if (ok && P.mode == kGradientOnly) {
+      for (uint32_t k = threadIdx.x; k < 4 * ncols; k += blockDim.x) P.grad_out[4 * c0 + k] = 0.0f;  // no records
+    }
+    if (has_next) {  // publish the new weights before the next batch loads them
       if (!grid_sync(P.sync, ++barriers * gridDim.x, &B->sync_ok)) {
         ok = false;
         if (threadIdx.x == 0) atomicOr(P.err, kErrTimeout);
@@ -586,6 +621,10 @@ __global__ void __launch_bounds__(kTrainThreads, 1)
       }
     }
   }
+  cp_async_wait_all();  // entry loads of a launch whose batches were all empty
+  // Every CTA has read the step state at launch and passed at least one grid
+  // barrier since, so CTA 0 may now write the advanced state.
+  if (P.mode == kTrainStep && ok && barriers > 0 && blockIdx.x == 0 && threadIdx.x == 0) *P.state = st;
 
   if (P.loss_acc != nullptr && warp > 0) {
 #pragma unroll
@@ -620,21 +659,16 @@ cudaError_t configure_train_kernels() {
 
 uint32_t train_smem_bytes() { return kTrainSmemBytes; }
 
-uint32_t train_grid(const TrainParams& p, int max_ctas) {
-  uint32_t tiles = 0;
-  for (int s = 0; s < p.steps; ++s) {
-    const uint32_t cap = p.batch[s].capacity < p.batch_cap ? p.batch[s].capacity : p.batch_cap;
-    const uint32_t t = (cap + kTile - 1) / kTile;
-    tiles = t > tiles ? t : tiles;
-  }
-  if (tiles == 0) tiles = 1;  // the prepare step still runs on an empty batch
-  uint32_t grid = tiles < static_cast<uint32_t>(max_ctas) ? tiles : static_cast<uint32_t>(max_ctas);
-  return grid < kMaxTrainCtas ? grid : kMaxTrainCtas;
+// One CTA per SM up to kMaxTrainCtas, whatever the batch sizes: CTAs without
+// tiles in a batch still own a slice of the parameters in its optimizer phase.
+uint32_t train_grid(const TrainParams&, int max_ctas) {
+  return static_cast<uint32_t>(max_ctas) < kMaxTrainCtas ? static_cast<uint32_t>(max_ctas) : kMaxTrainCtas;
 }
 
 cudaError_t launch_train(const TrainParams& p, const CUtensorMap* wmap, int max_ctas, cudaStream_t stream) {
   if (p.steps < 1 || p.steps > NRC_TRAIN_BATCH_COUNT) return cudaErrorInvalidValue;
   const uint32_t grid = train_grid(p, max_ctas);
+  if (grid < kMinTrainCtas) return cudaErrorInvalidConfiguration;
   // the grid barrier counts from zero in every launch
   cudaError_t e = cudaMemsetAsync(p.sync, 0, sizeof(uint32_t), stream);
   if (e != cudaSuccess) return e;

@@ -84,6 +84,17 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
       : "memory");
 }
 
+// 16-byte asynchronous copy global -> shared through the L2 (no L1 allocation).
+// Many of these in flight per thread hide the latency of gathering scattered
+// 16-byte pieces; cp_async_wait_all() waits for this thread's copies.
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 // 2-D tiled tensor load global -> shared through a tensor map (TMA); the
 // innermost coordinate c0 times the element size must be a multiple of 16 bytes.
 __device__ __forceinline__ void tma_load_2d(void* dst, const void* tmap, int32_t c0, int32_t c1, uint64_t* bar) {
