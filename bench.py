@@ -42,7 +42,7 @@ OUT_BYTES = 12
 def parse_args():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=1000)
+    p.add_argument("--steps", type=int, default=8000)
     p.add_argument("--warmup", type=int, default=20)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--eval-frames", type=int, default=4, help="distinct frames of eval records rotated")
@@ -50,8 +50,6 @@ def parse_args():
     p.add_argument("--e2e-steps", type=int, default=100)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-plain", action="store_true")
-    p.add_argument("--deterministic", type=int, default=1,
-                   help="1: fixed-order gradient reduction (per-CTA partials); 0: fp32 atomics")
     return p.parse_args()
 
 
@@ -169,11 +167,12 @@ def barrier(world: int):
 
 
 # ------------------------------------------------------------ CPU baseline --
-def cpu_frame_sample(steps: int, warmup: int, fraction: int = 512):
+def cpu_frame_sample(steps: int, warmup: int, fraction: int = 64, budget_s: float | None = None):
     """Times the CPU oracle (restatement of the reference's shader math) on all
     host cores: each step is 1/fraction of a 1080p frame (queries encoded and
     evaluated, train records encoded, back-propagated and one optimizer step).
-    Returns (queries/s at full-frame composition, threads, sample text)."""
+    With budget_s, steps run until that much time has passed (at least `steps`).
+    Returns (queries/s at full-frame composition, threads, sample text, s/frame)."""
     import numpy as np
 
     from oracle import oracle as O
@@ -202,8 +201,11 @@ def cpu_frame_sample(steps: int, warmup: int, fraction: int = 512):
     for _ in range(warmup):
         step()
     t0 = time.perf_counter()
-    for _ in range(steps):
+    done = 0
+    while done < steps or (budget_s is not None and time.perf_counter() - t0 < budget_s):
         step()
+        done += 1
+    steps = done
     dt = (time.perf_counter() - t0) / steps
     frame_s = dt * fraction
     sample = (f"{steps} steps of 1/{fraction} of a 1080p frame ({q} queries + {r} train records, "
@@ -214,17 +216,13 @@ def cpu_frame_sample(steps: int, warmup: int, fraction: int = 512):
 def reference_arm(args, world, rank):
     if rank != 0:
         return
-    steps = max(1, args.steps)
-    warm = max(0, args.warmup)
-    # bounded sample so that the whole run ends within minutes
-    budget = 60.0
-    qps, threads, sample, frame_s = cpu_frame_sample(1, 1)
-    per_step = frame_s / 512
-    steps_run = max(1, min(steps, int(budget / max(per_step, 1e-6))))
-    qps, threads, sample, frame_s = cpu_frame_sample(steps_run, min(warm, 3))
+    warm = min(max(0, args.warmup), 3)
+    # a bounded sample (about 60 s of CPU work) so that the whole run ends within minutes
+    qps, threads, sample, frame_s = cpu_frame_sample(1, warm, budget_s=60.0)
+    steps_run = int(sample.split(" ", 1)[0])
     line = {
         "impl": "reference", "metric": METRIC, "value": qps, "unit": "queries/s", "n_gpus": 1, "steps": steps_run,
-        "warmup": min(warm, 3), "ms_per_step": frame_s * 1e3, "higher_is_better": True, "scaling": "weak",
+        "warmup": warm, "requested_steps": args.steps, "ms_per_step": frame_s * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 math, fp16 activations (CPU restatement)", "data": "synthetic",
         "config": {"workload": "1080p frame: 2,073,600 queries + 4 x 16,384 train records"},
         "train_records_per_s": B * R / frame_s,
@@ -289,8 +287,7 @@ def ours_arm(args, world, rank, local):
 
     stream = torch.cuda.current_stream()
     evals, trains = make_pools(args, rank)
-    cache = Cache(seed=1234 + rank, learning_rate=1e-3, beta1=0.9, beta2=0.99, epsilon=1e-8,
-                  deterministic=args.deterministic)
+    cache = Cache(seed=1234 + rank, learning_rate=1e-3, beta1=0.9, beta2=0.99, epsilon=1e-8)
     out = torch.empty((Q, 3), dtype=torch.float32, device="cuda")
     eval_cnt = torch.tensor([Q], dtype=torch.int32, device="cuda")
     train_cnt = [torch.tensor([R], dtype=torch.int32, device="cuda") for _ in range(B)]
@@ -387,7 +384,7 @@ def ours_arm(args, world, rank, local):
             "records": "seeded synthetic; 4 distinct eval frames (464 MB) and 8 distinct train frames rotated",
             "l2": "inputs larger than L2: each frame's 116 MB of records is cold (4-frame rotation)",
             "hyper": "lr 1e-3, beta 0.9/0.99, eps 1e-8",
-            "gradient_reduction": "deterministic per-CTA partials" if args.deterministic else "fp32 atomics",
+            "gradient_reduction": "per-CTA partials summed in a fixed order (run-to-run identical)",
             "parallelism": f"replicas x{world}",
         },
         "train_records_per_s": world * B * R * K / total_s,
@@ -412,7 +409,7 @@ def ours_arm(args, world, rank, local):
         result["plain_fp16"] = {"queries_per_s": plain, "what": "nrc_encode + 6 torch fp16 GEMMs (cuBLAS), infer only",
                                 "fused_infer_queries_per_s": Q / infer_s}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        qps, threads, sample, _ = cpu_frame_sample(40, 2)
+        qps, threads, sample, _ = cpu_frame_sample(1, 2, budget_s=12.0)
         result["cpu_baseline"] = {"value": qps, "unit": "queries/s", "cores": threads, "kind": "port",
                                   "sample": sample}
     cache.close()

@@ -88,7 +88,8 @@ typedef struct nrc_config {
   float ema_alpha;
   float loss_scale;
   uint32_t use_ema_weights; /* use_weights receives the EMA instead of the weights */
-  uint32_t deterministic;   /* 1: gradients reduced in a fixed order (run-to-run identical) */
+  uint32_t deterministic;   /* kept for layout; weight gradients are always summed in a fixed
+                               order, so results are run-to-run identical either way */
   uint32_t track_loss;      /* 1: accumulate the relative-L2 loss (check path, FP64 sum) */
   uint64_t seed;            /* He initialisation seed */
 } nrc_config;

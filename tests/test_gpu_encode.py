@@ -19,6 +19,31 @@ def test_encode_bit_exact_vs_oracle(cuda, oracle, golden):
     assert np.array_equal(got, oracle.encode(rec))
 
 
+def test_encode_edge_positions_bit_exact(cuda, oracle):
+    """Positions where the frequency features' roundings are delicate: exact
+    dyadic points, values just off them, tiny and subnormal magnitudes, and
+    magnitudes where p * 2^11 overflows (the kernel's fallback form)."""
+    from vknrc_gb300 import Cache, synthetic as S
+
+    vals = np.array([0.0, -0.0, 1.0, 0.5, 0.25, 1.0 / 2048, 3.0 / 4096, 1e-30, 1e-40, -1e-40, 0.999999,
+                     np.nextafter(np.float32(0.5), np.float32(1)), np.nextafter(np.float32(0.5), np.float32(0)),
+                     -0.75, 7.3, -1234.5, 2.0 ** 99, 1.5 * 2.0 ** 100, 1e30, 3e38, -3e38, np.inf, -np.inf],
+                    dtype=np.float32)
+    rec = S.inputs(S.rng_for(5), vals.size * 3)
+    rec[:, 0] = np.tile(vals, 3)
+    rec[:, 1] = np.roll(np.tile(vals, 3), 7)
+    rec[:, 2] = np.roll(np.tile(vals, 3), 13)
+    with Cache() as c:
+        out = cuda.full((rec.shape[0], 64), -1, dtype=cuda.int16, device="cuda")
+        c.encode(dev(rec), count(rec.shape[0]), out)
+        got = host(out).view(np.uint16)
+    want = oracle.encode(rec)
+    nan_got = np.isnan(got.view(np.float16))
+    nan_want = np.isnan(want.view(np.float16))
+    assert np.array_equal(nan_got, nan_want)
+    assert np.array_equal(got[~nan_got], want[~nan_want])
+
+
 def test_encode_vs_reference_golden(cuda, golden):
     from vknrc_gb300 import Cache
 

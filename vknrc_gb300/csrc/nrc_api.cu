@@ -155,7 +155,7 @@ int nrc_default_config(nrc_config* cfg) {
   cfg->ema_alpha = 0.99f;       // shader/src/Constant.glsl:13
   cfg->loss_scale = 1.0f;       // shader/src/Constant.glsl:8
   cfg->use_ema_weights = 0;     // src/VkNRCState.hpp:36
-  cfg->deterministic = 0;
+  cfg->deterministic = 1;       // the only reduction there is
   cfg->track_loss = 0;
   cfg->seed = 0;
   return NRC_OK;

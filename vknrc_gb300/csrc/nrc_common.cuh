@@ -63,6 +63,18 @@ __device__ __forceinline__ float enc_tri(float p, float scale) {
   return __fmaf_rn(2.0f, fabsf(t), -1.0f);
 }
 
+// The same value from h = p 2^(k-1) - 0.25, one multiply fewer. Scaling by a
+// power of two commutes with rounding while nothing overflows or turns
+// subnormal, so h = y / 2 and floor(h) = f exactly, d = h - f = m / 2 exactly,
+// and t = 2d - 1 rounds as m - 1 does: every rounding is the one enc_tri makes.
+// Valid for |p| < 2^100 (p * 2^11 finite); NaN gives NaN in both.
+__device__ __forceinline__ float enc_tri_h(float p, float half_scale) {
+  const float h = __fmaf_rn(p, half_scale, -0.25f);
+  const float d = __fsub_rn(h, floorf(h));
+  const float t = __fmaf_rn(2.0f, d, -1.0f);
+  return __fmaf_rn(2.0f, fabsf(t), -1.0f);
+}
+
 // _quartic_cdf at radius 1/4 (NRCRecord.glsl:51-56), u = 4 (edge - x).
 __device__ __forceinline__ float enc_qcdf(float edge4, float x) {
   const float u = __fmaf_rn(x, -4.0f, edge4);
@@ -72,10 +84,45 @@ __device__ __forceinline__ float enc_qcdf(float edge4, float x) {
   return __saturatef(c);
 }
 
+// Two fp32 lanes in one 64-bit register: Blackwell's packed fp32 arithmetic
+// (fma/mul .f32x2) does both lanes with the scalar instructions' IEEE rounding.
+__device__ __forceinline__ uint64_t f32x2(float lo, float hi) {
+  uint64_t r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ void f32x2_split(uint64_t v, float& lo, float& hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ uint64_t fma_x2(uint64_t a, uint64_t b, uint64_t c) {
+  uint64_t r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+  return r;
+}
+__device__ __forceinline__ uint64_t mul_x2(uint64_t a, uint64_t b) {
+  uint64_t r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+
+// enc_qcdf at two edges for one x, lane by lane the same operations.
+__device__ __forceinline__ void enc_qcdf_x2(float edge4_lo, float edge4_hi, float x, float& c_lo, float& c_hi) {
+  const uint64_t u = fma_x2(f32x2(x, x), f32x2(-4.0f, -4.0f), f32x2(edge4_lo, edge4_hi));
+  const uint64_t u2 = mul_x2(u, u);
+  const uint64_t s =
+      fma_x2(fma_x2(u2, f32x2(0.2f, 0.2f), f32x2(-0.6666667f, -0.6666667f)), u2, f32x2(1.0f, 1.0f));
+  const uint64_t c = fma_x2(mul_x2(f32x2(0.9375f, 0.9375f), u), s, f32x2(0.5f, 0.5f));
+  f32x2_split(c, c_lo, c_hi);
+  c_lo = __saturatef(c_lo);
+  c_hi = __saturatef(c_hi);
+}
+
 // NRCOneBlob4Encode (NRCRecord.glsl:58-63), packed to two f16x2 words.
 __device__ __forceinline__ void enc_oneblob4(float x, uint32_t& w0, uint32_t& w1) {
-  const float f0 = enc_qcdf(0.0f, x), f1 = enc_qcdf(1.0f, x), f2 = enc_qcdf(2.0f, x);
-  const float f3 = enc_qcdf(3.0f, x), f4 = enc_qcdf(4.0f, x);
+  float f0, f1, f2, f3;
+  enc_qcdf_x2(0.0f, 1.0f, x, f0, f1);
+  enc_qcdf_x2(2.0f, 3.0f, x, f2, f3);
+  const float f4 = enc_qcdf(4.0f, x);
   w0 = pack_f16x2(__fsub_rn(f1, f0), __fsub_rn(f2, f1));
   w1 = pack_f16x2(__fsub_rn(f3, f2), __fsub_rn(f4, f3));
 }
@@ -102,11 +149,16 @@ __device__ __forceinline__ float enc_expf(float x) {
 // Frequency features k0 .. k0+2n-1 of one coordinate -> n words.
 template <int K0, int N>
 __device__ __forceinline__ void enc_freq(float p, uint32_t* o) {
+  if (fabsf(p) < 0x1p100f) {
 #pragma unroll
-  for (int i = 0; i < N; ++i) {
-    constexpr int kBase = K0;
-    o[i] = pack_f16x2(enc_tri(p, static_cast<float>(1 << (kBase + 2 * i))),
-                      enc_tri(p, static_cast<float>(1 << (kBase + 2 * i + 1))));
+    for (int i = 0; i < N; ++i)
+      o[i] = pack_f16x2(enc_tri_h(p, 0.5f * static_cast<float>(1 << (K0 + 2 * i))),
+                        enc_tri_h(p, 0.5f * static_cast<float>(1 << (K0 + 2 * i + 1))));
+  } else {
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      o[i] = pack_f16x2(enc_tri(p, static_cast<float>(1 << (K0 + 2 * i))),
+                        enc_tri(p, static_cast<float>(1 << (K0 + 2 * i + 1))));
   }
 }
 
