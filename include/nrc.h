@@ -155,6 +155,39 @@ NRC_API int nrc_infer(nrc_context* ctx, const nrc_input* d_inputs, const uint32_
 NRC_API int nrc_infer_encoded(nrc_context* ctx, const uint16_t* d_encoded, const uint32_t* d_count, uint32_t capacity,
                       float* d_out_rgb, int weight_set, void* stream);
 
+/* Where query results go when a query carries a destination word
+ * (nrc_inference.comp:50-73; the word's encoding is NRCRecord.glsl:19-33):
+ *  - 0xFFFFFFFF: nowhere;
+ *  - bit 0 = 0, screen: x = (dst >> 1) & 0x7FFF, y = dst >> 16. Pixel (x, y) of
+ *    bias_factor_r (rgba32f, row-major [height][width][4]: rgb = bias, a =
+ *    factor.r) and factor_gb (rg32f, [height][width][2]) becomes
+ *    (bias + (factor.r, factor.g, factor.b) * pred, 0);
+ *  - bit 0 = 1, train: batch b = (dst >> 1) & 3, records l = (dst >> 3) & 0x3FFF
+ *    to r = dst >> 17 inclusive: bias_rgb += factor_rgb * pred (self-training
+ *    target completion).
+ * pred = max(query output, 0); each update is one fused multiply-add per
+ * channel. Pixels outside width x height, records at or beyond a batch's
+ * capacity and batches whose pointer is null are skipped (the reference relies
+ * on robust image access and on well-formed ranges). The updates are plain
+ * read-modify-writes, as in the reference: destinations of one call must not
+ * repeat. */
+typedef struct nrc_scatter_targets {
+  float* bias_factor_r;
+  const float* factor_gb;
+  uint32_t width, height;
+  nrc_train_record* train_records[NRC_TRAIN_BATCH_COUNT];
+  uint32_t train_capacity[NRC_TRAIN_BATCH_COUNT];
+} nrc_scatter_targets;
+
+/* Cache query with the reference's destination epilogue fused in: as nrc_infer
+ * on d_inputs, then each query's prediction is written where d_dst[i] says
+ * (nrc_scatter_targets). d_out_rgb may be null; if given it also receives the
+ * clamped predictions. Replaces the whole of nrc_inference.comp:30-73 for
+ * unpacked records. */
+NRC_API int nrc_infer_scatter(nrc_context* ctx, const nrc_input* d_inputs, const uint32_t* d_dst,
+                              const uint32_t* d_count, uint32_t capacity, const nrc_scatter_targets* targets,
+                              float* d_out_rgb, int weight_set, void* stream);
+
 /* One training step on min(*d_count, train_batch_size, capacity) records:
  * nrc_train_prepare.comp (count clamp, written back to *d_count; step state
  * advanced only if n > 0) + nrc_gradient.comp (fused encode, forward,
@@ -186,6 +219,16 @@ NRC_API int nrc_gradient(nrc_context* ctx, const nrc_train_record* d_records, co
 NRC_API int nrc_frame(nrc_context* ctx, const nrc_input* d_eval_inputs, const uint32_t* d_eval_count, uint32_t eval_capacity,
               float* d_out_rgb, const nrc_train_record* const* d_train_records, uint32_t* const* d_train_counts,
               uint32_t train_capacity, void* stream);
+
+/* One frame of the reference schedule with the destination epilogue
+ * (src/rg/NRCRenderGraph.cpp:46-80, nrc_inference.comp:50-73): the queries
+ * update the screen images and complete the train records' targets in
+ * targets->train_records, then NRC_TRAIN_BATCH_COUNT chained training steps
+ * run on those records (targets->train_capacity[b] each, counts in
+ * d_train_counts[b]), the last one writing use_weights. */
+NRC_API int nrc_frame_scatter(nrc_context* ctx, const nrc_input* d_eval_inputs, const uint32_t* d_eval_dst,
+                              const uint32_t* d_eval_count, uint32_t eval_capacity,
+                              const nrc_scatter_targets* targets, uint32_t* const* d_train_counts, void* stream);
 
 /* One training step with nrc_train's semantics that allocates no device memory.
  * No counterpart in the reference: it serves callers that cannot call cudaMalloc,

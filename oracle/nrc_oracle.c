@@ -348,13 +348,11 @@ static void train_range(void* p, int64_t b, int64_t e, int tid) {
   x->loss[tid] = loss;
 }
 
-void oracle_train_grad(const uint16_t* w, const uint16_t* enc, const float* target, int64_t n,
-                       float loss_scale, int mode, double* grad, double* grad_abs, double* loss_sum,
-                       int nthreads) {
+static void train_grad_cached(const wcache* c, const uint16_t* enc, const float* target, int64_t n,
+                              float loss_scale, int mode, double* grad, double* grad_abs, double* loss_sum,
+                              int nthreads) {
   if (nthreads <= 0) nthreads = 1;
   if (nthreads > 256) nthreads = 256;
-  wcache* c = (wcache*)malloc(sizeof(wcache));
-  load_weights(w, c);
   train_ctx* x = (train_ctx*)calloc(1, sizeof(train_ctx));
   x->c = c;
   x->enc = enc;
@@ -386,6 +384,35 @@ void oracle_train_grad(const uint16_t* w, const uint16_t* enc, const float* targ
     free(x->gabs[t]);
   }
   free(x);
+}
+
+void oracle_train_grad(const uint16_t* w, const uint16_t* enc, const float* target, int64_t n,
+                       float loss_scale, int mode, double* grad, double* grad_abs, double* loss_sum,
+                       int nthreads) {
+  wcache* c = (wcache*)malloc(sizeof(wcache));
+  load_weights(w, c);
+  train_grad_cached(c, enc, target, n, loss_scale, mode, grad, grad_abs, loss_sum, nthreads);
+  free(c);
+}
+
+/* The FP64 oracle's training loop keeps its weights in FP64: the same gradient
+ * and loss as oracle_train_grad in FP64 mode (mode 1), with the weights given as
+ * double[ORACLE_P] in the parameter layout instead of fp16. */
+void oracle_train_grad_w64(const double* w, const uint16_t* enc, const float* target, int64_t n,
+                           float loss_scale, double* grad, double* loss_sum, int nthreads) {
+  wcache* c = (wcache*)malloc(sizeof(wcache));
+  for (int l = 0; l < 5; ++l)
+    for (int o = 0; o < 64; ++o)
+      for (int i = 0; i < 64; ++i) {
+        c->wtd[l][i][o] = w[l * 4096 + o * 64 + i];
+        c->wt[l][i][o] = (float)w[l * 4096 + o * 64 + i];
+      }
+  for (int o = 0; o < 3; ++o)
+    for (int i = 0; i < 64; ++i) {
+      c->w5td[i][o] = w[5 * 4096 + o * 64 + i];
+      c->w5t[i][o] = (float)w[5 * 4096 + o * 64 + i];
+    }
+  train_grad_cached(c, enc, target, n, loss_scale, 1, grad, NULL, loss_sum, nthreads);
   free(c);
 }
 
@@ -428,5 +455,45 @@ void oracle_adam(float* entries, const float* grad, uint32_t count, const oracle
     e[3] = ema;
     w16[i] = oracle_f32_to_f16(w);
     if (use16) use16[i] = oracle_f32_to_f16(use_ema ? ema : w);
+  }
+}
+
+/* ------------------------------------------------ query destinations -- */
+/* The destination epilogue of nrc_inference.comp:50-73 (word encoding
+ * NRCRecord.glsl:19-33) applied in query order to predictions pred[n][3]
+ * (already clamped at 0): a screen pixel of the rgba32f / rg32f images becomes
+ * (bias + (factor.r, factor.g, factor.b) * pred, 0); a train word adds
+ * factor * pred to the bias of records l..r of batch b. Each channel is one
+ * fused multiply-add. Out-of-range pixels and records, and null batches, are
+ * skipped. */
+void oracle_scatter(const float* pred, const uint32_t* dst, int64_t n, float* bias_factor_r, const float* factor_gb,
+                    uint32_t width, uint32_t height, float* const* train, const uint32_t* train_cap) {
+  for (int64_t i = 0; i < n; ++i) {
+    const uint32_t d = dst[i];
+    if (d == 0xFFFFFFFFu) continue;
+    const uint32_t e = d >> 1;
+    const float* p = pred + 3 * i;
+    if ((d & 1u) == 0u) {
+      const uint32_t x = e & 0x7FFFu, y = e >> 15;
+      if (x >= width || y >= height) continue;
+      const size_t px = (size_t)y * width + x;
+      float* v = bias_factor_r + 4 * px;
+      const float* gb = factor_gb + 2 * px;
+      const float r = fmaf(v[3], p[0], v[0]), g = fmaf(gb[0], p[1], v[1]), b = fmaf(gb[1], p[2], v[2]);
+      v[0] = r;
+      v[1] = g;
+      v[2] = b;
+      v[3] = 0.0f;
+    } else {
+      const uint32_t b = e & 3u, l = (e >> 2) & 0x3FFFu, r = e >> 16;
+      float* rec = train[b];
+      if (rec == NULL) continue;
+      for (uint32_t k = l; k <= r && k < train_cap[b]; ++k) {
+        float* t = rec + 20 * (size_t)k;
+        t[0] = fmaf(t[3], p[0], t[0]);
+        t[1] = fmaf(t[4], p[1], t[1]);
+        t[2] = fmaf(t[5], p[2], t[2]);
+      }
+    }
   }
 }

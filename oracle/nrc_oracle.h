@@ -60,6 +60,8 @@ void oracle_forward_f64(const uint16_t* w, const uint16_t* enc, int64_t n, doubl
 void oracle_train_grad(const uint16_t* w, const uint16_t* enc, const float* target, int64_t n,
                        float loss_scale, int mode, double* grad, double* grad_abs, double* loss_sum,
                        int nthreads);
+void oracle_train_grad_w64(const double* w, const uint16_t* enc, const float* target, int64_t n,
+                           float loss_scale, double* grad, double* loss_sum, int nthreads);
 
 /* Optimizer state and entries (src/VkNRCState.cpp:117-123). */
 typedef struct oracle_opt_state {
@@ -81,6 +83,9 @@ uint32_t oracle_prepare(uint32_t count, const oracle_hparams* hp, oracle_opt_sta
  * fp16 of (use_ema ? ema : w). No-op when count == 0. */
 void oracle_adam(float* entries, const float* grad, uint32_t count, const oracle_opt_state* st,
                  const oracle_hparams* hp, uint16_t* w16, uint16_t* use16, int use_ema);
+
+void oracle_scatter(const float* pred, const uint32_t* dst, int64_t n, float* bias_factor_r, const float* factor_gb,
+                    uint32_t width, uint32_t height, float* const* train, const uint32_t* train_cap);
 
 #ifdef __cplusplus
 }

@@ -37,6 +37,8 @@ def lib() -> ctypes.CDLL:
         _lib.oracle_forward_f32.argtypes = [vp, vp, i64, vp, i32]
         _lib.oracle_forward_f64.argtypes = [vp, vp, i64, vp, i32]
         _lib.oracle_train_grad.argtypes = [vp, vp, vp, i64, f32, i32, vp, vp, vp, i32]
+        _lib.oracle_train_grad_w64.argtypes = [vp, vp, vp, i64, f32, vp, vp, i32]
+        _lib.oracle_scatter.argtypes = [vp, vp, i64, vp, vp, ctypes.c_uint32, ctypes.c_uint32, vp, vp]
         _lib.oracle_prepare.argtypes = [ctypes.c_uint32, vp, vp]
         _lib.oracle_prepare.restype = ctypes.c_uint32
         _lib.oracle_adam.argtypes = [vp, vp, ctypes.c_uint32, vp, vp, vp, vp, i32]
@@ -112,6 +114,40 @@ def train_grad(weights, enc, target, loss_scale=1.0, mode=0, nthreads=1, want_ab
     lib().oracle_train_grad(_p(w), _p(e), _p(t), e.shape[0], loss_scale, mode, _p(g),
                             _p(a) if a is not None else None, ctypes.byref(loss), nthreads)
     return g, a, loss.value
+
+
+def train_grad_w64(weights64, enc, target, loss_scale=1.0, nthreads=1):
+    """FP64 gradient sums and loss with FP64 weights (the FP64 oracle's training
+    loop). Returns (grad[P] float64, loss_sum)."""
+    w = _c(weights64, np.float64)
+    assert w.size == P
+    e = _c(enc, np.uint16).reshape(-1, 64)
+    t = _c(target, np.float32).reshape(-1, 3)
+    g = np.zeros(P, np.float64)
+    loss = ctypes.c_double(0.0)
+    lib().oracle_train_grad_w64(_p(w), _p(e), _p(t), e.shape[0], loss_scale, _p(g), ctypes.byref(loss), nthreads)
+    return g, loss.value
+
+
+def scatter(pred, dst, bias_factor_r, factor_gb, train_records):
+    """Destination epilogue (nrc_inference.comp:50-73) on host copies: updates
+    bias_factor_r ([H][W][4] float32) and the train record arrays ((cap, 20)
+    float32 each, or None) in place, in query order."""
+    pred = _c(pred, np.float32).reshape(-1, 3)
+    dst = _c(dst, np.uint32).reshape(-1)
+    assert pred.shape[0] == dst.shape[0]
+    assert bias_factor_r.dtype == np.float32 and bias_factor_r.flags.c_contiguous
+    gb = _c(factor_gb, np.float32)
+    h, w = bias_factor_r.shape[0], bias_factor_r.shape[1]
+    ptrs = (ctypes.c_void_p * 4)()
+    caps = (ctypes.c_uint32 * 4)()
+    for b in range(4):
+        t = train_records[b] if b < len(train_records) else None
+        if t is not None:
+            assert t.dtype == np.float32 and t.flags.c_contiguous and t.shape[1] == 20
+            ptrs[b] = t.ctypes.data
+            caps[b] = t.shape[0]
+    lib().oracle_scatter(_p(pred), _p(dst), dst.shape[0], _p(bias_factor_r), _p(gb), w, h, ptrs, caps)
 
 
 class OptState(ctypes.Structure):

@@ -290,7 +290,50 @@ int nrc_infer(nrc_context* c, const nrc_input* in, const uint32_t* d_count, uint
   if (capacity == 0) return NRC_OK;
   if (in == nullptr || d_count == nullptr || out == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
   if (!aligned16(in) || (reinterpret_cast<uintptr_t>(out) & 3u)) return NRC_ERROR_MISALIGNED;
-  return from_cuda(nrc::launch_infer(in, false, d_count, capacity, weight_map_of(c, weight_set), out, true, c->err,
+  nrc::QueryOut q = {};
+  q.out = out;
+  q.clamp = 1;
+  return from_cuda(nrc::launch_infer(in, false, d_count, capacity, weight_map_of(c, weight_set), q, c->err,
+                                     c->num_sms, static_cast<cudaStream_t>(stream)));
+}
+
+// Checks a destination set and copies it into the kernel's output description.
+static int scatter_out(const nrc_scatter_targets* t, nrc::QueryOut* q) {
+  if (t == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  if (t->width > 0x8000u || t->height > 0x10000u) return NRC_ERROR_INVALID_ARGUMENT;  // 15 / 16 coordinate bits
+  if (t->width > 0 && t->height > 0) {
+    if (t->bias_factor_r == nullptr || t->factor_gb == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+    if (!aligned16(t->bias_factor_r) || (reinterpret_cast<uintptr_t>(t->factor_gb) & 7u)) return NRC_ERROR_MISALIGNED;
+    q->width = t->width;
+    q->height = t->height;
+    q->bias_factor_r = t->bias_factor_r;
+    q->factor_gb = t->factor_gb;
+  }
+  for (int b = 0; b < NRC_TRAIN_BATCH_COUNT; ++b) {
+    if (t->train_records[b] != nullptr && (reinterpret_cast<uintptr_t>(t->train_records[b]) & 3u))
+      return NRC_ERROR_MISALIGNED;
+    q->train[b] = t->train_records[b];
+    q->train_cap[b] = t->train_records[b] != nullptr ? t->train_capacity[b] : 0u;
+  }
+  return NRC_OK;
+}
+
+int nrc_infer_scatter(nrc_context* c, const nrc_input* in, const uint32_t* d_dst, const uint32_t* d_count,
+                      uint32_t capacity, const nrc_scatter_targets* targets, float* out, int weight_set,
+                      void* stream) {
+  int s = check_ctx(c);
+  if (s != NRC_OK) return s;
+  if (weight_set != NRC_WEIGHTS_USE && weight_set != NRC_WEIGHTS_TRAIN) return NRC_ERROR_INVALID_ARGUMENT;
+  nrc::QueryOut q = {};
+  if ((s = scatter_out(targets, &q)) != NRC_OK) return s;
+  if (capacity == 0) return NRC_OK;
+  if (in == nullptr || d_dst == nullptr || d_count == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  if (!aligned16(in) || (reinterpret_cast<uintptr_t>(d_dst) & 3u) || (reinterpret_cast<uintptr_t>(out) & 3u))
+    return NRC_ERROR_MISALIGNED;
+  q.out = out;
+  q.clamp = 1;
+  q.dst = d_dst;
+  return from_cuda(nrc::launch_infer(in, false, d_count, capacity, weight_map_of(c, weight_set), q, c->err,
                                      c->num_sms, static_cast<cudaStream_t>(stream)));
 }
 
@@ -302,7 +345,10 @@ int nrc_infer_encoded(nrc_context* c, const uint16_t* enc, const uint32_t* d_cou
   if (capacity == 0) return NRC_OK;
   if (enc == nullptr || d_count == nullptr || out == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
   if (!aligned16(enc) || (reinterpret_cast<uintptr_t>(out) & 3u)) return NRC_ERROR_MISALIGNED;
-  return from_cuda(nrc::launch_infer(enc, true, d_count, capacity, weight_map_of(c, weight_set), out, false, c->err,
+  nrc::QueryOut q = {};
+  q.out = out;
+  q.clamp = 0;
+  return from_cuda(nrc::launch_infer(enc, true, d_count, capacity, weight_map_of(c, weight_set), q, c->err,
                                      c->num_sms, static_cast<cudaStream_t>(stream)));
 }
 
@@ -381,6 +427,26 @@ int nrc_frame(nrc_context* c, const nrc_input* eval_in, const uint32_t* d_eval_c
   s = nrc_infer(c, eval_in, d_eval_count, eval_capacity, out, NRC_WEIGHTS_USE, stream);
   if (s != NRC_OK) return s;
   return nrc_train_batches(c, train_rec, train_counts, train_capacity, NRC_TRAIN_BATCH_COUNT, 1, stream);
+}
+
+int nrc_frame_scatter(nrc_context* c, const nrc_input* eval_in, const uint32_t* d_eval_dst,
+                      const uint32_t* d_eval_count, uint32_t eval_capacity, const nrc_scatter_targets* targets,
+                      uint32_t* const* train_counts, void* stream) {
+  int s = check_ctx(c);
+  if (s != NRC_OK) return s;
+  if (targets == nullptr || train_counts == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  uint32_t cap = 0;
+  for (int b = 0; b < NRC_TRAIN_BATCH_COUNT; ++b) {
+    if (targets->train_records[b] == nullptr || train_counts[b] == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+    if (b > 0 && targets->train_capacity[b] != cap) return NRC_ERROR_INVALID_ARGUMENT;  // one capacity, as nrc_frame
+    cap = targets->train_capacity[b];
+  }
+  s = nrc_infer_scatter(c, eval_in, d_eval_dst, d_eval_count, eval_capacity, targets, nullptr, NRC_WEIGHTS_USE,
+                        stream);
+  if (s != NRC_OK) return s;
+  const nrc_train_record* rec[NRC_TRAIN_BATCH_COUNT];
+  for (int b = 0; b < NRC_TRAIN_BATCH_COUNT; ++b) rec[b] = targets->train_records[b];
+  return nrc_train_batches(c, rec, train_counts, cap, NRC_TRAIN_BATCH_COUNT, 1, stream);
 }
 
 int nrc_get_weights(nrc_context* c, int which, uint16_t* host) {

@@ -72,10 +72,37 @@ __device__ __forceinline__ void issue_layer(uint32_t d, uint32_t a, uint64_t bde
   mma_ts(d, a + 24, bdesc0 + 6, idesc, 1u);
 }
 
+// The destination epilogue of nrc_inference.comp:50-73 for one query (encoding
+// of the word: NRCRecord.glsl:19-33). p = max(prediction, 0).
+__device__ __forceinline__ void scatter_query(const QueryOut& Q, uint32_t dst, float p0, float p1, float p2) {
+  if (dst == 0xFFFFFFFFu) return;
+  const uint32_t e = dst >> 1;
+  if ((dst & 1u) == 0u) {  // screen pixel: color = bias + (factor_r, factor_gb) * p, alpha 0
+    const uint32_t x = e & 0x7FFFu, y = e >> 15;
+    if (x >= Q.width || y >= Q.height) return;
+    const size_t px = static_cast<size_t>(y) * Q.width + x;
+    float4* bf = reinterpret_cast<float4*>(Q.bias_factor_r) + px;
+    const float4 v = *bf;
+    const float2 gb = reinterpret_cast<const float2*>(Q.factor_gb)[px];
+    *bf = make_float4(__fmaf_rn(v.w, p0, v.x), __fmaf_rn(gb.x, p1, v.y), __fmaf_rn(gb.y, p2, v.z), 0.0f);
+  } else {  // train records l..r of batch b: bias += factor * p
+    const uint32_t b = e & 3u, l = (e >> 2) & 0x3FFFu, r = e >> 16;
+    float* rec = reinterpret_cast<float*>(Q.train[b]);
+    if (rec == nullptr) return;
+    const uint32_t end = min(r + 1, Q.train_cap[b]);
+    for (uint32_t i = l; i < end; ++i) {
+      float* t = rec + static_cast<size_t>(i) * (sizeof(nrc_train_record) / 4);
+      t[0] = __fmaf_rn(t[3], p0, t[0]);
+      t[1] = __fmaf_rn(t[4], p1, t[1]);
+      t[2] = __fmaf_rn(t[5], p2, t[2]);
+    }
+  }
+}
+
 template <bool kEncoded>
 __global__ void __launch_bounds__(kInferThreads, 1)
     infer_kernel(const void* __restrict__ input, const uint32_t* __restrict__ d_count, uint32_t capacity,
-                 const __grid_constant__ CUtensorMap wmap, float* __restrict__ out, int clamp_out, uint32_t* err) {
+                 const __grid_constant__ CUtensorMap wmap, const __grid_constant__ QueryOut Q, uint32_t* err) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
   uint8_t* smem_w = smem;
@@ -140,6 +167,7 @@ __global__ void __launch_bounds__(kInferThreads, 1)
     if (tile >= num_tiles) break;
     const uint32_t rows_valid = min(static_cast<uint32_t>(kTile), n - tile * kTile);
     const size_t grow = static_cast<size_t>(tile) * kTile + row;
+    uint32_t qdst = 0xFFFFFFFFu;  // the query's destination word (scatter epilogue)
     uint32_t e[32];
     if (!kEncoded) {
       const uint32_t b = it & 1;
@@ -207,6 +235,8 @@ __global__ void __launch_bounds__(kInferThreads, 1)
           __syncwarp();
         }
       }
+      // load the destination word while the output layer's MMAs run
+      if (l == 5 && Q.dst != nullptr && row < static_cast<int>(rows_valid)) qdst = __ldg(Q.dst + grow);
       ok = ok && warp_all(mbar_wait(&B.d_ready, ph_d, kWaitLimitNs));
       if (!ok) break;
       ph_d ^= 1u;
@@ -227,12 +257,16 @@ __global__ void __launch_bounds__(kInferThreads, 1)
         uint32_t o4[4];
         tmem_ld4(d_col + lane_off, o4);
         if (row < static_cast<int>(rows_valid)) {
-          float* dst = out + grow * 3;
+          if (Q.out != nullptr) {
+            float* dst = Q.out + grow * 3;
 #pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            const float v = __uint_as_float(o4[c]);
-            dst[c] = clamp_out ? fmaxf(v, 0.0f) : v;
+            for (int c = 0; c < 3; ++c) {
+              const float v = __uint_as_float(o4[c]);
+              dst[c] = Q.clamp ? fmaxf(v, 0.0f) : v;
+            }
           }
+          scatter_query(Q, qdst, fmaxf(__uint_as_float(o4[0]), 0.0f), fmaxf(__uint_as_float(o4[1]), 0.0f),
+                        fmaxf(__uint_as_float(o4[2]), 0.0f));
         }
       }
     }
@@ -263,7 +297,7 @@ int infer_threads() { return kInferThreads; }
 int infer_tiles_per_cta() { return kSlots; }
 
 cudaError_t launch_infer(const void* input, bool encoded, const uint32_t* d_count, uint32_t capacity,
-                         const CUtensorMap* wmap, float* out, bool clamp_out, uint32_t* err, int num_sms,
+                         const CUtensorMap* wmap, const QueryOut& q, uint32_t* err, int num_sms,
                          cudaStream_t stream) {
   const uint32_t tiles = (capacity + kTile - 1) / kTile;
   const uint32_t want = (tiles + kSlots - 1) / kSlots;
@@ -279,9 +313,8 @@ cudaError_t launch_infer(const void* input, bool encoded, const uint32_t* d_coun
   cfg.stream = stream;
   cfg.attrs = &attr;
   cfg.numAttrs = 1;
-  const int clamp = clamp_out ? 1 : 0;
-  if (encoded) return cudaLaunchKernelEx(&cfg, infer_kernel<true>, input, d_count, capacity, *wmap, out, clamp, err);
-  return cudaLaunchKernelEx(&cfg, infer_kernel<false>, input, d_count, capacity, *wmap, out, clamp, err);
+  if (encoded) return cudaLaunchKernelEx(&cfg, infer_kernel<true>, input, d_count, capacity, *wmap, q, err);
+  return cudaLaunchKernelEx(&cfg, infer_kernel<false>, input, d_count, capacity, *wmap, q, err);
 }
 
 }  // namespace nrc

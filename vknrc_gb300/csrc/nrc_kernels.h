@@ -18,8 +18,21 @@ cudaError_t configure_train_kernels();
 uint32_t infer_smem_bytes();
 int infer_threads();
 int infer_tiles_per_cta();
+// Where the query kernel puts its results: a dense rgb array (optional,
+// clamped or not) and/or the reference's destination epilogue (dst != null).
+struct QueryOut {
+  float* out;
+  int clamp;
+  const uint32_t* dst;
+  float* bias_factor_r;
+  const float* factor_gb;
+  uint32_t width, height;
+  nrc_train_record* train[NRC_TRAIN_BATCH_COUNT];
+  uint32_t train_cap[NRC_TRAIN_BATCH_COUNT];
+};
+
 cudaError_t launch_infer(const void* input, bool encoded, const uint32_t* d_count, uint32_t capacity,
-                         const CUtensorMap* wmap, float* out, bool clamp_out, uint32_t* err, int num_sms,
+                         const CUtensorMap* wmap, const QueryOut& q, uint32_t* err, int num_sms,
                          cudaStream_t stream);
 
 // One launch of the persistent trainer: up to NRC_TRAIN_BATCH_COUNT chained

@@ -28,7 +28,8 @@ EXPORTS = [
     "nrc_status_string", "nrc_default_config", "nrc_create", "nrc_destroy", "nrc_reset", "nrc_he_init_host",
     "nrc_encode", "nrc_sph_encode", "nrc_infer", "nrc_infer_encoded", "nrc_train", "nrc_gradient", "nrc_frame",
     "nrc_get_weights", "nrc_set_weights", "nrc_get_optimizer", "nrc_set_optimizer", "nrc_get_loss",
-    "nrc_get_error", "nrc_get_device_buffers", "nrc_train_noalloc", "nrc_train_batches",
+    "nrc_get_error", "nrc_get_device_buffers", "nrc_train_noalloc", "nrc_train_batches", "nrc_infer_scatter",
+    "nrc_frame_scatter",
 ]
 
 
@@ -49,6 +50,29 @@ class Config(ctypes.Structure):
 class OptState(ctypes.Structure):
     _fields_ = [("t", ctypes.c_uint32), ("beta1_t", ctypes.c_float), ("beta2_t", ctypes.c_float),
                 ("alpha_t", ctypes.c_float), ("alpha_t_1", ctypes.c_float)]
+
+
+class ScatterTargets(ctypes.Structure):
+    """nrc_scatter_targets: where the destination epilogue writes."""
+    _fields_ = [("bias_factor_r", ctypes.c_void_p), ("factor_gb", ctypes.c_void_p), ("width", ctypes.c_uint32),
+                ("height", ctypes.c_uint32), ("train_records", ctypes.c_void_p * TRAIN_BATCH_COUNT),
+                ("train_capacity", ctypes.c_uint32 * TRAIN_BATCH_COUNT)]
+
+
+def scatter_targets(bias_factor_r=None, factor_gb=None, train_records: Sequence = ()) -> ScatterTargets:
+    """Build the targets from CUDA tensors: bias_factor_r (H, W, 4) and
+    factor_gb (H, W, 2) float32 images, up to four (cap, 20) train record arrays
+    (None entries are skipped)."""
+    t = ScatterTargets()
+    if bias_factor_r is not None:
+        t.bias_factor_r = _ptr(bias_factor_r)
+        t.factor_gb = _ptr(factor_gb)
+        t.height, t.width = bias_factor_r.shape[0], bias_factor_r.shape[1]
+    for b, r in enumerate(train_records):
+        if r is not None:
+            t.train_records[b] = _ptr(r)
+            t.train_capacity[b] = r.shape[0]
+    return t
 
 
 _lib: Optional[ctypes.CDLL] = None
@@ -91,6 +115,8 @@ def lib(build_if_missing: bool = True) -> ctypes.CDLL:
     L.nrc_get_loss.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_uint64)]
     L.nrc_get_error.argtypes = [vp]
     L.nrc_train_noalloc.argtypes = [vp, vp, vp, vp, vp, vp, u32, ctypes.POINTER(Config), vp, vp]
+    L.nrc_infer_scatter.argtypes = [vp, vp, vp, vp, u32, ctypes.POINTER(ScatterTargets), vp, i32, vp]
+    L.nrc_frame_scatter.argtypes = [vp, vp, vp, vp, u32, ctypes.POINTER(ScatterTargets), ctypes.POINTER(vp), vp]
     L.nrc_get_device_buffers.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp),
                                          ctypes.POINTER(vp)]
     _lib = L
@@ -172,6 +198,19 @@ class Cache:
         cap = enc.shape[0] if capacity is None else capacity
         check(lib().nrc_infer_encoded(self.h, _ptr(enc), _ptr(count), cap, _ptr(out), weight_set,
                                       _stream(stream)), "nrc_infer_encoded")
+
+    def infer_scatter(self, inputs, dst, count, targets: ScatterTargets, out=None, capacity=None,
+                      weight_set=WEIGHTS_USE, stream=None):
+        cap = inputs.shape[0] if capacity is None else capacity
+        check(lib().nrc_infer_scatter(self.h, _ptr(inputs), _ptr(dst), _ptr(count), cap, ctypes.byref(targets),
+                                      _ptr(out), weight_set, _stream(stream)), "nrc_infer_scatter")
+
+    def frame_scatter(self, eval_inputs, eval_dst, eval_count, targets: ScatterTargets, train_counts: Sequence,
+                      eval_capacity=None, stream=None):
+        ecap = eval_inputs.shape[0] if eval_capacity is None else eval_capacity
+        cnts = (ctypes.c_void_p * TRAIN_BATCH_COUNT)(*[_ptr(c) for c in train_counts])
+        check(lib().nrc_frame_scatter(self.h, _ptr(eval_inputs), _ptr(eval_dst), _ptr(eval_count), ecap,
+                                      ctypes.byref(targets), cnts, _stream(stream)), "nrc_frame_scatter")
 
     def train(self, records, count, capacity=None, write_use=False, stream=None):
         cap = records.shape[0] if capacity is None else capacity

@@ -73,3 +73,39 @@ def train_records(rng: np.random.Generator, n: int, target: str = "lognormal", s
     rec[:, 3:6] = 1.0
     rec[:, 6:20] = x
     return rec
+
+
+def dst_screen(x: np.ndarray, y: np.ndarray) -> np.ndarray:
+    """EncodeNRCEvalDstScreen (NRCRecord.glsl:20): (x | y << 15) << 1."""
+    return ((x.astype(np.uint32) | (y.astype(np.uint32) << 15)) << 1).astype(np.uint32)
+
+
+def dst_train(b: np.ndarray, l: np.ndarray, r: np.ndarray) -> np.ndarray:
+    """EncodeNRCEvalDstTrain (NRCRecord.glsl:21-23): (b | l << 2 | r << 16) << 1 | 1."""
+    b, l, r = (np.asarray(v, np.uint32) for v in (b, l, r))
+    return (((b | (l << 2) | (r << 16)) << 1) | 1).astype(np.uint32)
+
+
+DST_INVALID = np.uint32(0xFFFFFFFF)
+
+
+def frame_destinations(rng: np.random.Generator, width: int, height: int, train_counts, max_run: int = 8):
+    """Destination words of one frame's queries, as the path tracer emits them:
+    one per screen pixel, and for every train batch b its records 0..count-1
+    split into consecutive runs [l, r] of 1..max_run records (one query per run,
+    completing that run's targets). Returned in random order."""
+    ys, xs = np.divmod(np.arange(width * height, dtype=np.uint32), np.uint32(width))
+    words = [dst_screen(xs, ys)]
+    for b, n in enumerate(train_counts):
+        l = 0
+        ls, rs = [], []
+        while l < n:
+            run = int(rng.integers(1, max_run + 1))
+            r = min(n, l + run) - 1
+            ls.append(l)
+            rs.append(r)
+            l = r + 1
+        if ls:
+            words.append(dst_train(np.full(len(ls), b), np.array(ls), np.array(rs)))
+    d = np.concatenate(words)
+    return d[rng.permutation(d.size)]
