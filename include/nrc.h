@@ -252,6 +252,49 @@ NRC_API int nrc_train_noalloc(uint16_t* d_weights, uint16_t* d_use_weights, nrc_
                               nrc_optimizer_state* d_state, const nrc_train_record* d_records, uint32_t* d_count,
                               uint32_t capacity, const nrc_config* cfg, uint32_t* d_error, void* stream);
 
+/* ---------------------------------------------------------------------------
+ * Batched caches: many independent caches (separate weights and Adam state,
+ * uneven record counts) served by one persistent launch per phase. The
+ * reference runs one cache per renderer (VkNRCState, src/VkNRCState.hpp:27-52);
+ * these calls do, for n caches at once, what nrc_infer / nrc_train_batches do
+ * for one, and give each cache exactly the results it gets alone (every
+ * reduction runs in a fixed order within the cache's own CTA group).
+ * The SMs are split between the caches in proportion to their tiles
+ * (capacity / 128 records), at least one CTA each, unless `ctas` gives the split
+ * (one entry per job; a job's CTAs beyond its tiles idle). A context may appear
+ * at most once per call; all contexts must live on the current device. More
+ * than 32 jobs run as successive launches of up to 32.
+ * ------------------------------------------------------------------------- */
+typedef struct nrc_query_job {
+  nrc_context* ctx;
+  const nrc_input* inputs;  /* capacity records */
+  const uint32_t* d_count;  /* queries = min(*d_count, capacity) */
+  uint32_t capacity;
+  float* out_rgb;           /* capacity x 3, clamped to >= 0 as nrc_infer */
+  int weight_set;           /* NRC_WEIGHTS_USE or NRC_WEIGHTS_TRAIN */
+} nrc_query_job;
+
+typedef struct nrc_train_job {
+  nrc_context* ctx;
+  const nrc_train_record* records[NRC_TRAIN_BATCH_COUNT]; /* first nbatches used */
+  uint32_t* d_counts[NRC_TRAIN_BATCH_COUNT];               /* clamped and written back as nrc_train */
+  uint32_t capacity;
+  int nbatches;       /* 1..4 chained steps, as nrc_train_batches */
+  int write_use_last; /* the last step also writes use_weights */
+} nrc_train_job;
+
+/* nrc_infer for every job, one launch per 32 jobs. `ctas` may be NULL. */
+NRC_API int nrc_infer_many(const nrc_query_job* jobs, uint32_t njobs, const uint32_t* ctas, void* stream);
+
+/* nrc_train_batches for every job, one cooperative launch per 32 jobs. `ctas`
+ * may be NULL. */
+NRC_API int nrc_train_many(const nrc_train_job* jobs, uint32_t njobs, const uint32_t* ctas, void* stream);
+
+/* CTA split that nrc_infer_many / nrc_train_many use when `ctas` is NULL, for
+ * one launch of at most 32 jobs: writes njobs entries to out_ctas. */
+NRC_API int nrc_plan_query_ctas(const nrc_query_job* jobs, uint32_t njobs, uint32_t* out_ctas);
+NRC_API int nrc_plan_train_ctas(const nrc_train_job* jobs, uint32_t njobs, uint32_t* out_ctas);
+
 /* Host copies of the parameter state (synchronous). `which` selects
  * NRC_WEIGHTS_USE or NRC_WEIGHTS_TRAIN for the fp16 vectors. */
 NRC_API int nrc_get_weights(nrc_context* ctx, int which, uint16_t* host_w16);

@@ -1,6 +1,7 @@
 // C ABI of libnrc.so (include/nrc.h): context ownership, argument checks and
 // kernel launches. Host code only; kernels live in nrc_infer.cu, nrc_train.cu
 // and nrc_encode.cu.
+#include <algorithm>
 #include <cmath>
 #include <cudaTypedefs.h>
 #include <cstring>
@@ -447,6 +448,218 @@ int nrc_frame_scatter(nrc_context* c, const nrc_input* eval_in, const uint32_t* 
   const nrc_train_record* rec[NRC_TRAIN_BATCH_COUNT];
   for (int b = 0; b < NRC_TRAIN_BATCH_COUNT; ++b) rec[b] = targets->train_records[b];
   return nrc_train_batches(c, rec, train_counts, cap, NRC_TRAIN_BATCH_COUNT, 1, stream);
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------ batched caches --
+namespace {
+
+constexpr uint32_t kMaxJobsPerLaunch = 32;  // nrc::kMaxInferJobs == nrc::kMaxTrainJobs
+static_assert(nrc::kMaxInferJobs == kMaxJobsPerLaunch && nrc::kMaxTrainJobs == kMaxJobsPerLaunch, "job caps");
+
+// Split `total` CTAs over n jobs in proportion to weight[j] (largest remainder),
+// at least one and at most cap[j] each. Requires n <= total.
+void split_ctas(const uint64_t* weight, const uint32_t* cap, uint32_t n, uint32_t total, uint32_t* out) {
+  uint64_t wsum = 0;
+  for (uint32_t j = 0; j < n; ++j) wsum += weight[j];
+  uint32_t used = 0;
+  std::vector<double> rem(n, 0.0);
+  for (uint32_t j = 0; j < n; ++j) {
+    const double share = wsum > 0 ? double(total) * double(weight[j]) / double(wsum) : double(total) / n;
+    uint32_t g = static_cast<uint32_t>(share);
+    g = std::max(1u, std::min(g, cap[j]));
+    out[j] = g;
+    rem[j] = share - double(g);
+    used += g;
+  }
+  // hand out what is left (or take back the excess), largest remainder first
+  while (used < total) {
+    int best = -1;
+    for (uint32_t j = 0; j < n; ++j)
+      if (out[j] < cap[j] && (best < 0 || rem[j] > rem[best])) best = static_cast<int>(j);
+    if (best < 0) break;
+    ++out[best];
+    rem[best] -= 1.0;
+    ++used;
+  }
+  while (used > total) {
+    int best = -1;
+    for (uint32_t j = 0; j < n; ++j)
+      if (out[j] > 1 && (best < 0 || rem[j] < rem[best])) best = static_cast<int>(j);
+    if (best < 0) break;
+    --out[best];
+    rem[best] += 1.0;
+    --used;
+  }
+}
+
+int query_job_check(const nrc_query_job& q, int dev) {
+  if (q.ctx == nullptr || q.ctx->device != dev) return NRC_ERROR_INVALID_ARGUMENT;
+  if (q.weight_set != NRC_WEIGHTS_USE && q.weight_set != NRC_WEIGHTS_TRAIN) return NRC_ERROR_INVALID_ARGUMENT;
+  if (q.capacity == 0) return NRC_OK;
+  if (q.inputs == nullptr || q.d_count == nullptr || q.out_rgb == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  if (!aligned16(q.inputs) || (reinterpret_cast<uintptr_t>(q.out_rgb) & 3u)) return NRC_ERROR_MISALIGNED;
+  return NRC_OK;
+}
+
+int train_job_check(const nrc_train_job& t, int dev) {
+  if (t.ctx == nullptr || t.ctx->device != dev) return NRC_ERROR_INVALID_ARGUMENT;
+  if (t.nbatches < 1 || t.nbatches > NRC_TRAIN_BATCH_COUNT) return NRC_ERROR_INVALID_ARGUMENT;
+  for (int b = 0; b < t.nbatches; ++b) {
+    if (t.d_counts[b] == nullptr || (t.capacity > 0 && t.records[b] == nullptr)) return NRC_ERROR_INVALID_ARGUMENT;
+    if (t.records[b] != nullptr && !aligned16(t.records[b])) return NRC_ERROR_MISALIGNED;
+  }
+  return NRC_OK;
+}
+
+template <typename Job>
+int check_jobs(const Job* jobs, uint32_t n, int (*one)(const Job&, int)) {
+  if (jobs == nullptr && n > 0) return NRC_ERROR_INVALID_ARGUMENT;
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess) return NRC_ERROR_CUDA;
+  for (uint32_t j = 0; j < n; ++j) {
+    const int s = one(jobs[j], dev);
+    if (s != NRC_OK) return s;
+    for (uint32_t k = 0; k < j; ++k)
+      if (jobs[k].ctx == jobs[j].ctx) return NRC_ERROR_INVALID_ARGUMENT;  // one group per context
+  }
+  return NRC_OK;
+}
+
+int device_sms() {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return sms;
+}
+
+// The default split of one launch's CTAs (n <= 32 jobs of non-empty capacity).
+void plan_query(const nrc_query_job* jobs, uint32_t n, int sms, uint32_t* out) {
+  uint64_t w[kMaxJobsPerLaunch];
+  uint32_t cap[kMaxJobsPerLaunch];
+  uint32_t want = 0;
+  for (uint32_t j = 0; j < n; ++j) {
+    w[j] = (uint64_t(jobs[j].capacity) + nrc::kTile - 1) / nrc::kTile;
+    cap[j] = std::max(1u, nrc::infer_grid(jobs[j].capacity, sms));
+    want += cap[j];
+  }
+  split_ctas(w, cap, n, std::min<uint32_t>(want, static_cast<uint32_t>(sms)), out);
+}
+
+void plan_train(const nrc_train_job* jobs, uint32_t n, int sms, uint32_t* out) {
+  uint64_t w[kMaxJobsPerLaunch];
+  uint32_t cap[kMaxJobsPerLaunch];
+  for (uint32_t j = 0; j < n; ++j) {
+    const uint32_t rec = std::min(jobs[j].capacity, jobs[j].ctx->cfg.train_batch_size);
+    w[j] = uint64_t(jobs[j].nbatches) * std::max<uint64_t>(1, (uint64_t(rec) + nrc::kTile - 1) / nrc::kTile);
+    cap[j] = nrc::train_grid(nrc::TrainParams{}, sms);
+  }
+  split_ctas(w, cap, n, static_cast<uint32_t>(sms), out);
+}
+
+}  // namespace
+
+extern "C" {
+
+int nrc_plan_query_ctas(const nrc_query_job* jobs, uint32_t n, uint32_t* out) {
+  if (out == nullptr || n == 0 || n > kMaxJobsPerLaunch) return NRC_ERROR_INVALID_ARGUMENT;
+  int s = check_jobs(jobs, n, query_job_check);
+  if (s != NRC_OK) return s;
+  plan_query(jobs, n, device_sms(), out);
+  return NRC_OK;
+}
+
+int nrc_plan_train_ctas(const nrc_train_job* jobs, uint32_t n, uint32_t* out) {
+  if (out == nullptr || n == 0 || n > kMaxJobsPerLaunch) return NRC_ERROR_INVALID_ARGUMENT;
+  int s = check_jobs(jobs, n, train_job_check);
+  if (s != NRC_OK) return s;
+  plan_train(jobs, n, device_sms(), out);
+  return NRC_OK;
+}
+
+int nrc_infer_many(const nrc_query_job* jobs, uint32_t n, const uint32_t* ctas, void* stream) {
+  int s = check_jobs(jobs, n, query_job_check);
+  if (s != NRC_OK) return s;
+  const int sms = device_sms();
+  if (ctas != nullptr) {
+    uint32_t sum = 0;
+    for (uint32_t j = 0; j < n; ++j) {
+      if (ctas[j] == 0) return NRC_ERROR_INVALID_ARGUMENT;
+      if (j % kMaxJobsPerLaunch == 0) sum = 0;
+      sum += ctas[j];
+      if (sum > static_cast<uint32_t>(sms)) return NRC_ERROR_INVALID_ARGUMENT;
+    }
+  }
+  nrc::InferJob ij[kMaxJobsPerLaunch];
+  uint32_t g[kMaxJobsPerLaunch];
+  const nrc_query_job* sel[kMaxJobsPerLaunch];
+  nrc_query_job kept[kMaxJobsPerLaunch];
+  for (uint32_t base = 0; base < n; base += kMaxJobsPerLaunch) {
+    const uint32_t m = std::min(n - base, kMaxJobsPerLaunch);
+    uint32_t k = 0;
+    for (uint32_t j = 0; j < m; ++j) {
+      const nrc_query_job& q = jobs[base + j];
+      if (q.capacity == 0) continue;  // nothing to answer
+      kept[k] = q;
+      sel[k] = &jobs[base + j];
+      if (ctas != nullptr) g[k] = ctas[base + j];
+      ++k;
+    }
+    if (k == 0) continue;
+    if (ctas == nullptr) plan_query(kept, k, sms, g);
+    for (uint32_t j = 0; j < k; ++j) {
+      const nrc_query_job& q = *sel[j];
+      ij[j] = nrc::InferJob{};
+      ij[j].wmap = *weight_map_of(q.ctx, q.weight_set);
+      ij[j].input = q.inputs;
+      ij[j].d_count = q.d_count;
+      ij[j].capacity = q.capacity;
+      ij[j].err = q.ctx->err;
+      ij[j].q.out = q.out_rgb;
+      ij[j].q.clamp = 1;
+    }
+    const cudaError_t e = nrc::launch_infer_many(ij, static_cast<int>(k), g, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return from_cuda(e);
+  }
+  return NRC_OK;
+}
+
+int nrc_train_many(const nrc_train_job* jobs, uint32_t n, const uint32_t* ctas, void* stream) {
+  int s = check_jobs(jobs, n, train_job_check);
+  if (s != NRC_OK) return s;
+  const int sms = device_sms();
+  if (ctas != nullptr) {
+    uint32_t sum = 0;
+    for (uint32_t j = 0; j < n; ++j) {
+      if (ctas[j] == 0 || ctas[j] > nrc::train_grid(nrc::TrainParams{}, sms)) return NRC_ERROR_INVALID_ARGUMENT;
+      if (j % kMaxJobsPerLaunch == 0) sum = 0;
+      sum += ctas[j];
+      if (sum > static_cast<uint32_t>(sms)) return NRC_ERROR_INVALID_ARGUMENT;
+    }
+  }
+  if (std::min(n, kMaxJobsPerLaunch) > static_cast<uint32_t>(sms)) return NRC_ERROR_INVALID_ARGUMENT;
+  std::vector<nrc::TrainJob> tj(kMaxJobsPerLaunch);
+  uint32_t g[kMaxJobsPerLaunch];
+  for (uint32_t base = 0; base < n; base += kMaxJobsPerLaunch) {
+    const uint32_t m = std::min(n - base, kMaxJobsPerLaunch);
+    if (ctas == nullptr)
+      plan_train(jobs + base, m, sms, g);
+    else
+      for (uint32_t j = 0; j < m; ++j) g[j] = ctas[base + j];
+    for (uint32_t j = 0; j < m; ++j) {
+      const nrc_train_job& t = jobs[base + j];
+      nrc::TrainParams p = train_params(t.ctx, t.nbatches, nrc::kTrainStep);
+      for (int b = 0; b < t.nbatches; ++b)
+        p.batch[b] = nrc::TrainBatch{t.records[b], t.d_counts[b], t.capacity,
+                                     (t.write_use_last != 0 && b == t.nbatches - 1) ? 1 : 0};
+      tj[j].wmap = t.ctx->map_w16;
+      tj[j].p = p;
+    }
+    const cudaError_t e = nrc::launch_train_many(tj.data(), static_cast<int>(m), g, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return from_cuda(e);
+  }
+  return NRC_OK;
 }
 
 int nrc_get_weights(nrc_context* c, int which, uint16_t* host) {

@@ -15,6 +15,8 @@
 //     Every slot issues its own MMAs from its first warp (converged, one lane
 //     elected): a single issuing thread is bounded by its issue rate, several
 //     issuing warps keep the tensor pipe busy while other slots convert.
+#include <mutex>
+
 #include "nrc_common.cuh"
 #include "nrc_kernels.h"
 
@@ -99,10 +101,20 @@ __device__ __forceinline__ void scatter_query(const QueryOut& Q, uint32_t dst, f
   }
 }
 
-template <bool kEncoded>
-__global__ void __launch_bounds__(kInferThreads, 1)
-    infer_kernel(const void* __restrict__ input, const uint32_t* __restrict__ d_count, uint32_t capacity,
-                 const __grid_constant__ CUtensorMap wmap, const __grid_constant__ QueryOut Q, uint32_t* err) {
+// kScatter: the query carries a destination word (nrc_infer_scatter); the
+// plain query path is compiled without the destination load and epilogue.
+// One launch serves up to N caches: CTAs [group_start[j], group_start[j+1])
+// answer cache j's queries with its weights; with N = 1 the group is the grid.
+template <bool kEncoded, bool kScatter, int N>
+__global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_constant__ InferLaunch<N> L) {
+  int job = 0;
+  while (job + 1 < L.njobs && blockIdx.x >= L.group_start[job + 1]) ++job;
+  const InferJob& J = L.job[job];
+  const QueryOut& Q = J.q;
+  const uint32_t G = L.group_start[job + 1] - L.group_start[job];  // CTAs of this cache
+  const uint32_t rank = blockIdx.x - L.group_start[job];           // this CTA within them
+  const void* input = J.input;
+  uint32_t* err = J.err;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
   uint8_t* smem_w = smem;
@@ -128,13 +140,13 @@ __global__ void __launch_bounds__(kInferThreads, 1)
   // Everything below may read what the preceding kernel in the stream wrote.
   griddep_wait();
   griddep_launch_dependents();
-  const uint32_t n = min(*d_count, capacity);
+  const uint32_t n = min(*J.d_count, J.capacity);
   const uint32_t num_tiles = (n + kTile - 1) / kTile;
   if (warp == 0) {
     tmem_alloc(tmem_slot, 512);
     tmem_relinquish();
   }
-  if (threadIdx.x == 0) stage_weights_tma(smem_w, &wmap, w_full);
+  if (threadIdx.x == 0) stage_weights_tma(smem_w, &J.wmap, w_full);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
@@ -152,7 +164,7 @@ __global__ void __launch_bounds__(kInferThreads, 1)
   const uint32_t id64 = idesc_f16_f32(128, 64, 0, 0), id16 = idesc_f16_f32(128, 16, 0, 0);
   uint8_t* stage0 = smem_rec + (s * 2 + 0) * kRecTileBytes;
   const nrc_input* rec_in = static_cast<const nrc_input*>(input);
-  auto tile_of = [&](uint32_t it) { return (it * gridDim.x + blockIdx.x) * kSlots + s; };
+  auto tile_of = [&](uint32_t it) { return (it * G + rank) * kSlots + s; };
 
   if (!kEncoded && leader) {
     for (uint32_t b = 0; b < 2; ++b)
@@ -236,7 +248,7 @@ __global__ void __launch_bounds__(kInferThreads, 1)
         }
       }
       // load the destination word while the output layer's MMAs run
-      if (l == 5 && Q.dst != nullptr && row < static_cast<int>(rows_valid)) qdst = __ldg(Q.dst + grow);
+      if (kScatter && l == 5 && row < static_cast<int>(rows_valid)) qdst = __ldg(Q.dst + grow);
       ok = ok && warp_all(mbar_wait(&B.d_ready, ph_d, kWaitLimitNs));
       if (!ok) break;
       ph_d ^= 1u;
@@ -265,8 +277,9 @@ __global__ void __launch_bounds__(kInferThreads, 1)
               dst[c] = Q.clamp ? fmaxf(v, 0.0f) : v;
             }
           }
-          scatter_query(Q, qdst, fmaxf(__uint_as_float(o4[0]), 0.0f), fmaxf(__uint_as_float(o4[1]), 0.0f),
-                        fmaxf(__uint_as_float(o4[2]), 0.0f));
+          if (kScatter)
+            scatter_query(Q, qdst, fmaxf(__uint_as_float(o4[0]), 0.0f), fmaxf(__uint_as_float(o4[1]), 0.0f),
+                          fmaxf(__uint_as_float(o4[2]), 0.0f));
         }
       }
     }
@@ -283,26 +296,8 @@ __global__ void __launch_bounds__(kInferThreads, 1)
   }
 }
 
-}  // namespace
-
-cudaError_t configure_infer_kernels() {
-  cudaError_t e = cudaFuncSetAttribute(infer_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(infer_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
-  return e;
-}
-
-uint32_t infer_smem_bytes() { return kSmemBytes; }
-int infer_threads() { return kInferThreads; }
-int infer_tiles_per_cta() { return kSlots; }
-
-cudaError_t launch_infer(const void* input, bool encoded, const uint32_t* d_count, uint32_t capacity,
-                         const CUtensorMap* wmap, const QueryOut& q, uint32_t* err, int num_sms,
-                         cudaStream_t stream) {
-  const uint32_t tiles = (capacity + kTile - 1) / kTile;
-  const uint32_t want = (tiles + kSlots - 1) / kSlots;
-  const uint32_t grid = want < static_cast<uint32_t>(num_sms) ? want : static_cast<uint32_t>(num_sms);
-  if (grid == 0) return cudaSuccess;
+template <bool kEncoded, bool kScatter, int N>
+cudaError_t launch(const InferLaunch<N>& L, uint32_t grid, cudaStream_t stream) {
   cudaLaunchAttribute attr;
   attr.id = cudaLaunchAttributeProgrammaticStreamSerialization;
   attr.val.programmaticStreamSerializationAllowed = 1;
@@ -313,8 +308,70 @@ cudaError_t launch_infer(const void* input, bool encoded, const uint32_t* d_coun
   cfg.stream = stream;
   cfg.attrs = &attr;
   cfg.numAttrs = 1;
-  if (encoded) return cudaLaunchKernelEx(&cfg, infer_kernel<true>, input, d_count, capacity, *wmap, q, err);
-  return cudaLaunchKernelEx(&cfg, infer_kernel<false>, input, d_count, capacity, *wmap, q, err);
+  return cudaLaunchKernelEx(&cfg, infer_kernel<kEncoded, kScatter, N>, L);
+}
+
+template <bool kEncoded, bool kScatter, int N>
+cudaError_t set_smem() {
+  return cudaFuncSetAttribute(infer_kernel<kEncoded, kScatter, N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              kSmemBytes);
+}
+
+}  // namespace
+
+cudaError_t configure_infer_kernels() {
+  cudaError_t e = set_smem<true, false, 1>();
+  if (e == cudaSuccess) e = set_smem<false, false, 1>();
+  if (e == cudaSuccess) e = set_smem<false, true, 1>();
+  if (e == cudaSuccess) e = set_smem<false, false, kMaxInferJobs>();
+  return e;
+}
+
+uint32_t infer_smem_bytes() { return kSmemBytes; }
+int infer_threads() { return kInferThreads; }
+int infer_tiles_per_cta() { return kSlots; }
+
+uint32_t infer_grid(uint32_t capacity, int num_sms) {
+  const uint32_t tiles = (capacity + kTile - 1) / kTile;
+  const uint32_t want = (tiles + kSlots - 1) / kSlots;
+  return want < static_cast<uint32_t>(num_sms) ? want : static_cast<uint32_t>(num_sms);
+}
+
+cudaError_t launch_infer(const void* input, bool encoded, const uint32_t* d_count, uint32_t capacity,
+                         const CUtensorMap* wmap, const QueryOut& q, uint32_t* err, int num_sms,
+                         cudaStream_t stream) {
+  const uint32_t grid = infer_grid(capacity, num_sms);
+  if (grid == 0) return cudaSuccess;
+  InferLaunch<1> L;
+  L.job[0].wmap = *wmap;
+  L.job[0].input = input;
+  L.job[0].d_count = d_count;
+  L.job[0].capacity = capacity;
+  L.job[0].err = err;
+  L.job[0].q = q;
+  L.group_start[0] = 0;
+  L.group_start[1] = grid;
+  L.njobs = 1;
+  if (encoded) return launch<true, false>(L, grid, stream);
+  if (q.dst != nullptr) return launch<false, true>(L, grid, stream);
+  return launch<false, false>(L, grid, stream);
+}
+
+cudaError_t launch_infer_many(const InferJob* jobs, int njobs, const uint32_t* group_size, cudaStream_t stream) {
+  if (njobs < 1 || njobs > kMaxInferJobs) return cudaErrorInvalidValue;
+  static InferLaunch<kMaxInferJobs> L;  // host staging of the kernel parameters (copied at launch)
+  static std::mutex m;
+  std::lock_guard<std::mutex> lock(m);
+  uint32_t grid = 0;
+  for (int j = 0; j < njobs; ++j) {
+    if (jobs[j].q.dst != nullptr || group_size[j] < 1) return cudaErrorInvalidValue;
+    L.job[j] = jobs[j];
+    L.group_start[j] = grid;
+    grid += group_size[j];
+  }
+  L.group_start[njobs] = grid;
+  L.njobs = njobs;
+  return launch<false, false>(L, grid, stream);
 }
 
 }  // namespace nrc

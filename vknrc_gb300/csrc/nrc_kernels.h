@@ -35,6 +35,33 @@ cudaError_t launch_infer(const void* input, bool encoded, const uint32_t* d_coun
                          const CUtensorMap* wmap, const QueryOut& q, uint32_t* err, int num_sms,
                          cudaStream_t stream);
 
+// One cache's share of a query launch.
+struct InferJob {
+  CUtensorMap wmap;
+  const void* input;  // nrc_input records
+  const uint32_t* d_count;
+  uint32_t capacity;
+  uint32_t* err;
+  QueryOut q;
+};
+
+// Kernel parameters of a query launch over up to N caches; CTAs
+// [group_start[j], group_start[j + 1]) answer job j.
+template <int N>
+struct InferLaunch {
+  InferJob job[N];
+  uint32_t group_start[N + 1];
+  int njobs;
+};
+
+constexpr int kMaxInferJobs = 32;  // caches per batched query launch
+
+// CTAs the query kernel uses for `capacity` records on `num_sms` SMs.
+uint32_t infer_grid(uint32_t capacity, int num_sms);
+// One launch answering njobs caches' record queries (dense rgb output, no
+// destination words), group_size[j] >= 1 CTAs for job j, sum <= SMs.
+cudaError_t launch_infer_many(const InferJob* jobs, int njobs, const uint32_t* group_size, cudaStream_t stream);
+
 // One launch of the persistent trainer: up to NRC_TRAIN_BATCH_COUNT chained
 // batches, each a fused gradient pass followed by the optimizer step (mode
 // kTrainStep), or one gradient pass whose fixed-order sum is written to
@@ -68,9 +95,32 @@ struct TrainParams {
   uint32_t* err;
 };
 
+// One cache's share of a training launch: its weight tensor map and parameters.
+struct TrainJob {
+  CUtensorMap wmap;
+  TrainParams p;
+};
+
+// Kernel parameters of a launch over up to N caches; CTAs
+// [group_start[j], group_start[j + 1]) train cache j.
+template <int N>
+struct TrainLaunch {
+  TrainJob job[N];
+  uint32_t group_start[N + 1];
+  int njobs;
+};
+
+constexpr int kMaxTrainJobs = 32;  // caches per batched training launch
+
 uint32_t train_smem_bytes();
 uint32_t train_grid(const TrainParams& p, int max_ctas);
+// The grid barrier counter p.sync[0] and exit counter p.sync[1] must be zero
+// before the first launch on them; every launch leaves them at zero.
 cudaError_t launch_train(const TrainParams& p, const CUtensorMap* wmap, int max_ctas, cudaStream_t stream);
+// One cooperative launch training njobs caches, group_size[j] CTAs for job j
+// (1 .. 160 each, sum <= CTAs resident at one per SM). Jobs must not share a
+// context (parameter buffers, partials or barrier counters).
+cudaError_t launch_train_many(const TrainJob* jobs, int njobs, const uint32_t* group_size, cudaStream_t stream);
 
 cudaError_t launch_encode(const nrc_input* in, const uint32_t* d_count, uint32_t capacity, uint16_t* out,
                           int num_sms, cudaStream_t stream);

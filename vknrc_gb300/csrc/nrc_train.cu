@@ -31,6 +31,8 @@
 //     The reference's prepare pass (count clamp, step state) runs in CTA 0.
 //   - the epilogue runs on eight warps: the two warps that share a TMEM lane
 //     quadrant split each 64-wide row between them.
+#include <mutex>
+
 #include "nrc_common.cuh"
 #include "nrc_kernels.h"
 
@@ -213,8 +215,18 @@ __device__ __forceinline__ void adam_one(int i, float gsum, uint32_t n, const nr
   if (use16 != nullptr) use16[i] = __float2half_rn(hp.use_ema ? ema : w);
 }
 
-__global__ void __launch_bounds__(kTrainThreads, 1)
-    train_steps_kernel(const __grid_constant__ TrainParams P, const __grid_constant__ CUtensorMap wmap) {
+// One launch trains up to N caches: CTAs [group_start[j], group_start[j+1])
+// form cache j's group, which runs the whole schedule below on its own (its own
+// grid barrier, partial slots and parameter slices). With N = 1 the group is the
+// grid.
+template <int N>
+__global__ void __launch_bounds__(kTrainThreads, 1) train_steps_kernel(const __grid_constant__ TrainLaunch<N> L) {
+  int job = 0;
+  while (job + 1 < L.njobs && blockIdx.x >= L.group_start[job + 1]) ++job;
+  const TrainParams& P = L.job[job].p;
+  const CUtensorMap& wmap = L.job[job].wmap;
+  const uint32_t G = L.group_start[job + 1] - L.group_start[job];  // CTAs of this cache
+  const uint32_t rank = blockIdx.x - L.group_start[job];           // this CTA within them
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
   uint8_t* smem_w = smem;
@@ -247,10 +259,13 @@ __global__ void __launch_bounds__(kTrainThreads, 1)
   // This CTA's slice [c0, c1) of float4 gradient columns in the optimizer phase;
   // its optimizer entries stay in shared memory for the whole launch (only this
   // CTA updates them).
-  const uint32_t per = (kCols4 + gridDim.x - 1) / gridDim.x;  // <= kMaxSlice4
-  const uint32_t c0 = min(static_cast<uint32_t>(kCols4), blockIdx.x * per);
+  const uint32_t per = (kCols4 + G - 1) / G;
+  const uint32_t c0 = min(static_cast<uint32_t>(kCols4), rank * per);
   const uint32_t ncols = min(static_cast<uint32_t>(kCols4), c0 + per) - c0;
-  if (P.mode == kTrainStep) {
+  // Groups of fewer than kMinTrainCtas CTAs have slices too large to keep in
+  // shared memory; their optimizer reads and writes the entries in memory.
+  const bool cached = ncols <= kMaxSlice4;
+  if (P.mode == kTrainStep && cached) {
     for (uint32_t k = threadIdx.x; k < 4 * ncols; k += blockDim.x) cp_async16(ecache + k, P.entries + 4 * c0 + k);
     cp_async_commit();
   }
@@ -264,16 +279,14 @@ __global__ void __launch_bounds__(kTrainThreads, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = __shfl_sync(0xffffffffu, B->tmem_base, 0);
-  float* const my_partial = P.partials + static_cast<size_t>(blockIdx.x) * kParams;
+  float* const my_partial = P.partials + static_cast<size_t>(rank) * kParams;
   nrc_optimizer_state st = B->st;  // advanced per batch in every CTA alike
-  if (P.mode == kTrainStep && blockIdx.x == 0 && threadIdx.x == 0) {
+  if (P.mode == kTrainStep && rank == 0 && threadIdx.x == 0) {
     // Other CTAs read either the raw or the clamped count; both clamp to the same n.
     for (int s = 0; s < P.steps; ++s) *P.batch[s].d_count = min(B->count[s], P.batch_cap);
   }
   auto batch_records = [&](int s) { return min(min(B->count[s], P.batch_cap), P.batch[s].capacity); };
-  auto tiles_of = [&](uint32_t num_tiles) {
-    return blockIdx.x < num_tiles ? (num_tiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0u;
-  };
+  auto tiles_of = [&](uint32_t num_tiles) { return rank < num_tiles ? (num_tiles - rank + G - 1) / G : 0u; };
 
   // Role state that persists across the batches (mbarrier phases).
   const int ew = warp - 1;   // epilogue warp index (warps 1..8)
@@ -299,7 +312,7 @@ __global__ void __launch_bounds__(kTrainThreads, 1)
   auto issue_first_tiles = [&](const TrainBatch& bt, uint32_t n, uint32_t my_tiles) {
     for (uint32_t k = 0; k < 2 && k < my_tiles; ++k) {
       const uint32_t s = (ct + k) & 1;
-      issue_train_tile(bt.records, blockIdx.x + k * gridDim.x, n, stage + s * kTRecTileBytes, &B->rec_full[s]);
+      issue_train_tile(bt.records, rank + k * G, n, stage + s * kTRecTileBytes, &B->rec_full[s]);
     }
   };
   auto publish = [&]() {  // operand rows written: hand them to the tensor core
@@ -310,7 +323,7 @@ __global__ void __launch_bounds__(kTrainThreads, 1)
   // Epilogue warps: records of the CTA's tile `it` -> target, and the encoded
   // input act_0 in shared memory and TMEM, published to the MMA warp.
   auto prep_tile = [&](const TrainBatch& bt, uint32_t n, uint32_t it, uint32_t my_tiles) -> bool {
-    const uint32_t tile = blockIdx.x + it * gridDim.x;
+    const uint32_t tile = rank + it * G;
     const bool valid = row < static_cast<int>(min(static_cast<uint32_t>(kTile), n - tile * kTile));
     const uint32_t s = ct & 1, use = ct >> 1;  // stage and its use count
     if (!warp_all(mbar_wait(&B->rec_full[s], use & 1, kWaitLimitNs))) return false;
@@ -335,7 +348,7 @@ __global__ void __launch_bounds__(kTrainThreads, 1)
     mbar_arrive(&B->rec_empty[s]);
     if (leader && it + 2 < my_tiles) {
       if (mbar_wait(&B->rec_empty[s], use & 1, kWaitLimitNs))
-        issue_train_tile(bt.records, tile + 2 * gridDim.x, n, stage + s * kTRecTileBytes, &B->rec_full[s]);
+        issue_train_tile(bt.records, tile + 2 * G, n, stage + s * kTRecTileBytes, &B->rec_full[s]);
       else
         atomicOr(P.err, kErrTimeout);
     }
@@ -454,7 +467,7 @@ __global__ void __launch_bounds__(kTrainThreads, 1)
         return ok;
       };
       for (uint32_t it = 0; it < my_tiles && ok; ++it, ++ct) {
-        const uint32_t tile = blockIdx.x + it * gridDim.x;
+        const uint32_t tile = rank + it * G;
         const uint32_t rows_valid = min(static_cast<uint32_t>(kTile), n - tile * kTile);
         const bool valid = row < static_cast<int>(rows_valid);
         const bool last = it + 1 == my_tiles;
@@ -548,7 +561,7 @@ __global__ void __launch_bounds__(kTrainThreads, 1)
     if (ok && leader && tiles_next > 0) issue_first_tiles(P.batch[step + 1], n_next, tiles_next);
 
     // ------------------------------------------- reduction + optimizer --
-    if (!grid_sync(P.sync, ++barriers * gridDim.x, &B->sync_ok)) {
+    if (!grid_sync(P.sync, ++barriers * G, &B->sync_ok)) {
       ok = false;
       if (threadIdx.x == 0) atomicOr(P.err, kErrTimeout);
       break;
@@ -556,7 +569,7 @@ __global__ void __launch_bounds__(kTrainThreads, 1)
     // Gather this CTA's slice of every partial (one per CTA that had tiles)
     // behind act_0, many 16-byte copies in flight per thread.
     float4* stg = reinterpret_cast<float4*>(act + kActBytes);  // [active][ncols]
-    const uint32_t active = min(gridDim.x, num_tiles);
+    const uint32_t active = min(G, num_tiles);
     const bool reduce = n > 0 && ncols > 0;
     if (reduce) {
       const uint32_t total = active * ncols;
@@ -604,9 +617,11 @@ __global__ void __launch_bounds__(kTrainThreads, 1)
         if (cc < ncols) {
           const float gsum = part == 0 ? acc.x : part == 1 ? acc.y : part == 2 ? acc.z : acc.w;
           const uint32_t k = 4 * cc + part;  // parameter index within the slice
-          if (P.mode == kTrainStep)
-            adam_one(4 * c0 + k, gsum, n, st, hp, ecache[k], P.entries, P.w16, use16);
-          else
+          if (P.mode == kTrainStep) {
+            nrc_optimizer_entry e = cached ? ecache[k] : P.entries[4 * c0 + k];
+            adam_one(4 * c0 + k, gsum, n, st, hp, e, P.entries, P.w16, use16);
+            if (cached) ecache[k] = e;
+          } else
             P.grad_out[4 * c0 + k] = gsum;
         }
       }
@@ -614,7 +629,7 @@ __global__ void __launch_bounds__(kTrainThreads, 1)
       for (uint32_t k = threadIdx.x; k < 4 * ncols; k += blockDim.x) P.grad_out[4 * c0 + k] = 0.0f;  // no records
     }
     if (has_next) {  // publish the new weights before the next batch loads them
-      if (!grid_sync(P.sync, ++barriers * gridDim.x, &B->sync_ok)) {
+      if (!grid_sync(P.sync, ++barriers * G, &B->sync_ok)) {
         ok = false;
         if (threadIdx.x == 0) atomicOr(P.err, kErrTimeout);
         break;
@@ -624,7 +639,7 @@ __global__ void __launch_bounds__(kTrainThreads, 1)
   cp_async_wait_all();  // entry loads of a launch whose batches were all empty
   // Every CTA has read the step state at launch and passed at least one grid
   // barrier since, so CTA 0 may now write the advanced state.
-  if (P.mode == kTrainStep && ok && barriers > 0 && blockIdx.x == 0 && threadIdx.x == 0) *P.state = st;
+  if (P.mode == kTrainStep && ok && barriers > 0 && rank == 0 && threadIdx.x == 0) *P.state = st;
 
   if (P.loss_acc != nullptr && warp > 0) {
 #pragma unroll
@@ -649,12 +664,43 @@ __global__ void __launch_bounds__(kTrainThreads, 1)
     tc_fence_after();
     tmem_dealloc(tmem, 512);
   }
+  // The group's barrier counter (sync[0]) starts every launch at zero: the last
+  // CTA of the group to get here, when every CTA has left its barrier waits,
+  // resets it and the exit counter (sync[1]).
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(P.sync + 1, 1u) == G - 1) {
+      atomicExch(P.sync, 0u);
+      atomicExch(P.sync + 1, 0u);
+      __threadfence();
+    }
+  }
+}
+
+template <int N>
+cudaError_t launch(const TrainLaunch<N>& L, uint32_t grid, cudaStream_t stream) {
+  cudaLaunchAttribute attr;
+  attr.id = cudaLaunchAttributeCooperative;
+  attr.val.cooperative = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(kTrainThreads);
+  cfg.dynamicSmemBytes = kTrainSmemBytes;
+  cfg.stream = stream;
+  cfg.attrs = &attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, train_steps_kernel<N>, L);
 }
 
 }  // namespace
 
 cudaError_t configure_train_kernels() {
-  return cudaFuncSetAttribute(train_steps_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTrainSmemBytes);
+  cudaError_t e =
+      cudaFuncSetAttribute(train_steps_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTrainSmemBytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(train_steps_kernel<kMaxTrainJobs>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             kTrainSmemBytes);
+  return e;
 }
 
 uint32_t train_smem_bytes() { return kTrainSmemBytes; }
@@ -669,20 +715,31 @@ cudaError_t launch_train(const TrainParams& p, const CUtensorMap* wmap, int max_
   if (p.steps < 1 || p.steps > NRC_TRAIN_BATCH_COUNT) return cudaErrorInvalidValue;
   const uint32_t grid = train_grid(p, max_ctas);
   if (grid < kMinTrainCtas) return cudaErrorInvalidConfiguration;
-  // the grid barrier counts from zero in every launch
-  cudaError_t e = cudaMemsetAsync(p.sync, 0, sizeof(uint32_t), stream);
-  if (e != cudaSuccess) return e;
-  cudaLaunchAttribute attr;
-  attr.id = cudaLaunchAttributeCooperative;
-  attr.val.cooperative = 1;
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(grid);
-  cfg.blockDim = dim3(kTrainThreads);
-  cfg.dynamicSmemBytes = kTrainSmemBytes;
-  cfg.stream = stream;
-  cfg.attrs = &attr;
-  cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, train_steps_kernel, p, *wmap);
+  TrainLaunch<1> L;
+  L.job[0].wmap = *wmap;
+  L.job[0].p = p;
+  L.group_start[0] = 0;
+  L.group_start[1] = grid;
+  L.njobs = 1;
+  return launch(L, grid, stream);
+}
+
+cudaError_t launch_train_many(const TrainJob* jobs, int njobs, const uint32_t* group_size, cudaStream_t stream) {
+  if (njobs < 1 || njobs > kMaxTrainJobs) return cudaErrorInvalidValue;
+  static TrainLaunch<kMaxTrainJobs> L;  // host staging of the kernel parameters (copied at launch)
+  static std::mutex m;
+  std::lock_guard<std::mutex> lock(m);
+  uint32_t grid = 0;
+  for (int j = 0; j < njobs; ++j) {
+    if (jobs[j].p.steps < 1 || jobs[j].p.steps > NRC_TRAIN_BATCH_COUNT) return cudaErrorInvalidValue;
+    if (group_size[j] < 1 || group_size[j] > kMaxTrainCtas) return cudaErrorInvalidConfiguration;
+    L.job[j] = jobs[j];
+    L.group_start[j] = grid;
+    grid += group_size[j];
+  }
+  L.group_start[njobs] = grid;
+  L.njobs = njobs;
+  return launch(L, grid, stream);
 }
 
 }  // namespace nrc

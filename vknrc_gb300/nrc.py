@@ -29,7 +29,7 @@ EXPORTS = [
     "nrc_encode", "nrc_sph_encode", "nrc_infer", "nrc_infer_encoded", "nrc_train", "nrc_gradient", "nrc_frame",
     "nrc_get_weights", "nrc_set_weights", "nrc_get_optimizer", "nrc_set_optimizer", "nrc_get_loss",
     "nrc_get_error", "nrc_get_device_buffers", "nrc_train_noalloc", "nrc_train_batches", "nrc_infer_scatter",
-    "nrc_frame_scatter",
+    "nrc_frame_scatter", "nrc_infer_many", "nrc_train_many", "nrc_plan_query_ctas", "nrc_plan_train_ctas",
 ]
 
 
@@ -73,6 +73,19 @@ def scatter_targets(bias_factor_r=None, factor_gb=None, train_records: Sequence 
             t.train_records[b] = _ptr(r)
             t.train_capacity[b] = r.shape[0]
     return t
+
+
+class QueryJob(ctypes.Structure):
+    """nrc_query_job: one cache's queries in a batched launch."""
+    _fields_ = [("ctx", ctypes.c_void_p), ("inputs", ctypes.c_void_p), ("d_count", ctypes.c_void_p),
+                ("capacity", ctypes.c_uint32), ("out_rgb", ctypes.c_void_p), ("weight_set", ctypes.c_int)]
+
+
+class TrainJob(ctypes.Structure):
+    """nrc_train_job: one cache's chained training steps in a batched launch."""
+    _fields_ = [("ctx", ctypes.c_void_p), ("records", ctypes.c_void_p * TRAIN_BATCH_COUNT),
+                ("d_counts", ctypes.c_void_p * TRAIN_BATCH_COUNT), ("capacity", ctypes.c_uint32),
+                ("nbatches", ctypes.c_int), ("write_use_last", ctypes.c_int)]
 
 
 _lib: Optional[ctypes.CDLL] = None
@@ -119,6 +132,10 @@ def lib(build_if_missing: bool = True) -> ctypes.CDLL:
     L.nrc_frame_scatter.argtypes = [vp, vp, vp, vp, u32, ctypes.POINTER(ScatterTargets), ctypes.POINTER(vp), vp]
     L.nrc_get_device_buffers.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp),
                                          ctypes.POINTER(vp)]
+    L.nrc_infer_many.argtypes = [ctypes.POINTER(QueryJob), u32, vp, vp]
+    L.nrc_train_many.argtypes = [ctypes.POINTER(TrainJob), u32, vp, vp]
+    L.nrc_plan_query_ctas.argtypes = [ctypes.POINTER(QueryJob), u32, vp]
+    L.nrc_plan_train_ctas.argtypes = [ctypes.POINTER(TrainJob), u32, vp]
     _lib = L
     return L
 
@@ -279,3 +296,61 @@ class Cache:
         check(lib().nrc_get_device_buffers(self.h, ctypes.byref(w), ctypes.byref(u), ctypes.byref(e), ctypes.byref(s)),
               "nrc_get_device_buffers")
         return w.value, u.value, e.value, s.value
+
+
+# ------------------------------------------------------------ batched caches --
+def query_job(cache: "Cache", inputs, count, out, capacity=None, weight_set=WEIGHTS_USE) -> QueryJob:
+    """The job holds references to its tensors, so their device memory stays
+    allocated (and distinct) for as long as the job object lives."""
+    j = QueryJob(cache.h, _ptr(inputs), _ptr(count), inputs.shape[0] if capacity is None else capacity,
+                 _ptr(out), weight_set)
+    j._keep = (cache, inputs, count, out)
+    return j
+
+
+def train_job(cache: "Cache", records: Sequence, counts: Sequence, capacity=None, write_use_last=True) -> TrainJob:
+    j = TrainJob()
+    j.ctx = cache.h
+    for b, (r, c) in enumerate(zip(records, counts)):
+        j.records[b] = _ptr(r)
+        j.d_counts[b] = _ptr(c)
+    j.capacity = records[0].shape[0] if capacity is None else capacity
+    j.nbatches = len(records)
+    j.write_use_last = int(write_use_last)
+    j._keep = (cache, list(records), list(counts))  # see query_job
+    return j
+
+
+def _ctas(ctas):
+    if ctas is None:
+        return None
+    a = (ctypes.c_uint32 * len(ctas))(*ctas)
+    return ctypes.cast(a, ctypes.c_void_p), a
+
+
+def infer_many(jobs: Sequence[QueryJob], ctas=None, stream=None) -> None:
+    """nrc_infer_many: every job's queries, one launch per 32 caches."""
+    arr = (QueryJob * len(jobs))(*jobs)
+    c = _ctas(ctas)
+    check(lib().nrc_infer_many(arr, len(jobs), c[0] if c else None, _stream(stream)), "nrc_infer_many")
+
+
+def train_many(jobs: Sequence[TrainJob], ctas=None, stream=None) -> None:
+    """nrc_train_many: every job's chained training steps, one launch per 32 caches."""
+    arr = (TrainJob * len(jobs))(*jobs)
+    c = _ctas(ctas)
+    check(lib().nrc_train_many(arr, len(jobs), c[0] if c else None, _stream(stream)), "nrc_train_many")
+
+
+def plan_query_ctas(jobs: Sequence[QueryJob]) -> list:
+    arr = (QueryJob * len(jobs))(*jobs)
+    out = (ctypes.c_uint32 * len(jobs))()
+    check(lib().nrc_plan_query_ctas(arr, len(jobs), ctypes.cast(out, ctypes.c_void_p)), "nrc_plan_query_ctas")
+    return list(out)
+
+
+def plan_train_ctas(jobs: Sequence[TrainJob]) -> list:
+    arr = (TrainJob * len(jobs))(*jobs)
+    out = (ctypes.c_uint32 * len(jobs))()
+    check(lib().nrc_plan_train_ctas(arr, len(jobs), ctypes.cast(out, ctypes.c_void_p)), "nrc_plan_train_ctas")
+    return list(out)
