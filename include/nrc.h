@@ -295,6 +295,80 @@ NRC_API int nrc_train_many(const nrc_train_job* jobs, uint32_t njobs, const uint
 NRC_API int nrc_plan_query_ctas(const nrc_query_job* jobs, uint32_t njobs, uint32_t* out_ctas);
 NRC_API int nrc_plan_train_ctas(const nrc_train_job* jobs, uint32_t njobs, uint32_t* out_ctas);
 
+/* ---------------------------------------------------------------------------
+ * Serving: a device-resident loop over many render sessions. No counterpart in
+ * the reference, which serves one renderer (src/main.cpp:84-91); each session
+ * here is one cache (weights and Adam state stay on the GPU) plus frame slots in
+ * device memory, and one frame request runs the reference's frame schedule
+ * (src/rg/NRCRenderGraph.cpp:46-80) on a slot: the cache query of its records
+ * with use_weights, then NRC_TRAIN_BATCH_COUNT chained training steps, the last
+ * writing use_weights.
+ *  - Sessions are admitted by the server's device-memory budget: opening one
+ *    that does not fit returns NRC_ERROR_OUT_OF_MEMORY; closing one frees its
+ *    share.
+ *  - Requests are batched continuously: a worker thread takes queued requests
+ *    (first come, first served; one in flight per session, in submission order)
+ *    into the next batched launch as SMs free up, while earlier batches still
+ *    run, up to max_batch_sessions per launch.
+ *  - Every session trains with a fixed CTA group (train_ctas), so its results
+ *    are the same whatever it is batched with.
+ * ------------------------------------------------------------------------- */
+typedef struct nrc_server nrc_server;
+
+typedef struct nrc_server_config {
+  uint64_t hbm_budget_bytes;    /* device memory for session state and frame slots */
+  uint32_t max_batch_sessions;  /* requests per batched launch, 1..32 */
+  uint32_t max_inflight_batches;/* launched, unfinished batches, 1..8 */
+} nrc_server_config;
+
+typedef struct nrc_session_desc {
+  nrc_config cache;        /* the session cache's hyper-parameters and seed */
+  uint32_t max_queries;    /* query records per frame */
+  uint32_t train_records;  /* records per training batch (NRC_TRAIN_BATCH_COUNT per frame) */
+  uint32_t frame_slots;    /* frame buffers in device memory, 1..16 */
+  uint32_t train_ctas;     /* CTAs of the session's training group, 1..152; 0 = from train_records */
+} nrc_session_desc;
+
+/* Device buffers of one frame slot. The caller writes the records and counts,
+ * then submits the slot; after the request completes the slot's out_rgb holds
+ * the clamped query results, the train records hold what the caller wrote
+ * (counts are clamped as nrc_train does). */
+typedef struct nrc_frame_buffers {
+  nrc_input* queries;                             /* max_queries records */
+  uint32_t* query_count;
+  float* out_rgb;                                 /* max_queries x 3 */
+  nrc_train_record* train[NRC_TRAIN_BATCH_COUNT]; /* train_records each */
+  uint32_t* train_count[NRC_TRAIN_BATCH_COUNT];
+} nrc_frame_buffers;
+
+typedef struct nrc_server_stats {
+  uint64_t submitted, completed, batches;
+  uint64_t bytes_in_use;
+  double latency_p50_ms, latency_p99_ms, latency_max_ms; /* submit -> completion, since the last reset */
+  double mean_batch_sessions;
+} nrc_server_stats;
+
+/* Creates the server and its worker thread on the current device. */
+NRC_API int nrc_server_create(const nrc_server_config* cfg, nrc_server** out);
+/* Finishes every submitted request, stops the worker, closes all sessions. */
+NRC_API int nrc_server_destroy(nrc_server* srv);
+NRC_API int nrc_server_open_session(nrc_server* srv, const nrc_session_desc* desc, uint32_t* session);
+/* Waits for the session's requests to finish, then frees its memory. */
+NRC_API int nrc_server_close_session(nrc_server* srv, uint32_t session);
+NRC_API int nrc_server_frame_buffers(nrc_server* srv, uint32_t session, uint32_t slot, nrc_frame_buffers* out);
+/* The session's cache, for nrc_get_weights / nrc_get_optimizer and the like
+ * (only while none of its requests is pending). */
+NRC_API int nrc_server_session_cache(nrc_server* srv, uint32_t session, nrc_context** ctx);
+/* Queues frame slot `slot` of `session`. `ready_event` (a cudaEvent_t, may be
+ * NULL) is waited on by the server's stream before the request runs: record it
+ * after writing the slot. Returns a ticket. */
+NRC_API int nrc_server_submit(nrc_server* srv, uint32_t session, uint32_t slot, void* ready_event, uint64_t* ticket);
+/* Waits until the ticket's request has completed on the GPU (timeout_ms < 0:
+ * no limit; NRC_ERROR_DEVICE_TIMEOUT when it runs out). latency_ms (may be
+ * NULL) receives its submit-to-completion time. */
+NRC_API int nrc_server_wait(nrc_server* srv, uint64_t ticket, double timeout_ms, double* latency_ms);
+NRC_API int nrc_server_get_stats(nrc_server* srv, nrc_server_stats* stats, int reset_latencies);
+
 /* Host copies of the parameter state (synchronous). `which` selects
  * NRC_WEIGHTS_USE or NRC_WEIGHTS_TRAIN for the fp16 vectors. */
 NRC_API int nrc_get_weights(nrc_context* ctx, int which, uint16_t* host_w16);

@@ -17,6 +17,7 @@ struct nrc_context {
   int device = 0;
   int num_sms = 0;
   void* block = nullptr;  // one device allocation, carved below
+  size_t block_bytes = 0;
   __half* w16 = nullptr;  // training weights (reference: weights)
   __half* use16 = nullptr;  // rendering weights (reference: use_weights)
   nrc_optimizer_entry* entries = nullptr;
@@ -51,6 +52,14 @@ cudaError_t make_weight_map(CUtensorMap* map, const void* w16) {
                             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+size_t context_device_bytes(const nrc_context* c) { return c->block_bytes; }
+
+size_t context_device_bytes_for(int num_sms) {
+  auto up = [](size_t x) { return (x + 255) & ~size_t(255); };
+  return 2 * up(kParams * 2) + up(kParams * sizeof(nrc_optimizer_entry)) + up(sizeof(nrc_optimizer_state)) + 512 +
+         up(size_t(num_sms) * kParams * sizeof(float));
 }
 
 }  // namespace nrc
@@ -204,6 +213,7 @@ int nrc_create(const nrc_config* cfg_in, nrc_context** out) {
     delete c;
     return from_cuda(e);
   }
+  c->block_bytes = total;
   uint8_t* b = static_cast<uint8_t*>(c->block);
   c->w16 = reinterpret_cast<__half*>(b + o_w16);
   c->use16 = reinterpret_cast<__half*>(b + o_use);

@@ -122,6 +122,11 @@ cudaError_t launch_train(const TrainParams& p, const CUtensorMap* wmap, int max_
 // context (parameter buffers, partials or barrier counters).
 cudaError_t launch_train_many(const TrainJob* jobs, int njobs, const uint32_t* group_size, cudaStream_t stream);
 
+// Device bytes one context holds (its single allocation), and the same for a
+// context about to be created on a device with num_sms SMs.
+size_t context_device_bytes(const nrc_context* c);
+size_t context_device_bytes_for(int num_sms);
+
 cudaError_t launch_encode(const nrc_input* in, const uint32_t* d_count, uint32_t capacity, uint16_t* out,
                           int num_sms, cudaStream_t stream);
 cudaError_t launch_sph_encode(const float* dirs, const uint32_t* d_count, uint32_t capacity, float* out,

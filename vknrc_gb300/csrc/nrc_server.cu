@@ -1,0 +1,453 @@
+// Serving loop: many render sessions, each a device-resident cache plus frame
+// slots, whose frame requests a worker thread batches continuously into
+// nrc_infer_many / nrc_train_many launches. Host code only.
+//
+// The reference serves a single renderer whose frame is one query pass and four
+// chained training passes (src/rg/NRCRenderGraph.cpp:46-80, driven once per
+// frame from src/main.cpp:84-91); a request here is that frame for one session.
+//
+// Scheduling:
+//   - requests queue in submission order; a session has at most one request in
+//     flight (its training must see the previous frame's weights), so later
+//     requests of a busy session wait while other sessions' requests pass them;
+//   - the worker forms a batch from the eligible requests as long as the batch
+//     has fewer than max_batch_sessions requests and their training groups fit
+//     in the SMs, launches it on its stream (query launch, then training launch,
+//     then an event) and goes on forming the next batch while this one runs, up
+//     to max_inflight_batches unfinished batches;
+//   - finished batches are retired in launch order by polling their events; a
+//     request's latency runs from its submission to the moment the worker sees
+//     its batch's event complete.
+//   - sessions are admitted against a device-memory budget (cache state + frame
+//     slots), so the set of resident sessions never exceeds it.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <mutex>
+#include <new>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "nrc_common.cuh"
+#include "nrc_kernels.h"
+
+namespace {
+
+constexpr uint32_t kMaxBatch = 32;
+constexpr uint32_t kMaxSlots = 16;
+
+using Clock = std::chrono::steady_clock;
+
+int64_t now_ns() {
+  return std::chrono::duration_cast<std::chrono::nanoseconds>(Clock::now().time_since_epoch()).count();
+}
+
+size_t up256(size_t x) { return (x + 255) & ~size_t(255); }
+
+struct Session {
+  bool open = false;
+  nrc_session_desc desc{};
+  nrc_context* ctx = nullptr;
+  void* block = nullptr;  // all frame slots, one allocation
+  size_t bytes = 0;       // cache state + slots, charged to the budget
+  std::vector<nrc_frame_buffers> slots;
+  uint32_t train_ctas = 0;
+  bool in_flight = false;
+  uint32_t pending = 0;   // queued or in flight
+};
+
+struct Request {
+  uint64_t ticket;
+  uint32_t session, slot;
+  cudaEvent_t ready;
+  int64_t t_submit;
+};
+
+// What a launch needs of a request's session, copied under the lock (the
+// session table may grow while the launch is issued).
+struct LaunchItem {
+  nrc_context* ctx;
+  nrc_frame_buffers f;
+  uint32_t max_queries, train_records, train_ctas;
+  cudaEvent_t ready;
+};
+
+struct Batch {
+  cudaEvent_t done;
+  std::vector<Request> reqs;
+};
+
+size_t slot_bytes(const nrc_session_desc& d) {
+  return up256(size_t(d.max_queries) * sizeof(nrc_input)) + 256 + up256(size_t(d.max_queries) * 3 * sizeof(float)) +
+         NRC_TRAIN_BATCH_COUNT * up256(size_t(d.train_records) * sizeof(nrc_train_record)) + 256;
+}
+
+double quantile(std::vector<int64_t> v, double q) {
+  if (v.empty()) return 0.0;
+  const size_t k = std::min(v.size() - 1, static_cast<size_t>(q * double(v.size() - 1) + 0.5));
+  std::nth_element(v.begin(), v.begin() + k, v.end());
+  return double(v[k]) * 1e-6;
+}
+
+}  // namespace
+
+struct nrc_server {
+  nrc_server_config cfg{};
+  int device = 0;
+  int sms = 0;
+  cudaStream_t stream = nullptr;
+  std::mutex m;
+  std::condition_variable cv_work;  // new requests, or stop
+  std::condition_variable cv_done;  // requests completed
+  std::deque<Request> queue;
+  std::deque<Batch> inflight;
+  std::vector<cudaEvent_t> free_events;
+  std::vector<Session> sessions;
+  std::unordered_map<uint64_t, int64_t> done;  // ticket -> latency (ns), until waited on
+  std::vector<int64_t> latencies;
+  uint64_t next_ticket = 1;
+  uint64_t submitted = 0, completed = 0, batches = 0, batched_requests = 0;
+  uint64_t bytes_in_use = 0;
+  bool stop = false;
+  int worker_status = NRC_OK;
+  std::thread worker;
+};
+
+namespace {
+
+cudaEvent_t take_event(nrc_server* S) {
+  if (!S->free_events.empty()) {
+    cudaEvent_t e = S->free_events.back();
+    S->free_events.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+  return e;
+}
+
+// Retires finished batches in launch order. Caller holds the lock.
+bool retire(nrc_server* S) {
+  bool any = false;
+  while (!S->inflight.empty()) {
+    Batch& b = S->inflight.front();
+    const cudaError_t q = cudaEventQuery(b.done);
+    if (q == cudaErrorNotReady) break;
+    if (q != cudaSuccess) S->worker_status = NRC_ERROR_CUDA;
+    const int64_t t = now_ns();
+    for (const Request& r : b.reqs) {
+      Session& s = S->sessions[r.session];
+      s.in_flight = false;
+      --s.pending;
+      S->done[r.ticket] = t - r.t_submit;
+      S->latencies.push_back(t - r.t_submit);
+      ++S->completed;
+    }
+    S->free_events.push_back(b.done);
+    S->inflight.pop_front();
+    any = true;
+  }
+  return any;
+}
+
+// Takes the eligible requests for the next batch out of the queue and fills
+// `items` with what their launch needs. Caller holds the lock.
+std::vector<Request> pick(nrc_server* S, std::vector<LaunchItem>& items) {
+  std::vector<Request> out;
+  items.clear();
+  uint32_t ctas = 0;
+  std::vector<uint32_t> chosen;
+  for (auto it = S->queue.begin(); it != S->queue.end() && out.size() < S->cfg.max_batch_sessions;) {
+    Session& s = S->sessions[it->session];
+    const bool busy = s.in_flight || std::find(chosen.begin(), chosen.end(), it->session) != chosen.end();
+    if (busy) {  // keeps this session's later requests behind it too
+      chosen.push_back(it->session);
+      ++it;
+      continue;
+    }
+    if (ctas + s.train_ctas > static_cast<uint32_t>(S->sms)) break;  // the batch is full: first come, first served
+    ctas += s.train_ctas;
+    chosen.push_back(it->session);
+    s.in_flight = true;
+    items.push_back(LaunchItem{s.ctx, s.slots[it->slot], s.desc.max_queries, s.desc.train_records, s.train_ctas,
+                               it->ready});
+    out.push_back(*it);
+    it = S->queue.erase(it);
+  }
+  return out;
+}
+
+int launch_batch(nrc_server* S, const std::vector<LaunchItem>& items, cudaEvent_t done) {
+  nrc_query_job q[kMaxBatch];
+  nrc_train_job t[kMaxBatch];
+  uint32_t ctas[kMaxBatch];
+  const uint32_t n = static_cast<uint32_t>(items.size());
+  for (uint32_t j = 0; j < n; ++j) {
+    const LaunchItem& it = items[j];
+    const nrc_frame_buffers& f = it.f;
+    if (it.ready != nullptr && cudaStreamWaitEvent(S->stream, it.ready, 0) != cudaSuccess) return NRC_ERROR_CUDA;
+    q[j] = nrc_query_job{it.ctx, f.queries, f.query_count, it.max_queries, f.out_rgb, NRC_WEIGHTS_USE};
+    t[j] = nrc_train_job{};
+    t[j].ctx = it.ctx;
+    for (int b = 0; b < NRC_TRAIN_BATCH_COUNT; ++b) {
+      t[j].records[b] = f.train[b];
+      t[j].d_counts[b] = f.train_count[b];
+    }
+    t[j].capacity = it.train_records;
+    t[j].nbatches = NRC_TRAIN_BATCH_COUNT;
+    t[j].write_use_last = 1;
+    ctas[j] = it.train_ctas;
+  }
+  int st = nrc_infer_many(q, n, nullptr, S->stream);
+  if (st == NRC_OK) st = nrc_train_many(t, n, ctas, S->stream);
+  if (st == NRC_OK && cudaEventRecord(done, S->stream) != cudaSuccess) st = NRC_ERROR_CUDA;
+  return st;
+}
+
+void worker_main(nrc_server* S) {
+  cudaSetDevice(S->device);
+  std::unique_lock<std::mutex> lk(S->m);
+  std::vector<LaunchItem> items;
+  for (;;) {
+    if (retire(S)) S->cv_done.notify_all();
+    if (S->stop && S->queue.empty() && S->inflight.empty()) break;
+    bool launched = false;
+    if (S->inflight.size() < S->cfg.max_inflight_batches && !S->queue.empty()) {
+      std::vector<Request> reqs = pick(S, items);
+      if (!reqs.empty()) {
+        cudaEvent_t ev = take_event(S);
+        lk.unlock();  // launches are asynchronous; submitters need not wait for them
+        const int st = ev ? launch_batch(S, items, ev) : NRC_ERROR_CUDA;
+        lk.lock();
+        if (st != NRC_OK) {
+          // the requests complete as failed: unblock their sessions and waiters
+          S->worker_status = st;
+          for (const Request& r : reqs) {
+            Session& s = S->sessions[r.session];
+            s.in_flight = false;
+            --s.pending;
+            S->done[r.ticket] = -1;
+            ++S->completed;
+          }
+          if (ev) S->free_events.push_back(ev);
+          S->cv_done.notify_all();
+        } else {
+          S->inflight.push_back(Batch{ev, std::move(reqs)});
+          ++S->batches;
+          S->batched_requests += S->inflight.back().reqs.size();
+          launched = true;
+        }
+      }
+    }
+    if (launched) continue;
+    if (S->inflight.empty()) {
+      S->cv_work.wait(lk, [&] { return S->stop || !S->queue.empty(); });
+    } else {
+      // a batch is running: poll its event closely (latency) without holding the lock
+      lk.unlock();
+      std::this_thread::sleep_for(std::chrono::microseconds(5));
+      lk.lock();
+    }
+  }
+}
+
+bool valid_session(nrc_server* S, uint32_t id) { return id < S->sessions.size() && S->sessions[id].open; }
+
+}  // namespace
+
+extern "C" {
+
+int nrc_server_create(const nrc_server_config* cfg, nrc_server** out) {
+  if (cfg == nullptr || out == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  *out = nullptr;
+  if (cfg->max_batch_sessions < 1 || cfg->max_batch_sessions > kMaxBatch || cfg->max_inflight_batches < 1 ||
+      cfg->max_inflight_batches > 8 || cfg->hbm_budget_bytes == 0)
+    return NRC_ERROR_INVALID_ARGUMENT;
+  int dev = 0, count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) return NRC_ERROR_NO_DEVICE;
+  if (cudaGetDevice(&dev) != cudaSuccess) return NRC_ERROR_CUDA;
+  int major = 0, minor = 0, sms = 0;
+  cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+  cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (!(major == 10 && minor == 3)) return NRC_ERROR_UNSUPPORTED_DEVICE;
+  nrc_server* S = new (std::nothrow) nrc_server();
+  if (S == nullptr) return NRC_ERROR_OUT_OF_MEMORY;
+  S->cfg = *cfg;
+  S->device = dev;
+  S->sms = sms;
+  if (cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete S;
+    return NRC_ERROR_CUDA;
+  }
+  S->worker = std::thread(worker_main, S);
+  *out = S;
+  return NRC_OK;
+}
+
+int nrc_server_destroy(nrc_server* S) {
+  if (S == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  {
+    std::lock_guard<std::mutex> lk(S->m);
+    S->stop = true;
+  }
+  S->cv_work.notify_all();
+  if (S->worker.joinable()) S->worker.join();
+  cudaStreamSynchronize(S->stream);
+  for (Session& s : S->sessions) {
+    if (!s.open) continue;
+    nrc_destroy(s.ctx);
+    cudaFree(s.block);
+  }
+  for (cudaEvent_t e : S->free_events) cudaEventDestroy(e);
+  cudaStreamDestroy(S->stream);
+  const int st = S->worker_status;
+  delete S;
+  return st;
+}
+
+int nrc_server_open_session(nrc_server* S, const nrc_session_desc* d, uint32_t* id) {
+  if (S == nullptr || d == nullptr || id == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  if (d->max_queries == 0 || d->train_records == 0 || d->frame_slots < 1 || d->frame_slots > kMaxSlots ||
+      d->train_ctas > static_cast<uint32_t>(S->sms))
+    return NRC_ERROR_INVALID_ARGUMENT;
+  const size_t slots = size_t(d->frame_slots) * slot_bytes(*d);
+  const size_t bytes = slots + nrc::context_device_bytes_for(S->sms);
+  {
+    std::lock_guard<std::mutex> lk(S->m);
+    if (S->bytes_in_use + bytes > S->cfg.hbm_budget_bytes) return NRC_ERROR_OUT_OF_MEMORY;
+    S->bytes_in_use += bytes;  // reserved while the session is built
+  }
+  Session s;
+  s.desc = *d;
+  s.bytes = bytes;
+  // Training group: one CTA per 16 tiles of a batch unless given (a fixed
+  // function of the session alone, so its results do not depend on the mix).
+  const uint32_t tiles = (d->train_records + nrc::kTile - 1) / nrc::kTile;
+  s.train_ctas = d->train_ctas ? d->train_ctas : std::max(1u, std::min<uint32_t>((tiles + 15) / 16, S->sms));
+  int st = nrc_create(&d->cache, &s.ctx);
+  if (st == NRC_OK && cudaMalloc(&s.block, slots) != cudaSuccess) st = NRC_ERROR_OUT_OF_MEMORY;
+  if (st == NRC_OK && cudaMemset(s.block, 0, slots) != cudaSuccess) st = NRC_ERROR_CUDA;
+  if (st != NRC_OK) {
+    if (s.ctx) nrc_destroy(s.ctx);
+    if (s.block) cudaFree(s.block);
+    std::lock_guard<std::mutex> lk(S->m);
+    S->bytes_in_use -= bytes;
+    return st;
+  }
+  uint8_t* p = static_cast<uint8_t*>(s.block);
+  for (uint32_t k = 0; k < d->frame_slots; ++k) {
+    nrc_frame_buffers f{};
+    f.queries = reinterpret_cast<nrc_input*>(p);
+    p += up256(size_t(d->max_queries) * sizeof(nrc_input));
+    f.query_count = reinterpret_cast<uint32_t*>(p);
+    for (int b = 0; b < NRC_TRAIN_BATCH_COUNT; ++b) f.train_count[b] = reinterpret_cast<uint32_t*>(p) + 4 + b;
+    p += 256;
+    f.out_rgb = reinterpret_cast<float*>(p);
+    p += up256(size_t(d->max_queries) * 3 * sizeof(float));
+    for (int b = 0; b < NRC_TRAIN_BATCH_COUNT; ++b) {
+      f.train[b] = reinterpret_cast<nrc_train_record*>(p);
+      p += up256(size_t(d->train_records) * sizeof(nrc_train_record));
+    }
+    p += 256;
+    s.slots.push_back(f);
+  }
+  s.open = true;
+  std::lock_guard<std::mutex> lk(S->m);
+  for (uint32_t k = 0; k < S->sessions.size(); ++k)
+    if (!S->sessions[k].open) {
+      S->sessions[k] = std::move(s);
+      *id = k;
+      return NRC_OK;
+    }
+  S->sessions.push_back(std::move(s));
+  *id = static_cast<uint32_t>(S->sessions.size() - 1);
+  return NRC_OK;
+}
+
+int nrc_server_close_session(nrc_server* S, uint32_t id) {
+  if (S == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  Session s;
+  {
+    std::unique_lock<std::mutex> lk(S->m);
+    if (!valid_session(S, id)) return NRC_ERROR_INVALID_ARGUMENT;
+    S->cv_done.wait(lk, [&] { return S->sessions[id].pending == 0; });
+    s = std::move(S->sessions[id]);
+    S->sessions[id] = Session{};
+    S->bytes_in_use -= s.bytes;
+  }
+  nrc_destroy(s.ctx);
+  cudaFree(s.block);
+  return NRC_OK;
+}
+
+int nrc_server_frame_buffers(nrc_server* S, uint32_t id, uint32_t slot, nrc_frame_buffers* out) {
+  if (S == nullptr || out == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(S->m);
+  if (!valid_session(S, id) || slot >= S->sessions[id].slots.size()) return NRC_ERROR_INVALID_ARGUMENT;
+  *out = S->sessions[id].slots[slot];
+  return NRC_OK;
+}
+
+int nrc_server_session_cache(nrc_server* S, uint32_t id, nrc_context** ctx) {
+  if (S == nullptr || ctx == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(S->m);
+  if (!valid_session(S, id)) return NRC_ERROR_INVALID_ARGUMENT;
+  *ctx = S->sessions[id].ctx;
+  return NRC_OK;
+}
+
+int nrc_server_submit(nrc_server* S, uint32_t id, uint32_t slot, void* ready, uint64_t* ticket) {
+  if (S == nullptr || ticket == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  {
+    std::lock_guard<std::mutex> lk(S->m);
+    if (S->stop || !valid_session(S, id) || slot >= S->sessions[id].slots.size()) return NRC_ERROR_INVALID_ARGUMENT;
+    const uint64_t t = S->next_ticket++;
+    S->queue.push_back(Request{t, id, slot, static_cast<cudaEvent_t>(ready), now_ns()});
+    ++S->sessions[id].pending;
+    ++S->submitted;
+    *ticket = t;
+  }
+  S->cv_work.notify_one();
+  return NRC_OK;
+}
+
+int nrc_server_wait(nrc_server* S, uint64_t ticket, double timeout_ms, double* latency_ms) {
+  if (S == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  std::unique_lock<std::mutex> lk(S->m);
+  if (ticket == 0 || ticket >= S->next_ticket) return NRC_ERROR_INVALID_ARGUMENT;
+  auto ready = [&] { return S->done.count(ticket) != 0; };
+  if (timeout_ms < 0) {
+    S->cv_done.wait(lk, ready);
+  } else if (!S->cv_done.wait_for(lk, std::chrono::duration<double, std::milli>(timeout_ms), ready)) {
+    return NRC_ERROR_DEVICE_TIMEOUT;
+  }
+  const int64_t ns = S->done[ticket];
+  S->done.erase(ticket);
+  if (latency_ms) *latency_ms = double(ns) * 1e-6;
+  return ns < 0 ? (S->worker_status != NRC_OK ? S->worker_status : NRC_ERROR_CUDA) : NRC_OK;
+}
+
+int nrc_server_get_stats(nrc_server* S, nrc_server_stats* st, int reset) {
+  if (S == nullptr || st == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(S->m);
+  st->submitted = S->submitted;
+  st->completed = S->completed;
+  st->batches = S->batches;
+  st->bytes_in_use = S->bytes_in_use;
+  st->latency_p50_ms = quantile(S->latencies, 0.5);
+  st->latency_p99_ms = quantile(S->latencies, 0.99);
+  st->latency_max_ms = S->latencies.empty() ? 0.0 : double(*std::max_element(S->latencies.begin(),
+                                                                               S->latencies.end())) * 1e-6;
+  st->mean_batch_sessions = S->batches ? double(S->batched_requests) / double(S->batches) : 0.0;
+  if (reset) {
+    S->latencies.clear();
+    S->batches = 0;
+    S->batched_requests = 0;
+  }
+  return S->worker_status;
+}
+
+}  // extern "C"

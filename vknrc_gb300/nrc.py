@@ -30,6 +30,9 @@ EXPORTS = [
     "nrc_get_weights", "nrc_set_weights", "nrc_get_optimizer", "nrc_set_optimizer", "nrc_get_loss",
     "nrc_get_error", "nrc_get_device_buffers", "nrc_train_noalloc", "nrc_train_batches", "nrc_infer_scatter",
     "nrc_frame_scatter", "nrc_infer_many", "nrc_train_many", "nrc_plan_query_ctas", "nrc_plan_train_ctas",
+    "nrc_server_create", "nrc_server_destroy", "nrc_server_open_session", "nrc_server_close_session",
+    "nrc_server_frame_buffers", "nrc_server_session_cache", "nrc_server_submit", "nrc_server_wait",
+    "nrc_server_get_stats",
 ]
 
 
@@ -88,6 +91,28 @@ class TrainJob(ctypes.Structure):
                 ("nbatches", ctypes.c_int), ("write_use_last", ctypes.c_int)]
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("max_batch_sessions", ctypes.c_uint32),
+                ("max_inflight_batches", ctypes.c_uint32)]
+
+
+class SessionDesc(ctypes.Structure):
+    _fields_ = [("cache", Config), ("max_queries", ctypes.c_uint32), ("train_records", ctypes.c_uint32),
+                ("frame_slots", ctypes.c_uint32), ("train_ctas", ctypes.c_uint32)]
+
+
+class FrameBuffers(ctypes.Structure):
+    _fields_ = [("queries", ctypes.c_void_p), ("query_count", ctypes.c_void_p), ("out_rgb", ctypes.c_void_p),
+                ("train", ctypes.c_void_p * TRAIN_BATCH_COUNT), ("train_count", ctypes.c_void_p * TRAIN_BATCH_COUNT)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64), ("batches", ctypes.c_uint64),
+                ("bytes_in_use", ctypes.c_uint64), ("latency_p50_ms", ctypes.c_double),
+                ("latency_p99_ms", ctypes.c_double), ("latency_max_ms", ctypes.c_double),
+                ("mean_batch_sessions", ctypes.c_double)]
+
+
 _lib: Optional[ctypes.CDLL] = None
 
 
@@ -136,6 +161,15 @@ def lib(build_if_missing: bool = True) -> ctypes.CDLL:
     L.nrc_train_many.argtypes = [ctypes.POINTER(TrainJob), u32, vp, vp]
     L.nrc_plan_query_ctas.argtypes = [ctypes.POINTER(QueryJob), u32, vp]
     L.nrc_plan_train_ctas.argtypes = [ctypes.POINTER(TrainJob), u32, vp]
+    L.nrc_server_create.argtypes = [ctypes.POINTER(ServerConfig), ctypes.POINTER(vp)]
+    L.nrc_server_destroy.argtypes = [vp]
+    L.nrc_server_open_session.argtypes = [vp, ctypes.POINTER(SessionDesc), ctypes.POINTER(u32)]
+    L.nrc_server_close_session.argtypes = [vp, u32]
+    L.nrc_server_frame_buffers.argtypes = [vp, u32, u32, ctypes.POINTER(FrameBuffers)]
+    L.nrc_server_session_cache.argtypes = [vp, u32, ctypes.POINTER(vp)]
+    L.nrc_server_submit.argtypes = [vp, u32, u32, vp, ctypes.POINTER(u64)]
+    L.nrc_server_wait.argtypes = [vp, u64, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]
+    L.nrc_server_get_stats.argtypes = [vp, ctypes.POINTER(ServerStats), i32]
     _lib = L
     return L
 
@@ -354,3 +388,101 @@ def plan_train_ctas(jobs: Sequence[TrainJob]) -> list:
     out = (ctypes.c_uint32 * len(jobs))()
     check(lib().nrc_plan_train_ctas(arr, len(jobs), ctypes.cast(out, ctypes.c_void_p)), "nrc_plan_train_ctas")
     return list(out)
+
+
+# ------------------------------------------------------------------ serving --
+class SessionCache(Cache):
+    """A view of a server session's cache (state reads only; the server owns it)."""
+
+    def __init__(self, handle):
+        self.h = handle
+
+    def close(self) -> None:
+        self.h = None
+
+
+class _DeviceArray:
+    """Exposes raw device memory through __cuda_array_interface__ (for torch.as_tensor)."""
+
+    def __init__(self, ptr: int, shape, typestr: str):
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": typestr, "data": (ptr, False),
+                                         "version": 3, "strides": None}
+
+
+def device_view(ptr: int, shape, dtype):
+    """A torch tensor viewing `ptr` (no copy); the memory must outlive the view."""
+    import torch
+
+    typestr = {torch.float32: "<f4", torch.int32: "<i4", torch.uint32: "<u4"}[dtype]
+    return torch.as_tensor(_DeviceArray(ptr, shape, typestr), device="cuda")
+
+
+class Server:
+    """nrc_server: device-resident sessions whose frame requests are batched
+    continuously by a worker thread inside libnrc.so."""
+
+    def __init__(self, hbm_budget_bytes: int, max_batch_sessions: int = 32, max_inflight_batches: int = 2):
+        cfg = ServerConfig(hbm_budget_bytes, max_batch_sessions, max_inflight_batches)
+        h = ctypes.c_void_p()
+        check(lib().nrc_server_create(ctypes.byref(cfg), ctypes.byref(h)), "nrc_server_create")
+        self.h = h
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            check(lib().nrc_server_destroy(self.h), "nrc_server_destroy")
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def open_session(self, max_queries: int, train_records: int, frame_slots: int = 2, train_ctas: int = 0,
+                     **cfg) -> int:
+        d = SessionDesc(default_config(**cfg), max_queries, train_records, frame_slots, train_ctas)
+        sid = ctypes.c_uint32()
+        check(lib().nrc_server_open_session(self.h, ctypes.byref(d), ctypes.byref(sid)), "nrc_server_open_session")
+        return sid.value
+
+    def close_session(self, sid: int) -> None:
+        check(lib().nrc_server_close_session(self.h, sid), "nrc_server_close_session")
+
+    def frame_buffers(self, sid: int, slot: int) -> FrameBuffers:
+        f = FrameBuffers()
+        check(lib().nrc_server_frame_buffers(self.h, sid, slot, ctypes.byref(f)), "nrc_server_frame_buffers")
+        return f
+
+    def frame_views(self, sid: int, slot: int, max_queries: int, train_records: int) -> dict:
+        """Torch views of a frame slot: queries (Q, 14), query_count (1,), out (Q, 3),
+        train [4 x (R, 20)], train_count [4 x (1,)]."""
+        import torch
+
+        f = self.frame_buffers(sid, slot)
+        return {"queries": device_view(f.queries, (max_queries, IN_FLOATS), torch.float32),
+                "query_count": device_view(f.query_count, (1,), torch.int32),
+                "out": device_view(f.out_rgb, (max_queries, 3), torch.float32),
+                "train": [device_view(f.train[b], (train_records, TRAIN_FLOATS), torch.float32)
+                          for b in range(TRAIN_BATCH_COUNT)],
+                "train_count": [device_view(f.train_count[b], (1,), torch.int32) for b in range(TRAIN_BATCH_COUNT)]}
+
+    def cache(self, sid: int) -> SessionCache:
+        c = ctypes.c_void_p()
+        check(lib().nrc_server_session_cache(self.h, sid, ctypes.byref(c)), "nrc_server_session_cache")
+        return SessionCache(c)
+
+    def submit(self, sid: int, slot: int, ready_event=None) -> int:
+        t = ctypes.c_uint64()
+        ev = ready_event.cuda_event if ready_event is not None else None
+        check(lib().nrc_server_submit(self.h, sid, slot, ev, ctypes.byref(t)), "nrc_server_submit")
+        return t.value
+
+    def wait(self, ticket: int, timeout_ms: float = -1.0) -> float:
+        lat = ctypes.c_double()
+        check(lib().nrc_server_wait(self.h, ticket, timeout_ms, ctypes.byref(lat)), "nrc_server_wait")
+        return lat.value
+
+    def stats(self, reset: bool = False) -> dict:
+        st = ServerStats()
+        check(lib().nrc_server_get_stats(self.h, ctypes.byref(st), int(reset)), "nrc_server_get_stats")
+        return {k: getattr(st, k) for k, _ in ServerStats._fields_}
