@@ -50,6 +50,9 @@ def parse_args():
     p.add_argument("--e2e-steps", type=int, default=100)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-plain", action="store_true")
+    p.add_argument("--no-batched", action="store_true", help="skip the batched-caches leg")
+    p.add_argument("--no-serving", action="store_true", help="skip the serving leg")
+    p.add_argument("--serve-seconds", type=float, default=2.0, help="duration of the serving leg's arrivals")
     return p.parse_args()
 
 
@@ -279,6 +282,206 @@ def plain_fp16_infer(c, evals, steps=20):
     return Q * steps / (s.elapsed_time(e) / 1e3)
 
 
+# ------------------------------------------------------- batched caches leg --
+BATCHED_QUERIES = [256 * 256, 640 * 360, 960 * 540, 1280 * 720, 1600 * 900, 1920 * 1080, 2048 * 1152, 2560 * 1440]
+BATCHED_TRAIN = [4096, 8192, 16384, 24576, 32768, 40960, 49152, 65536]
+
+
+def _records_view(pool, n):
+    """n query records: slices of the rotated pool frames, concatenated when n
+    exceeds one frame."""
+    import torch
+
+    if n <= pool[0].shape[0]:
+        return pool[0][:n]
+    return torch.cat([pool[0], pool[1][: n - pool[0].shape[0]]])
+
+
+def batched_leg(evals, trains, steps=50):
+    """Eight independent caches with uneven query counts (256x256 .. 2560x1440)
+    and training batches (4,096 .. 65,536 records, four chained steps each):
+    one batched query launch and one batched training launch per frame,
+    captured in a CUDA graph, against the same caches served one after another
+    through the single-cache frame call."""
+    import torch
+
+    from vknrc_gb300 import Cache, nrc
+
+    n = len(BATCHED_QUERIES)
+    caches = [Cache(seed=3000 + j, train_batch_size=BATCHED_TRAIN[j], learning_rate=1e-3, beta2=0.99)
+              for j in range(n)]
+    solo = [Cache(seed=3000 + j, train_batch_size=BATCHED_TRAIN[j], learning_rate=1e-3, beta2=0.99)
+            for j in range(n)]
+    qs = [_records_view(evals, q) for q in BATCHED_QUERIES]
+    outs = [torch.empty((q, 3), dtype=torch.float32, device="cuda") for q in BATCHED_QUERIES]
+    recs = []
+    for j, r in enumerate(BATCHED_TRAIN):
+        src = [torch.cat([trains[(j + k) % len(trains)][b] for k in range((r + R - 1) // R)])[:r] for b in range(B)]
+        recs.append(src)
+    qc = [torch.tensor([q], dtype=torch.int32, device="cuda") for q in BATCHED_QUERIES]
+    tc = [[torch.tensor([r], dtype=torch.int32, device="cuda") for _ in range(B)] for r in BATCHED_TRAIN]
+    qjobs = [nrc.query_job(c, q, k, o) for c, q, k, o in zip(caches, qs, qc, outs)]
+    tjobs = [nrc.train_job(c, rr, t) for c, rr, t in zip(caches, recs, tc)]
+    plan_q, plan_t = nrc.plan_query_ctas(qjobs), nrc.plan_train_ctas(tjobs)
+    stream = torch.cuda.Stream()
+    stream.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            nrc.infer_many(qjobs, stream=stream)
+            nrc.train_many(tjobs, stream=stream)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=stream):
+            nrc.infer_many(qjobs, stream=stream)
+            nrc.train_many(tjobs, stream=stream)
+        for _ in range(3):
+            g.replay()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        for _ in range(steps):
+            g.replay()
+        e.record(stream)
+    stream.synchronize()
+    batched_s = s.elapsed_time(e) / 1e3 / steps
+    # the same work, cache after cache, through nrc_frame
+    cur = torch.cuda.current_stream()
+
+    def solo_frame():
+        for j, c in enumerate(solo):
+            c.frame(qs[j], qc[j], outs[j], recs[j], tc[j])
+
+    for _ in range(3):
+        solo_frame()
+    s2, e2 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s2.record(cur)
+    for _ in range(steps):
+        solo_frame()
+    e2.record(cur)
+    torch.cuda.synchronize()
+    solo_s = s2.elapsed_time(e2) / 1e3 / steps
+    errs = [c.error() for c in caches + solo]
+    for c in caches + solo:
+        c.close()
+    if any(errs):
+        raise RuntimeError(f"device error in the batched leg: {errs}")
+    nq, nr = sum(BATCHED_QUERIES), B * sum(BATCHED_TRAIN)
+    return {
+        "workload": "8 caches: queries 256x256 .. 2560x1440 (uneven), 4 chained training steps of 4,096 .. 65,536 "
+                    "records each; one batched query launch + one batched training launch per frame, CUDA graph",
+        "caches": n, "queries_per_frame": nq, "train_records_per_frame": nr, "steps": steps,
+        "ms_per_frame": batched_s * 1e3, "cache_frames_per_s": n / batched_s, "queries_per_s": nq / batched_s,
+        "train_records_per_s": nr / batched_s,
+        "one_by_one": {"ms_per_frame": solo_s * 1e3, "cache_frames_per_s": n / solo_s,
+                       "what": "nrc_frame per cache, cache after cache (query kernel + training launch each)"},
+        "speedup_vs_one_by_one": solo_s / batched_s,
+        "ctas": {"query": plan_q, "train": plan_t, "chosen_by": "proportional split of the SMs by tiles"},
+    }
+
+
+# --------------------------------------------------------------- serving leg --
+SERVE_RES = [(1280, 720), (1920, 1080), (2560, 1440)]
+
+
+def serving_leg(evals, trains, seconds=2.0, sessions=32, rate=2000.0, budget=40 << 30):
+    """32 render sessions with resolutions drawn from 720p/1080p/1440p, frame
+    requests arriving as a Poisson process (2000 requests/s aggregate), each
+    request = the query of the session's frame records + four chained training
+    steps of 16,384 records on its device-resident cache, sessions admitted
+    under a 40 GB device-memory budget."""
+    import numpy as np
+    import torch
+
+    from vknrc_gb300 import Cache, nrc
+
+    rng = np.random.default_rng(4242)
+    res = [SERVE_RES[i] for i in rng.integers(0, len(SERVE_RES), sessions)]
+    with nrc.Server(budget, max_batch_sessions=32, max_inflight_batches=3) as srv:
+        ids = []
+        for k, (w, h) in enumerate(res):
+            ids.append(srv.open_session(w * h, R, frame_slots=2, seed=5000 + k, learning_rate=1e-3, beta2=0.99))
+        for k, sid in enumerate(ids):
+            q = res[k][0] * res[k][1]
+            for slot in range(2):
+                v = srv.frame_views(sid, slot, q, R)
+                v["queries"].copy_(_records_view(evals[slot:] + evals[:slot], q))
+                v["query_count"].fill_(q)
+                for b in range(B):
+                    v["train"][b].copy_(trains[(k + slot) % len(trains)][b])
+                    v["train_count"][b].fill_(R)
+        torch.cuda.synchronize()
+        used = srv.stats()["bytes_in_use"]
+
+        def run(arrivals):
+            tickets = []
+            t0 = time.perf_counter()
+            nxt = [0] * sessions
+            for t_arr, sess in arrivals:
+                while True:
+                    dt = t_arr - (time.perf_counter() - t0)
+                    if dt <= 0:
+                        break
+                    if dt > 2e-4:
+                        time.sleep(dt - 1e-4)
+                tickets.append(srv.submit(ids[sess], nxt[sess] % 2))
+                nxt[sess] += 1
+            for t in tickets:
+                srv.wait(t, 600000)
+            return time.perf_counter() - t0
+
+        # warm-up, then the Poisson stream
+        run([(0.0, k) for k in range(sessions)])
+        srv.stats(reset=True)
+        n = int(rate * seconds)
+        times = np.cumsum(rng.exponential(1.0 / rate, n))
+        who = rng.integers(0, sessions, n)
+        wall = run(list(zip(times.tolist(), who.tolist())))
+        st_poisson = srv.stats(reset=True)
+        # saturation: every request submitted at once (closed batch of work)
+        m = 8 * sessions
+        wall_sat = run([(0.0, k % sessions) for k in range(m)])
+        st_sat = srv.stats(reset=True)
+        errs = [srv.cache(i).error() for i in ids]
+    if any(errs):
+        raise RuntimeError(f"device error in the serving leg: {errs}")
+    # the plain path: one request at a time through nrc_frame (same mix of resolutions)
+    mix = [res[i] for i in who[:96]]
+    solo = {}
+    for (w, h) in set(mix):
+        with Cache(seed=6000, learning_rate=1e-3, beta2=0.99) as c:
+            q = w * h
+            out = torch.empty((q, 3), dtype=torch.float32, device="cuda")
+            qc = torch.tensor([q], dtype=torch.int32, device="cuda")
+            tc = [torch.tensor([R], dtype=torch.int32, device="cuda") for _ in range(B)]
+            x = _records_view(evals, q)
+            for _ in range(3):
+                c.frame(x, qc, out, trains[0], tc)
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record()
+            for k in range(20):
+                c.frame(x, qc, out, trains[k % len(trains)], tc)
+            e.record()
+            torch.cuda.synchronize()
+            solo[(w, h)] = s.elapsed_time(e) / 1e3 / 20
+    solo_fps = len(mix) / sum(solo[r] for r in mix)
+    sat_fps = m / wall_sat
+    return {
+        "workload": "32 sessions (720p/1080p/1440p drawn from a seeded generator), Poisson arrivals at 2000 req/s, "
+                    "request = query of the frame's records + 4 x 16,384-record training steps; 40 GB budget",
+        "sessions": sessions, "resolutions": {f"{w}x{h}": res.count((w, h)) for (w, h) in SERVE_RES},
+        "bytes_in_use": used, "budget_bytes": budget,
+        "offered_req_per_s": rate, "requests": n, "wall_s": wall,
+        "frames_per_s": n / wall,
+        "latency_ms": {"p50": st_poisson["latency_p50_ms"], "p99": st_poisson["latency_p99_ms"],
+                       "max": st_poisson["latency_max_ms"]},
+        "mean_batch_sessions": st_poisson["mean_batch_sessions"],
+        "saturation": {"requests": m, "frames_per_s": sat_fps, "latency_p50_ms": st_sat["latency_p50_ms"],
+                       "latency_p99_ms": st_sat["latency_p99_ms"],
+                       "mean_batch_sessions": st_sat["mean_batch_sessions"]},
+        "plain_path": {"frames_per_s": solo_fps,
+                       "what": "one request at a time through nrc_frame (fused single-cache path), same resolution mix"},
+        "saturation_vs_plain_path": sat_fps / solo_fps,
+    }
+
+
 def ours_arm(args, world, rank, local):
     import numpy as np
     import torch
@@ -408,6 +611,10 @@ def ours_arm(args, world, rank, local):
     if plain is not None:
         result["plain_fp16"] = {"queries_per_s": plain, "what": "nrc_encode + 6 torch fp16 GEMMs (cuBLAS), infer only",
                                 "fused_infer_queries_per_s": Q / infer_s}
+    if rank == 0 and world == 1 and not args.no_batched:
+        result["batched"] = batched_leg(evals, trains)
+    if rank == 0 and world == 1 and not args.no_serving:
+        result["serving"] = serving_leg(evals, trains, seconds=args.serve_seconds)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         qps, threads, sample, _ = cpu_frame_sample(1, 2, budget_s=12.0)
         result["cpu_baseline"] = {"value": qps, "unit": "queries/s", "cores": threads, "kind": "port",

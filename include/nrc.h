@@ -308,8 +308,9 @@ NRC_API int nrc_plan_train_ctas(const nrc_train_job* jobs, uint32_t njobs, uint3
  *    share.
  *  - Requests are batched continuously: a worker thread takes queued requests
  *    (first come, first served; one in flight per session, in submission order)
- *    into the next batched launch as SMs free up, while earlier batches still
- *    run, up to max_batch_sessions per launch.
+ *    into the next batched launch, up to max_batch_sessions per launch, while
+ *    earlier batches still run; each in-flight batch has its own stream, so the
+ *    batches' kernels overlap on the device.
  *  - Every session trains with a fixed CTA group (train_ctas), so its results
  *    are the same whatever it is batched with.
  * ------------------------------------------------------------------------- */
@@ -326,7 +327,7 @@ typedef struct nrc_session_desc {
   uint32_t max_queries;    /* query records per frame */
   uint32_t train_records;  /* records per training batch (NRC_TRAIN_BATCH_COUNT per frame) */
   uint32_t frame_slots;    /* frame buffers in device memory, 1..16 */
-  uint32_t train_ctas;     /* CTAs of the session's training group, 1..152; 0 = from train_records */
+  uint32_t train_ctas;     /* CTAs of the session's training group, 1..152; 0 = one per 4 tiles of 128 records */
 } nrc_session_desc;
 
 /* Device buffers of one frame slot. The caller writes the records and counts,

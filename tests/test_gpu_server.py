@@ -96,7 +96,7 @@ def test_session_alone_equals_in_mix_and_direct_calls(cuda):
         assert c.error() == 0
     # the same schedule through the batched-cache calls, with the session's CTA group
     with Cache(seed=seed) as ref:
-        g = max(1, min((r // 128 + 15) // 16, 152))
+        g = max(1, min((r // 128 + 3) // 4, 152))
         for k in range(frames):
             queries, train = _frame(seed, k, q, r)
             out = dev(np.full((q, 3), -1, np.float32))

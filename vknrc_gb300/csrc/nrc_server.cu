@@ -12,12 +12,14 @@
 //     requests of a busy session wait while other sessions' requests pass them;
 //   - the worker forms a batch from the eligible requests as long as the batch
 //     has fewer than max_batch_sessions requests and their training groups fit
-//     in the SMs, launches it on its stream (query launch, then training launch,
-//     then an event) and goes on forming the next batch while this one runs, up
-//     to max_inflight_batches unfinished batches;
-//   - finished batches are retired in launch order by polling their events; a
-//     request's latency runs from its submission to the moment the worker sees
-//     its batch's event complete.
+//     in the SMs, launches it (query launch, then training launch, then an
+//     event) on the next of max_inflight_batches streams and goes on forming the
+//     next batch while this one runs: batches hold disjoint sessions, so they
+//     are independent, and their kernels share the SMs (a batch's small
+//     training groups run beside the next batch's queries);
+//   - finished batches are retired by polling their events; a request's latency
+//     runs from its submission to the moment the worker sees its batch's event
+//     complete.
 //   - sessions are admitted against a device-memory budget (cache state + frame
 //     slots), so the set of resident sessions never exceeds it.
 #include <algorithm>
@@ -79,6 +81,13 @@ struct Batch {
   std::vector<Request> reqs;
 };
 
+// Training group of a session: one CTA per four tiles of a training batch, a
+// fixed function of the session alone (its results must not depend on the mix).
+uint32_t default_train_ctas(uint32_t train_records, int sms) {
+  const uint32_t tiles = (train_records + nrc::kTile - 1) / nrc::kTile;
+  return std::max(1u, std::min<uint32_t>((tiles + 3) / 4, static_cast<uint32_t>(std::min(sms, 152))));
+}
+
 size_t slot_bytes(const nrc_session_desc& d) {
   return up256(size_t(d.max_queries) * sizeof(nrc_input)) + 256 + up256(size_t(d.max_queries) * 3 * sizeof(float)) +
          NRC_TRAIN_BATCH_COUNT * up256(size_t(d.train_records) * sizeof(nrc_train_record)) + 256;
@@ -97,7 +106,8 @@ struct nrc_server {
   nrc_server_config cfg{};
   int device = 0;
   int sms = 0;
-  cudaStream_t stream = nullptr;
+  std::vector<cudaStream_t> streams;  // one per in-flight batch
+  uint64_t launched = 0;
   std::mutex m;
   std::condition_variable cv_work;  // new requests, or stop
   std::condition_variable cv_done;  // requests completed
@@ -128,13 +138,17 @@ cudaEvent_t take_event(nrc_server* S) {
   return e;
 }
 
-// Retires finished batches in launch order. Caller holds the lock.
+// Retires finished batches (in any order: they run on different streams).
+// Caller holds the lock.
 bool retire(nrc_server* S) {
   bool any = false;
-  while (!S->inflight.empty()) {
-    Batch& b = S->inflight.front();
+  for (auto bi = S->inflight.begin(); bi != S->inflight.end();) {
+    Batch& b = *bi;
     const cudaError_t q = cudaEventQuery(b.done);
-    if (q == cudaErrorNotReady) break;
+    if (q == cudaErrorNotReady) {
+      ++bi;
+      continue;
+    }
     if (q != cudaSuccess) S->worker_status = NRC_ERROR_CUDA;
     const int64_t t = now_ns();
     for (const Request& r : b.reqs) {
@@ -146,7 +160,7 @@ bool retire(nrc_server* S) {
       ++S->completed;
     }
     S->free_events.push_back(b.done);
-    S->inflight.pop_front();
+    bi = S->inflight.erase(bi);
     any = true;
   }
   return any;
@@ -179,7 +193,7 @@ std::vector<Request> pick(nrc_server* S, std::vector<LaunchItem>& items) {
   return out;
 }
 
-int launch_batch(nrc_server* S, const std::vector<LaunchItem>& items, cudaEvent_t done) {
+int launch_batch(const std::vector<LaunchItem>& items, cudaStream_t stream, cudaEvent_t done) {
   nrc_query_job q[kMaxBatch];
   nrc_train_job t[kMaxBatch];
   uint32_t ctas[kMaxBatch];
@@ -187,7 +201,7 @@ int launch_batch(nrc_server* S, const std::vector<LaunchItem>& items, cudaEvent_
   for (uint32_t j = 0; j < n; ++j) {
     const LaunchItem& it = items[j];
     const nrc_frame_buffers& f = it.f;
-    if (it.ready != nullptr && cudaStreamWaitEvent(S->stream, it.ready, 0) != cudaSuccess) return NRC_ERROR_CUDA;
+    if (it.ready != nullptr && cudaStreamWaitEvent(stream, it.ready, 0) != cudaSuccess) return NRC_ERROR_CUDA;
     q[j] = nrc_query_job{it.ctx, f.queries, f.query_count, it.max_queries, f.out_rgb, NRC_WEIGHTS_USE};
     t[j] = nrc_train_job{};
     t[j].ctx = it.ctx;
@@ -200,9 +214,9 @@ int launch_batch(nrc_server* S, const std::vector<LaunchItem>& items, cudaEvent_
     t[j].write_use_last = 1;
     ctas[j] = it.train_ctas;
   }
-  int st = nrc_infer_many(q, n, nullptr, S->stream);
-  if (st == NRC_OK) st = nrc_train_many(t, n, ctas, S->stream);
-  if (st == NRC_OK && cudaEventRecord(done, S->stream) != cudaSuccess) st = NRC_ERROR_CUDA;
+  int st = nrc_infer_many(q, n, nullptr, stream);
+  if (st == NRC_OK) st = nrc_train_many(t, n, ctas, stream);
+  if (st == NRC_OK && cudaEventRecord(done, stream) != cudaSuccess) st = NRC_ERROR_CUDA;
   return st;
 }
 
@@ -218,8 +232,9 @@ void worker_main(nrc_server* S) {
       std::vector<Request> reqs = pick(S, items);
       if (!reqs.empty()) {
         cudaEvent_t ev = take_event(S);
+        cudaStream_t stream = S->streams[S->launched++ % S->streams.size()];
         lk.unlock();  // launches are asynchronous; submitters need not wait for them
-        const int st = ev ? launch_batch(S, items, ev) : NRC_ERROR_CUDA;
+        const int st = ev ? launch_batch(items, stream, ev) : NRC_ERROR_CUDA;
         lk.lock();
         if (st != NRC_OK) {
           // the requests complete as failed: unblock their sessions and waiters
@@ -278,9 +293,14 @@ int nrc_server_create(const nrc_server_config* cfg, nrc_server** out) {
   S->cfg = *cfg;
   S->device = dev;
   S->sms = sms;
-  if (cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking) != cudaSuccess) {
-    delete S;
-    return NRC_ERROR_CUDA;
+  for (uint32_t k = 0; k < cfg->max_inflight_batches; ++k) {
+    cudaStream_t st = nullptr;
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
+      for (cudaStream_t x : S->streams) cudaStreamDestroy(x);
+      delete S;
+      return NRC_ERROR_CUDA;
+    }
+    S->streams.push_back(st);
   }
   S->worker = std::thread(worker_main, S);
   *out = S;
@@ -295,14 +315,14 @@ int nrc_server_destroy(nrc_server* S) {
   }
   S->cv_work.notify_all();
   if (S->worker.joinable()) S->worker.join();
-  cudaStreamSynchronize(S->stream);
+  for (cudaStream_t x : S->streams) cudaStreamSynchronize(x);
   for (Session& s : S->sessions) {
     if (!s.open) continue;
     nrc_destroy(s.ctx);
     cudaFree(s.block);
   }
   for (cudaEvent_t e : S->free_events) cudaEventDestroy(e);
-  cudaStreamDestroy(S->stream);
+  for (cudaStream_t x : S->streams) cudaStreamDestroy(x);
   const int st = S->worker_status;
   delete S;
   return st;
@@ -323,10 +343,7 @@ int nrc_server_open_session(nrc_server* S, const nrc_session_desc* d, uint32_t* 
   Session s;
   s.desc = *d;
   s.bytes = bytes;
-  // Training group: one CTA per 16 tiles of a batch unless given (a fixed
-  // function of the session alone, so its results do not depend on the mix).
-  const uint32_t tiles = (d->train_records + nrc::kTile - 1) / nrc::kTile;
-  s.train_ctas = d->train_ctas ? d->train_ctas : std::max(1u, std::min<uint32_t>((tiles + 15) / 16, S->sms));
+  s.train_ctas = d->train_ctas ? d->train_ctas : default_train_ctas(d->train_records, S->sms);
   int st = nrc_create(&d->cache, &s.ctx);
   if (st == NRC_OK && cudaMalloc(&s.block, slots) != cudaSuccess) st = NRC_ERROR_OUT_OF_MEMORY;
   if (st == NRC_OK && cudaMemset(s.block, 0, slots) != cudaSuccess) st = NRC_ERROR_CUDA;
