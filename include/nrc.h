@@ -103,7 +103,8 @@ typedef enum nrc_status {
   NRC_ERROR_OUT_OF_MEMORY = 5,
   NRC_ERROR_DEVICE_TIMEOUT = 6, /* a kernel's bounded wait ran out (latched) */
   NRC_ERROR_MISALIGNED = 7,
-  NRC_ERROR_TOO_LARGE = 8 /* more records than nrc_train_noalloc's fixed scratch holds */
+  NRC_ERROR_TOO_LARGE = 8, /* more records than nrc_train_noalloc's fixed scratch holds */
+  NRC_ERROR_BAD_CHECKPOINT = 9 /* checkpoint blob of the wrong size, version or checksum */
 } nrc_status;
 
 /* Which fp16 weight vector a query uses. The reference renders with
@@ -369,6 +370,106 @@ NRC_API int nrc_server_submit(nrc_server* srv, uint32_t session, uint32_t slot, 
  * NULL) receives its submit-to-completion time. */
 NRC_API int nrc_server_wait(nrc_server* srv, uint64_t ticket, double timeout_ms, double* latency_ms);
 NRC_API int nrc_server_get_stats(nrc_server* srv, nrc_server_stats* stats, int reset_latencies);
+
+/* ---------------------------------------------------------------------------
+ * Scene unpack: the reference's packed path-vertex records are expanded to
+ * nrc_input from the scene buffers (UnpackNRCInput, shader/src/NRCRecord.glsl:
+ * 97-125, over shader/src/Scene.glsl:8-71), as nrc_inference.comp:33-36 and
+ * nrc_gradient.comp:29-33 do before the encode.
+ * ------------------------------------------------------------------------- */
+
+/* std430 Material (shader/src/Scene.glsl:12-19), 64 bytes. A texture id of
+ * 0xFFFFFFFF selects the constant colour. */
+typedef struct nrc_material {
+  float diffuse[3];
+  uint32_t diffuse_texture_id;
+  float specular[3];
+  uint32_t specular_texture_id;
+  float emission[3];
+  uint32_t emission_texture_id;
+  float metallic, roughness, ior;
+  uint32_t pad_;
+} nrc_material;
+
+/* One scene texture: R8G8B8A8_SRGB texels, row-major [height][width][4]
+ * (src/VkScene.cpp:190-195). Sampled as the reference's sampler does
+ * (src/rg/NRCRenderGraph.cpp:132): bilinear, REPEAT addressing, one mip level,
+ * sRGB decoded per texel before filtering. */
+typedef struct nrc_texture {
+  const uint8_t* texels;
+  uint32_t width, height;
+} nrc_texture;
+
+/* Scene buffers (device pointers; Scene.glsl:30-48). Counts bound every index a
+ * record or an index buffer holds: a record whose primitive, instance, vertex,
+ * texcoord or material index is out of range unpacks to zeros, and a texture
+ * id at or beyond texture_count reads as the constant colour (the reference
+ * trusts its buffers). */
+typedef struct nrc_scene {
+  const float* vertices;            /* Vertex {x, y, z}, vertex_count */
+  const uint32_t* vertex_indices;   /* 3 per primitive */
+  const float* texcoords;           /* vec2, texcoord_count */
+  const uint32_t* texcoord_indices; /* 3 per primitive */
+  const nrc_material* materials;    /* material_count */
+  const uint32_t* material_ids;     /* per primitive */
+  const float* transforms;          /* per instance: mat3x4, 3 columns of 4 floats (p' = vec4(p, 1) * T) */
+  const nrc_texture* textures;      /* device array, texture_count entries */
+  uint32_t vertex_count, texcoord_count, material_count, primitive_count, instance_count, texture_count;
+} nrc_scene;
+
+/* PackedNRCInput, NRCEvalRecord, NRCTrainRecord (NRCRecord.glsl:6-38). */
+typedef struct nrc_packed_input {
+  uint32_t primitive_id;
+  uint32_t flip_bit_instance_id; /* bit 31: flip the normal; bits 0..30: instance */
+  uint32_t barycentric_2x16u;    /* unorm16 pair: barycentrics 1 and 2 */
+  uint32_t scattered_dir_2x16u;  /* unorm16 pair: sphere-encoded direction */
+} nrc_packed_input;
+
+typedef struct nrc_eval_record {
+  uint32_t dst; /* destination word, as nrc_infer_scatter takes it */
+  nrc_packed_input input;
+} nrc_eval_record;
+
+typedef struct nrc_packed_train_record {
+  float bias[3];
+  float factor[3];
+  nrc_packed_input input;
+} nrc_packed_train_record;
+
+/* Unpacks min(*d_count, capacity) eval records into d_inputs (and their
+ * destination words into d_dst, may be NULL), ready for nrc_infer_scatter. */
+NRC_API int nrc_unpack_eval(const nrc_scene* scene, const nrc_eval_record* d_records, const uint32_t* d_count,
+                            uint32_t capacity, nrc_input* d_inputs, uint32_t* d_dst, void* stream);
+
+/* Unpacks min(*d_count, capacity) train records (bias and factor copied) into
+ * d_out, ready for nrc_train / nrc_train_batches. */
+NRC_API int nrc_unpack_train(const nrc_scene* scene, const nrc_packed_train_record* d_records,
+                             const uint32_t* d_count, uint32_t capacity, nrc_train_record* d_out, void* stream);
+
+/* Screen pass (shader/src/screen.frag:10-31) on a headless image: `d_color` is
+ * the composited rgba32f image ([height][width][4], rgb used; the bias_factor_r
+ * image after nrc_infer_scatter). With accumulate != 0 the color becomes the
+ * running average (color + acc * accumulate_count) / (accumulate_count + 1)
+ * (none when the count is 0) and is stored to d_accumulate (rgba32f, alpha 0),
+ * as the reference's accumulation image. Then the Hejl 2015 filmic tone map
+ * (white point 3.2) and gamma 1/2.2; results to d_out_rgba8 (UNORM8, alpha 255)
+ * and/or d_out_rgba (float, alpha 1), either may be NULL. The tone curve's small
+ * negative values near black take pow() of 0. Replaces rg::ScreenPass
+ * (src/rg/ScreenPass.cpp:62-71) minus the swapchain. */
+NRC_API int nrc_screen(const float* d_color, float* d_accumulate, uint32_t width, uint32_t height, int accumulate,
+                       uint32_t accumulate_count, uint8_t* d_out_rgba8, float* d_out_rgba, void* stream);
+
+/* Checkpoints of one cache (no counterpart in the reference, which keeps its
+ * cache for the process's lifetime): a self-describing host blob of
+ * nrc_checkpoint_bytes() bytes holding the hyper-parameters, the optimizer step
+ * state, the Adam entries {m, v, w, ema} and both fp16 weight vectors, with a
+ * checksum. nrc_load_checkpoint restores all of them into an existing context
+ * (any seed), so training continues exactly as it would have in the saved one;
+ * a blob of the wrong size, version or checksum returns
+ * NRC_ERROR_BAD_CHECKPOINT and changes nothing. Both are synchronous. */
+NRC_API size_t nrc_checkpoint_bytes(void);
+NRC_API int nrc_save_checkpoint(nrc_context* ctx, void* host_blob, size_t bytes);
+NRC_API int nrc_load_checkpoint(nrc_context* ctx, const void* host_blob, size_t bytes);
 
 /* Host copies of the parameter state (synchronous). `which` selects
  * NRC_WEIGHTS_USE or NRC_WEIGHTS_TRAIN for the fp16 vectors. */

@@ -497,3 +497,166 @@ void oracle_scatter(const float* pred, const uint32_t* dst, int64_t n, float* bi
     }
   }
 }
+
+/* ---------------------------------------------------------- screen -- */
+/* The screen pass, shader/src/screen.frag:10-31: optional running average into
+ * the accumulation image (:20-26), ToneMapFilmic_Hejl2015 with white point 3.2
+ * (:10-15), gamma 1/2.2 (:29). GLSL leaves contraction to its compiler; this
+ * restatement fixes one sequence (each `a * b + c` one fused multiply-add,
+ * `color += acc * count` one too) that the GPU kernel repeats. pow() of a
+ * negative base is undefined in GLSL; the tone curve dips below zero near black
+ * (about -6e-4 at 0), so the base is clamped to zero first. rgba8 is the UNORM
+ * conversion round(clamp(x, 0, 1) * 255), ties to even. */
+static inline float hejl_curve(float x) {
+  const float va = fmaf(1.425f, x, 0.05f);
+  return fmaf(x, va, 0.004f) / fmaf(x, va + 0.55f, 0.0491f) - 0.0821f;
+}
+
+void oracle_screen(const float* color, float* accumulate, uint32_t width, uint32_t height, int accumulate_on,
+                   uint32_t accumulate_count, uint8_t* out_rgba8, float* out_rgba) {
+  const float wf = hejl_curve(3.2f); /* vf.w: the white point through the same curve */
+  const int64_t n = (int64_t)width * height;
+  for (int64_t i = 0; i < n; ++i) {
+    float c[3] = {color[4 * i], color[4 * i + 1], color[4 * i + 2]};
+    if (accumulate_on) {
+      if (accumulate_count != 0) {
+        const float k = (float)accumulate_count, k1 = (float)(accumulate_count + 1u);
+        for (int j = 0; j < 3; ++j) c[j] = fmaf(accumulate[4 * i + j], k, c[j]) / k1;
+      }
+      for (int j = 0; j < 3; ++j) accumulate[4 * i + j] = c[j];
+      accumulate[4 * i + 3] = 0.0f;
+    }
+    for (int j = 0; j < 3; ++j) {
+      const float t = hejl_curve(c[j]) / wf;
+      const float s = powf(fmaxf(t, 0.0f), 1.0f / 2.2f);
+      if (out_rgba) out_rgba[4 * i + j] = s;
+      if (out_rgba8) out_rgba8[4 * i + j] = (uint8_t)lrintf(fminf(fmaxf(s, 0.0f), 1.0f) * 255.0f);
+    }
+    if (out_rgba) out_rgba[4 * i + 3] = 1.0f;
+    if (out_rgba8) out_rgba8[4 * i + 3] = 255;
+  }
+}
+
+/* ---------------------------------------------------------- unpack -- */
+/* UnpackNRCInput (shader/src/NRCRecord.glsl:97-125) over the scene buffers
+ * (shader/src/Scene.glsl:50-71) and the reference's texture sampler (bilinear,
+ * REPEAT, one level, R8G8B8A8_SRGB: src/rg/NRCRenderGraph.cpp:132,
+ * src/VkScene.cpp:190). GLSL leaves the op sequence to its compiler; this
+ * restatement fixes one that the GPU kernel repeats: dot products and
+ * interpolations as fused multiply-add chains in component order, cross
+ * products as multiply-then-subtract, normalize as a division by sqrt, unorm16
+ * as u / 65535, lerp(x, y, t) = fma(t, y - x, x), exact fp32 filter weights
+ * (hardware samplers quantise them), sRGB decoded per texel through a table
+ * computed in double. Records with out-of-range indices unpack to zeros; a
+ * texture id at or beyond the texture count reads as the constant colour. */
+static float g_srgb[256];
+static int g_srgb_ready = 0;
+
+static void srgb_init(void) {
+  if (g_srgb_ready) return;
+  for (int i = 0; i < 256; ++i) {
+    const double c = i / 255.0;
+    g_srgb[i] = (float)(c <= 0.04045 ? c / 12.92 : pow((c + 0.055) / 1.055, 2.4));
+  }
+  g_srgb_ready = 1;
+}
+
+static inline float unorm16f(uint32_t u) { return (float)(u & 0xFFFFu) / 65535.0f; }
+static inline float lerpf(float x, float y, float t) { return fmaf(t, y - x, x); }
+static inline float interpf(float a, float b, float c, float w0, float w1, float w2) {
+  return fmaf(c, w2, fmaf(b, w1, a * w0));
+}
+
+static uint32_t wrapf(float f, uint32_t n) {
+  const float nf = (float)n;
+  int r = (int)fmaf(-nf, floorf(f / nf), f);
+  if (r < 0) r += (int)n;
+  if (r >= (int)n) r -= (int)n;
+  return (uint32_t)r;
+}
+
+static void sample_tex(const uint8_t* texels, uint32_t w, uint32_t h, float tu, float tv, float out[3]) {
+  if (w == 0 || h == 0 || texels == NULL) {
+    out[0] = out[1] = out[2] = 0.0f;
+    return;
+  }
+  float u = fmaf(tu, (float)w, -0.5f), v = fmaf(tv, (float)h, -0.5f);
+  if (!(fabsf(u) < 8388608.0f)) u = 0.0f;
+  if (!(fabsf(v) < 8388608.0f)) v = 0.0f;
+  const float fu = floorf(u), fv = floorf(v);
+  const float a = u - fu, b = v - fv;
+  const uint32_t i0 = wrapf(fu, w), j0 = wrapf(fv, h);
+  const uint32_t i1 = i0 + 1 == w ? 0 : i0 + 1, j1 = j0 + 1 == h ? 0 : j0 + 1;
+  const uint8_t* t00 = texels + 4 * ((size_t)j0 * w + i0);
+  const uint8_t* t10 = texels + 4 * ((size_t)j0 * w + i1);
+  const uint8_t* t01 = texels + 4 * ((size_t)j1 * w + i0);
+  const uint8_t* t11 = texels + 4 * ((size_t)j1 * w + i1);
+  for (int c = 0; c < 3; ++c)
+    out[c] = lerpf(lerpf(g_srgb[t00[c]], g_srgb[t10[c]], a), lerpf(g_srgb[t01[c]], g_srgb[t11[c]], a), b);
+}
+
+void oracle_unpack(const oracle_scene* S, const uint32_t* packed, int64_t n, int64_t stride_words,
+                   float* out, int64_t out_stride) {
+  srgb_init();
+  const float pi = 3.14159265358979323846f;
+  for (int64_t i = 0; i < n; ++i) {
+    const uint32_t* in = packed + i * stride_words;
+    float* r = out + i * out_stride;
+    for (int k = 0; k < 14; ++k) r[k] = 0.0f;
+    const uint32_t prim = in[0], inst = in[1] & 0x7FFFFFFFu;
+    const int flip = (in[1] >> 31) != 0;
+    if (prim >= S->primitive_count || inst >= S->instance_count) continue;
+    uint32_t vi[3], ti[3];
+    int ok = 1;
+    for (int k = 0; k < 3; ++k) {
+      vi[k] = S->vertex_indices[(size_t)prim * 3 + k];
+      ti[k] = S->texcoord_indices[(size_t)prim * 3 + k];
+      if (vi[k] >= S->vertex_count || ti[k] >= S->texcoord_count) ok = 0;
+    }
+    const uint32_t mid = S->material_ids[prim];
+    if (!ok || mid >= S->material_count) continue;
+    const float* T = S->transforms + (size_t)inst * 12;
+    float v[3][3];
+    for (int k = 0; k < 3; ++k) {
+      const float* p = S->vertices + (size_t)vi[k] * 3;
+      for (int c = 0; c < 3; ++c) {
+        const float* col = T + 4 * c;
+        v[k][c] = fmaf(p[2], col[2], fmaf(p[1], col[1], p[0] * col[0])) + col[3];
+      }
+    }
+    float e1[3], e2[3], nn[3];
+    for (int c = 0; c < 3; ++c) {
+      e1[c] = v[1][c] - v[0][c];
+      e2[c] = v[2][c] - v[0][c];
+    }
+    nn[0] = e1[1] * e2[2] - e1[2] * e2[1];
+    nn[1] = e1[2] * e2[0] - e1[0] * e2[2];
+    nn[2] = e1[0] * e2[1] - e1[1] * e2[0];
+    const float len = sqrtf(fmaf(nn[2], nn[2], fmaf(nn[1], nn[1], nn[0] * nn[0])));
+    for (int c = 0; c < 3; ++c) nn[c] = flip ? -(nn[c] / len) : nn[c] / len;
+    const float b1 = unorm16f(in[2]), b2 = unorm16f(in[2] >> 16);
+    const float b0 = (1.0f - b1) - b2;
+    for (int c = 0; c < 3; ++c) r[c] = interpf(v[0][c], v[1][c], v[2][c], b0, b1, b2);
+    r[3] = unorm16f(in[3]);
+    r[4] = unorm16f(in[3] >> 16);
+    const float zc = nn[2] < -1.0f ? -1.0f : (nn[2] > 1.0f ? 1.0f : nn[2]);
+    r[5] = (nn[0] == 0.0f && nn[1] == 0.0f) ? 0.5f : 0.5f + atan2f(nn[1], nn[0]) / (2.0f * pi);
+    r[6] = acosf(zc) / pi;
+    const oracle_material* m = S->materials + mid;
+    r[7] = m->roughness;
+    const float* tc[3];
+    for (int k = 0; k < 3; ++k) tc[k] = S->texcoords + (size_t)ti[k] * 2;
+    const float tu = interpf(tc[0][0], tc[1][0], tc[2][0], b0, b1, b2);
+    const float tv = interpf(tc[0][1], tc[1][1], tc[2][1], b0, b1, b2);
+    const uint32_t ids[2] = {m->diffuse_texture_id, m->specular_texture_id};
+    const float* konst[2] = {m->diffuse, m->specular};
+    for (int c = 0; c < 2; ++c) {
+      float col[3] = {konst[c][0], konst[c][1], konst[c][2]};
+      if (ids[c] != 0xFFFFFFFFu && ids[c] < S->texture_count) {
+        const oracle_texture* t = S->textures + ids[c];
+        sample_tex(t->texels, t->width, t->height, tu, tv, col);
+      }
+      for (int k = 0; k < 3; ++k) r[8 + 3 * c + k] = col[k];
+    }
+  }
+}

@@ -87,6 +87,48 @@ void oracle_adam(float* entries, const float* grad, uint32_t count, const oracle
 void oracle_scatter(const float* pred, const uint32_t* dst, int64_t n, float* bias_factor_r, const float* factor_gb,
                     uint32_t width, uint32_t height, float* const* train, const uint32_t* train_cap);
 
+/* Scene buffers for oracle_unpack, the host mirror of nrc_scene (include/nrc.h);
+ * pointers are host pointers. */
+typedef struct oracle_material {
+  float diffuse[3];
+  uint32_t diffuse_texture_id;
+  float specular[3];
+  uint32_t specular_texture_id;
+  float emission[3];
+  uint32_t emission_texture_id;
+  float metallic, roughness, ior;
+  uint32_t pad_;
+} oracle_material;
+
+typedef struct oracle_texture {
+  const uint8_t* texels;
+  uint32_t width, height;
+} oracle_texture;
+
+typedef struct oracle_scene {
+  const float* vertices;
+  const uint32_t* vertex_indices;
+  const float* texcoords;
+  const uint32_t* texcoord_indices;
+  const oracle_material* materials;
+  const uint32_t* material_ids;
+  const float* transforms;
+  const oracle_texture* textures;
+  uint32_t vertex_count, texcoord_count, material_count, primitive_count, instance_count, texture_count;
+} oracle_scene;
+
+/* UnpackNRCInput (NRCRecord.glsl:97-125) of n packed inputs (4 words each,
+ * records stride_words apart) into nrc_input floats (14 each, out_stride apart). */
+void oracle_unpack(const oracle_scene* scene, const uint32_t* packed, int64_t n, int64_t stride_words, float* out,
+                   int64_t out_stride);
+
+/* Screen pass (shader/src/screen.frag:10-31) over width x height rgba32f pixels:
+ * color (rgb used) -> optional running average into accumulate (rgba32f, updated
+ * in place when accumulate_on) -> Hejl 2015 filmic tone map (white 3.2) -> gamma
+ * 1/2.2 -> out_rgba (float, alpha 1) and/or out_rgba8 (UNORM8, alpha 255). */
+void oracle_screen(const float* color, float* accumulate, uint32_t width, uint32_t height, int accumulate_on,
+                   uint32_t accumulate_count, uint8_t* out_rgba8, float* out_rgba);
+
 #ifdef __cplusplus
 }
 #endif

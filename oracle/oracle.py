@@ -42,6 +42,8 @@ def lib() -> ctypes.CDLL:
         _lib.oracle_prepare.argtypes = [ctypes.c_uint32, vp, vp]
         _lib.oracle_prepare.restype = ctypes.c_uint32
         _lib.oracle_adam.argtypes = [vp, vp, ctypes.c_uint32, vp, vp, vp, vp, i32]
+        _lib.oracle_screen.argtypes = [vp, vp, ctypes.c_uint32, ctypes.c_uint32, i32, ctypes.c_uint32, vp, vp]
+        _lib.oracle_unpack.argtypes = [vp, vp, i64, i64, vp, i64]
         _lib.oracle_expf.argtypes = [f32]
         _lib.oracle_expf.restype = f32
     return _lib
@@ -148,6 +150,56 @@ def scatter(pred, dst, bias_factor_r, factor_gb, train_records):
             ptrs[b] = t.ctypes.data
             caps[b] = t.shape[0]
     lib().oracle_scatter(_p(pred), _p(dst), dst.shape[0], _p(bias_factor_r), _p(gb), w, h, ptrs, caps)
+
+
+def screen(color, accumulate=None, accumulate_count=0):
+    """Screen pass (screen.frag:10-31) on host arrays: color (H, W, 4) float32;
+    accumulate (H, W, 4) float32 updated in place when given. Returns
+    (rgba8 (H, W, 4) uint8, rgba (H, W, 4) float32)."""
+    c = _c(color, np.float32)
+    h, w = c.shape[0], c.shape[1]
+    o8 = np.empty((h, w, 4), np.uint8)
+    of = np.empty((h, w, 4), np.float32)
+    if accumulate is not None:
+        assert accumulate.dtype == np.float32 and accumulate.flags.c_contiguous
+    lib().oracle_screen(_p(c), _p(accumulate) if accumulate is not None else None, w, h, int(accumulate is not None),
+                        accumulate_count, _p(o8), _p(of))
+    return o8, of
+
+
+class _Scene(ctypes.Structure):
+    _fields_ = [("vertices", ctypes.c_void_p), ("vertex_indices", ctypes.c_void_p), ("texcoords", ctypes.c_void_p),
+                ("texcoord_indices", ctypes.c_void_p), ("materials", ctypes.c_void_p),
+                ("material_ids", ctypes.c_void_p), ("transforms", ctypes.c_void_p), ("textures", ctypes.c_void_p),
+                ("vertex_count", ctypes.c_uint32), ("texcoord_count", ctypes.c_uint32),
+                ("material_count", ctypes.c_uint32), ("primitive_count", ctypes.c_uint32),
+                ("instance_count", ctypes.c_uint32), ("texture_count", ctypes.c_uint32)]
+
+
+class _Texture(ctypes.Structure):
+    _fields_ = [("texels", ctypes.c_void_p), ("width", ctypes.c_uint32), ("height", ctypes.c_uint32)]
+
+
+def unpack(sc: dict, packed_words: np.ndarray, first_word: int = 0) -> np.ndarray:
+    """UnpackNRCInput (NRCRecord.glsl:97-125) on host: packed_words (n, k)
+    uint32 records whose packed input starts at column first_word. Returns
+    (n, 14) float32 nrc_input records."""
+    arrs = {k: np.ascontiguousarray(v) for k, v in sc.items() if k != "textures"}
+    texs = [np.ascontiguousarray(t) for t in sc["textures"]]
+    ttab = (_Texture * max(1, len(texs)))()
+    for i, t in enumerate(texs):
+        ttab[i] = _Texture(t.ctypes.data, t.shape[1], t.shape[0])
+    S = _Scene(_p(arrs["vertices"]), _p(arrs["vertex_indices"]), _p(arrs["texcoords"]), _p(arrs["texcoord_indices"]),
+               _p(arrs["materials"]), _p(arrs["material_ids"]), _p(arrs["transforms"]),
+               ctypes.cast(ttab, ctypes.c_void_p), arrs["vertices"].shape[0], arrs["texcoords"].shape[0],
+               arrs["materials"].shape[0], arrs["vertex_indices"].shape[0], arrs["transforms"].shape[0], len(texs))
+    w = np.ascontiguousarray(packed_words, np.uint32)
+    n = w.shape[0]
+    out = np.empty((n, 14), np.float32)
+    base = w[:, first_word:]
+    lib().oracle_unpack(ctypes.byref(S), _p(np.ascontiguousarray(base)) if first_word else _p(w), n,
+                        base.shape[1] if first_word else w.shape[1], _p(out), 14)
+    return out
 
 
 class OptState(ctypes.Structure):

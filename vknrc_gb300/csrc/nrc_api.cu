@@ -150,6 +150,7 @@ const char* nrc_status_string(int s) {
     case NRC_ERROR_DEVICE_TIMEOUT: return "a kernel's bounded wait timed out";
     case NRC_ERROR_MISALIGNED: return "device buffer not 16-byte aligned";
     case NRC_ERROR_TOO_LARGE: return "more records than the fixed no-allocation scratch holds (16,384)";
+    case NRC_ERROR_BAD_CHECKPOINT: return "checkpoint blob of the wrong size, version or checksum";
     default: return "unknown status";
   }
 }
@@ -669,6 +670,150 @@ int nrc_train_many(const nrc_train_job* jobs, uint32_t n, const uint32_t* ctas, 
     const cudaError_t e = nrc::launch_train_many(tj.data(), static_cast<int>(m), g, static_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return from_cuda(e);
   }
+  return NRC_OK;
+}
+
+// ---------------------------------------------------------------- unpack --
+static int scene_check(const nrc_scene* sc) {
+  if (sc == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  const bool geometry = sc->primitive_count > 0 && sc->instance_count > 0;
+  if (geometry && (sc->vertices == nullptr || sc->vertex_indices == nullptr || sc->texcoords == nullptr ||
+                   sc->texcoord_indices == nullptr || sc->materials == nullptr || sc->material_ids == nullptr ||
+                   sc->transforms == nullptr))
+    return NRC_ERROR_INVALID_ARGUMENT;
+  if (sc->texture_count > 0 && sc->textures == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  if ((reinterpret_cast<uintptr_t>(sc->materials) & 15u) || (reinterpret_cast<uintptr_t>(sc->textures) & 7u))
+    return NRC_ERROR_MISALIGNED;
+  return NRC_OK;
+}
+
+int nrc_unpack_eval(const nrc_scene* sc, const nrc_eval_record* rec, const uint32_t* d_count, uint32_t capacity,
+                    nrc_input* out, uint32_t* out_dst, void* stream) {
+  int s = scene_check(sc);
+  if (s != NRC_OK) return s;
+  if (capacity == 0) return NRC_OK;
+  if (rec == nullptr || d_count == nullptr || out == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  if ((reinterpret_cast<uintptr_t>(rec) & 3u) || (reinterpret_cast<uintptr_t>(out) & 7u) ||
+      (reinterpret_cast<uintptr_t>(out_dst) & 3u))
+    return NRC_ERROR_MISALIGNED;
+  return from_cuda(nrc::launch_unpack(*sc, false, rec, d_count, capacity, out, out_dst, device_sms(),
+                                      static_cast<cudaStream_t>(stream)));
+}
+
+int nrc_unpack_train(const nrc_scene* sc, const nrc_packed_train_record* rec, const uint32_t* d_count,
+                     uint32_t capacity, nrc_train_record* out, void* stream) {
+  int s = scene_check(sc);
+  if (s != NRC_OK) return s;
+  if (capacity == 0) return NRC_OK;
+  if (rec == nullptr || d_count == nullptr || out == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  if ((reinterpret_cast<uintptr_t>(rec) & 3u) || !aligned16(out)) return NRC_ERROR_MISALIGNED;
+  return from_cuda(nrc::launch_unpack(*sc, true, rec, d_count, capacity, out, nullptr, device_sms(),
+                                      static_cast<cudaStream_t>(stream)));
+}
+
+// ---------------------------------------------------------------- screen --
+int nrc_screen(const float* color, float* accum, uint32_t width, uint32_t height, int accumulate,
+               uint32_t accumulate_count, uint8_t* out8, float* outf, void* stream) {
+  if (width == 0 || height == 0) return NRC_OK;
+  if (uint64_t(width) * height > 0xFFFFFFFFull) return NRC_ERROR_INVALID_ARGUMENT;
+  if (color == nullptr || (accumulate && accum == nullptr)) return NRC_ERROR_INVALID_ARGUMENT;
+  if (!aligned16(color) || (accumulate && !aligned16(accum)) || (outf && !aligned16(outf)) ||
+      (out8 && (reinterpret_cast<uintptr_t>(out8) & 3u)))
+    return NRC_ERROR_MISALIGNED;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return from_cuda(nrc::launch_screen(color, accumulate ? accum : nullptr, width, height, accumulate != 0,
+                                      accumulate_count, out8, outf, sms, static_cast<cudaStream_t>(stream)));
+}
+
+// ------------------------------------------------------------ checkpoints --
+// Blob layout (little-endian): a 64-byte header, then the step state padded to
+// 32 bytes, the Adam entries, the training weights and the rendering weights.
+//   0 magic "NRCCKPT1" | 8 version | 12 parameter count | 16 batch cap |
+//   20 lr, beta1, beta2, eps, ema alpha, loss scale (f32) | 44 use_ema |
+//   48 payload bytes (u64) | 56 FNV-1a 64 of the payload
+namespace {
+constexpr size_t kCkptHeader = 64;
+constexpr size_t kCkptPayload = 32 + size_t(kParams) * sizeof(nrc_optimizer_entry) + 2 * size_t(kParams) * 2;
+constexpr uint32_t kCkptVersion = 1;
+
+uint64_t fnv1a(const uint8_t* p, size_t n) {
+  uint64_t h = 1469598103934665603ull;
+  for (size_t i = 0; i < n; ++i) {
+    h ^= p[i];
+    h *= 1099511628211ull;
+  }
+  return h;
+}
+}  // namespace
+
+size_t nrc_checkpoint_bytes(void) { return kCkptHeader + kCkptPayload; }
+
+int nrc_save_checkpoint(nrc_context* c, void* blob, size_t bytes) {
+  int s = check_ctx(c);
+  if (s != NRC_OK) return s;
+  if (blob == nullptr || bytes < nrc_checkpoint_bytes()) return NRC_ERROR_INVALID_ARGUMENT;
+  uint8_t* b = static_cast<uint8_t*>(blob);
+  std::memset(b, 0, nrc_checkpoint_bytes());
+  uint8_t* pay = b + kCkptHeader;
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(pay, c->state, sizeof(nrc_optimizer_state), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(pay + 32, c->entries, size_t(kParams) * sizeof(nrc_optimizer_entry), cudaMemcpyDeviceToHost);
+  uint8_t* w = pay + 32 + size_t(kParams) * sizeof(nrc_optimizer_entry);
+  if (e == cudaSuccess) e = cudaMemcpy(w, c->w16, size_t(kParams) * 2, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(w + size_t(kParams) * 2, c->use16, size_t(kParams) * 2, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return from_cuda(e);
+  const nrc_config& g = c->cfg;
+  std::memcpy(b, "NRCCKPT1", 8);
+  const uint32_t u[3] = {kCkptVersion, static_cast<uint32_t>(kParams), g.train_batch_size};
+  std::memcpy(b + 8, u, 12);
+  const float f[6] = {g.learning_rate, g.beta1, g.beta2, g.epsilon, g.ema_alpha, g.loss_scale};
+  std::memcpy(b + 20, f, 24);
+  std::memcpy(b + 44, &g.use_ema_weights, 4);
+  const uint64_t pb = kCkptPayload, h = fnv1a(pay, kCkptPayload);
+  std::memcpy(b + 48, &pb, 8);
+  std::memcpy(b + 56, &h, 8);
+  return NRC_OK;
+}
+
+int nrc_load_checkpoint(nrc_context* c, const void* blob, size_t bytes) {
+  int s = check_ctx(c);
+  if (s != NRC_OK) return s;
+  if (blob == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  if (bytes != nrc_checkpoint_bytes()) return NRC_ERROR_BAD_CHECKPOINT;
+  const uint8_t* b = static_cast<const uint8_t*>(blob);
+  uint32_t u[3];
+  uint64_t pb = 0, h = 0;
+  std::memcpy(u, b + 8, 12);
+  std::memcpy(&pb, b + 48, 8);
+  std::memcpy(&h, b + 56, 8);
+  const uint8_t* pay = b + kCkptHeader;
+  if (std::memcmp(b, "NRCCKPT1", 8) != 0 || u[0] != kCkptVersion || u[1] != static_cast<uint32_t>(kParams) ||
+      pb != kCkptPayload || fnv1a(pay, kCkptPayload) != h)
+    return NRC_ERROR_BAD_CHECKPOINT;
+  float f[6];
+  uint32_t use_ema = 0;
+  std::memcpy(f, b + 20, 24);
+  std::memcpy(&use_ema, b + 44, 4);
+  if (u[2] == 0 || !(f[5] != 0.0f)) return NRC_ERROR_BAD_CHECKPOINT;
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(c->state, pay, sizeof(nrc_optimizer_state), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(c->entries, pay + 32, size_t(kParams) * sizeof(nrc_optimizer_entry), cudaMemcpyHostToDevice);
+  const uint8_t* w = pay + 32 + size_t(kParams) * sizeof(nrc_optimizer_entry);
+  if (e == cudaSuccess) e = cudaMemcpy(c->w16, w, size_t(kParams) * 2, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(c->use16, w + size_t(kParams) * 2, size_t(kParams) * 2, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return from_cuda(e);
+  c->cfg.train_batch_size = u[2];
+  c->cfg.learning_rate = f[0];
+  c->cfg.beta1 = f[1];
+  c->cfg.beta2 = f[2];
+  c->cfg.epsilon = f[3];
+  c->cfg.ema_alpha = f[4];
+  c->cfg.loss_scale = f[5];
+  c->cfg.use_ema_weights = use_ema;
   return NRC_OK;
 }
 

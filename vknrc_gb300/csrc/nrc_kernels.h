@@ -131,6 +131,10 @@ cudaError_t launch_encode(const nrc_input* in, const uint32_t* d_count, uint32_t
                           int num_sms, cudaStream_t stream);
 cudaError_t launch_sph_encode(const float* dirs, const uint32_t* d_count, uint32_t capacity, float* out,
                               int num_sms, cudaStream_t stream);
+cudaError_t launch_unpack(const nrc_scene& scene, bool train, const void* in, const uint32_t* d_count,
+                          uint32_t capacity, void* out, uint32_t* out_dst, int num_sms, cudaStream_t stream);
+cudaError_t launch_screen(const float* color, float* accum, uint32_t width, uint32_t height, int acc_on,
+                          uint32_t acc_count, uint8_t* out8, float* outf, int num_sms, cudaStream_t stream);
 cudaError_t launch_fill_f32(float* p, float v, size_t n, cudaStream_t stream);
 
 }  // namespace nrc

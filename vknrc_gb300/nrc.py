@@ -22,7 +22,8 @@ TRAIN_BATCH_COUNT = 4
 WEIGHTS_USE, WEIGHTS_TRAIN = 0, 1
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "no CUDA device", 4: "unsupported device",
-          5: "out of device memory", 6: "device timeout", 7: "misaligned buffer", 8: "too large"}
+          5: "out of device memory", 6: "device timeout", 7: "misaligned buffer", 8: "too large",
+          9: "bad checkpoint"}
 
 EXPORTS = [
     "nrc_status_string", "nrc_default_config", "nrc_create", "nrc_destroy", "nrc_reset", "nrc_he_init_host",
@@ -32,7 +33,8 @@ EXPORTS = [
     "nrc_frame_scatter", "nrc_infer_many", "nrc_train_many", "nrc_plan_query_ctas", "nrc_plan_train_ctas",
     "nrc_server_create", "nrc_server_destroy", "nrc_server_open_session", "nrc_server_close_session",
     "nrc_server_frame_buffers", "nrc_server_session_cache", "nrc_server_submit", "nrc_server_wait",
-    "nrc_server_get_stats",
+    "nrc_server_get_stats", "nrc_screen", "nrc_checkpoint_bytes", "nrc_save_checkpoint", "nrc_load_checkpoint",
+    "nrc_unpack_eval", "nrc_unpack_train",
 ]
 
 
@@ -113,6 +115,16 @@ class ServerStats(ctypes.Structure):
                 ("mean_batch_sessions", ctypes.c_double)]
 
 
+class SceneStruct(ctypes.Structure):
+    """nrc_scene: device pointers of the scene buffers and their counts."""
+    _fields_ = [("vertices", ctypes.c_void_p), ("vertex_indices", ctypes.c_void_p), ("texcoords", ctypes.c_void_p),
+                ("texcoord_indices", ctypes.c_void_p), ("materials", ctypes.c_void_p),
+                ("material_ids", ctypes.c_void_p), ("transforms", ctypes.c_void_p), ("textures", ctypes.c_void_p),
+                ("vertex_count", ctypes.c_uint32), ("texcoord_count", ctypes.c_uint32),
+                ("material_count", ctypes.c_uint32), ("primitive_count", ctypes.c_uint32),
+                ("instance_count", ctypes.c_uint32), ("texture_count", ctypes.c_uint32)]
+
+
 _lib: Optional[ctypes.CDLL] = None
 
 
@@ -170,6 +182,13 @@ def lib(build_if_missing: bool = True) -> ctypes.CDLL:
     L.nrc_server_submit.argtypes = [vp, u32, u32, vp, ctypes.POINTER(u64)]
     L.nrc_server_wait.argtypes = [vp, u64, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]
     L.nrc_server_get_stats.argtypes = [vp, ctypes.POINTER(ServerStats), i32]
+    L.nrc_screen.argtypes = [vp, vp, u32, u32, i32, u32, vp, vp, vp]
+    L.nrc_unpack_eval.argtypes = [ctypes.POINTER(SceneStruct), vp, vp, u32, vp, vp, vp]
+    L.nrc_unpack_train.argtypes = [ctypes.POINTER(SceneStruct), vp, vp, u32, vp, vp]
+    L.nrc_checkpoint_bytes.restype = ctypes.c_size_t
+    L.nrc_checkpoint_bytes.argtypes = []
+    L.nrc_save_checkpoint.argtypes = [vp, vp, ctypes.c_size_t]
+    L.nrc_load_checkpoint.argtypes = [vp, vp, ctypes.c_size_t]
     _lib = L
     return L
 
@@ -324,6 +343,16 @@ class Cache:
 
     def error(self) -> int:
         return lib().nrc_get_error(self.h)
+
+    def save_checkpoint(self) -> bytes:
+        n = lib().nrc_checkpoint_bytes()
+        buf = ctypes.create_string_buffer(n)
+        check(lib().nrc_save_checkpoint(self.h, buf, n), "nrc_save_checkpoint")
+        return buf.raw
+
+    def load_checkpoint(self, blob: bytes) -> None:
+        buf = ctypes.create_string_buffer(blob, len(blob))
+        check(lib().nrc_load_checkpoint(self.h, buf, len(blob)), "nrc_load_checkpoint")
 
     def device_buffers(self):
         w, u, e, s = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
@@ -486,3 +515,50 @@ class Server:
         st = ServerStats()
         check(lib().nrc_server_get_stats(self.h, ctypes.byref(st), int(reset)), "nrc_server_get_stats")
         return {k: getattr(st, k) for k, _ in ServerStats._fields_}
+
+
+def screen(color, accumulate=None, accumulate_count=0, out_rgba8=None, out_rgba=None, stream=None) -> None:
+    """nrc_screen on (H, W, 4) float32 CUDA tensors; out_rgba8 is (H, W, 4) uint8."""
+    h, w = color.shape[0], color.shape[1]
+    check(lib().nrc_screen(_ptr(color), _ptr(accumulate), w, h, int(accumulate is not None), accumulate_count,
+                           _ptr(out_rgba8), _ptr(out_rgba), _stream(stream)), "nrc_screen")
+
+
+# ------------------------------------------------------------ scene unpack --
+class DeviceScene:
+    """A scene (the dict of numpy arrays that synthetic.scene makes) uploaded to
+    the GPU, with its nrc_scene description."""
+
+    def __init__(self, sc: dict):
+        import torch
+
+        def up(a):
+            return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+        self.keep = {k: up(v) for k, v in sc.items() if k != "textures"}
+        self.tex = [up(t) for t in sc["textures"]]
+        table = np.zeros((max(1, len(self.tex)), 2), np.uint64)
+        for i, t in enumerate(self.tex):
+            table[i, 0] = t.data_ptr()
+            table[i, 1] = np.uint64(t.shape[1]) | (np.uint64(t.shape[0]) << np.uint64(32))
+        self.table = up(table.view(np.int64))
+        k = self.keep
+        self.s = SceneStruct(k["vertices"].data_ptr(), k["vertex_indices"].data_ptr(), k["texcoords"].data_ptr(),
+                             k["texcoord_indices"].data_ptr(), k["materials"].data_ptr(), k["material_ids"].data_ptr(),
+                             k["transforms"].data_ptr(), self.table.data_ptr(), k["vertices"].shape[0],
+                             k["texcoords"].shape[0], k["materials"].shape[0], k["vertex_indices"].shape[0],
+                             k["transforms"].shape[0], len(self.tex))
+
+
+def unpack_eval(scene: DeviceScene, records, count, out_inputs, out_dst=None, capacity=None, stream=None) -> None:
+    """nrc_unpack_eval: records (n, 5) uint32/int32 CUDA tensor -> out_inputs (n, 14) float32, out_dst (n,)."""
+    cap = records.shape[0] if capacity is None else capacity
+    check(lib().nrc_unpack_eval(ctypes.byref(scene.s), _ptr(records), _ptr(count), cap, _ptr(out_inputs),
+                                _ptr(out_dst), _stream(stream)), "nrc_unpack_eval")
+
+
+def unpack_train(scene: DeviceScene, records, count, out_records, capacity=None, stream=None) -> None:
+    """nrc_unpack_train: records (n, 10) 32-bit words -> out_records (n, 20) float32."""
+    cap = records.shape[0] if capacity is None else capacity
+    check(lib().nrc_unpack_train(ctypes.byref(scene.s), _ptr(records), _ptr(count), cap, _ptr(out_records),
+                                 _stream(stream)), "nrc_unpack_train")

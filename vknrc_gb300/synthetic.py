@@ -109,3 +109,86 @@ def frame_destinations(rng: np.random.Generator, width: int, height: int, train_
             words.append(dst_train(np.full(len(ls), b), np.array(ls), np.array(rs)))
     d = np.concatenate(words)
     return d[rng.permutation(d.size)]
+
+
+# ------------------------------------------------------------------ scenes --
+def scene(rng: np.random.Generator, vertices: int = 300, primitives: int = 200, instances: int = 5,
+          materials: int = 12, texture_sizes=((5, 3), (64, 32), (1, 1), (17, 9))) -> dict:
+    """A seeded synthetic scene in the layout of the reference's scene buffers
+    (shader/src/Scene.glsl:8-48): vertices, per-primitive vertex / texcoord
+    index triples, texcoords (spanning several texture periods, negative ones
+    included, to exercise REPEAT addressing), std430 materials (some textured,
+    some constant, a few with texture ids past the table), per-primitive
+    material ids, mat3x4 instance transforms and rgba8 sRGB textures."""
+    sc = {}
+    sc["vertices"] = rng.uniform(-1, 1, (vertices, 3)).astype(np.float32)
+    # three distinct vertices per primitive (a degenerate triangle has no normal)
+    sc["vertex_indices"] = rng.random((primitives, vertices)).argsort(axis=1)[:, :3].astype(np.uint32)
+    n_tc = vertices // 2
+    sc["texcoords"] = rng.uniform(-2, 3, (n_tc, 2)).astype(np.float32)
+    sc["texcoord_indices"] = rng.integers(0, n_tc, (primitives, 3)).astype(np.uint32)
+    mats = np.zeros((materials, 16), np.float32)
+    ids = mats.view(np.uint32)
+    mats[:, 0:3] = rng.uniform(0, 1, (materials, 3))
+    mats[:, 4:7] = rng.uniform(0, 1, (materials, 3))
+    mats[:, 8:11] = rng.uniform(0, 1, (materials, 3))
+    mats[:, 12] = rng.uniform(0, 1, materials)  # metallic
+    mats[:, 13] = rng.uniform(0, 1, materials)  # roughness
+    mats[:, 14] = 1.5                          # ior
+    nt = len(texture_sizes)
+    choice = rng.integers(-1, nt + 1, (materials, 3))  # -1: constant; nt: past the table
+    for col, word in ((0, 3), (1, 7), (2, 11)):
+        ids[:, word] = np.where(choice[:, col] < 0, 0xFFFFFFFF, choice[:, col]).astype(np.uint32)
+    sc["materials"] = mats
+    sc["material_ids"] = rng.integers(0, materials, primitives).astype(np.uint32)
+    t = np.zeros((instances, 3, 4), np.float32)
+    for i in range(instances):
+        q, _ = np.linalg.qr(rng.standard_normal((3, 3)))
+        m = q * rng.uniform(0.5, 2.0)
+        t[i, :, :3] = m
+        t[i, :, 3] = rng.uniform(-3, 3, 3)
+    sc["transforms"] = t
+    sc["textures"] = [rng.integers(0, 256, (h, w, 4), dtype=np.uint8) for (w, h) in texture_sizes]
+    return sc
+
+
+def packed_inputs(rng: np.random.Generator, sc: dict, n: int, bad_fraction: float = 0.0) -> np.ndarray:
+    """(n, 4) uint32 PackedNRCInput words (NRCRecord.glsl:6-9): primitive id,
+    flip bit | instance id, barycentrics and sphere-encoded direction as unorm16
+    pairs. A fraction of records carries out-of-range ids."""
+    p = sc["vertex_indices"].shape[0]
+    inst = sc["transforms"].shape[0]
+    out = np.empty((n, 4), np.uint32)
+    out[:, 0] = rng.integers(0, p, n)
+    out[:, 1] = rng.integers(0, inst, n).astype(np.uint32) | (rng.integers(0, 2, n).astype(np.uint32) << 31)
+    b = rng.uniform(0, 1, (n, 2))
+    over = b.sum(1) > 1
+    b[over] = 1 - b[over]
+    bq = np.round(b * 65535).astype(np.uint32)
+    out[:, 2] = bq[:, 0] | (bq[:, 1] << 16)
+    d = np.round(sph_encode(sphere(rng, n)) * 65535).astype(np.uint32)
+    out[:, 3] = d[:, 0] | (d[:, 1] << 16)
+    if bad_fraction > 0:
+        bad = rng.random(n) < bad_fraction
+        half = rng.random(n) < 0.5
+        out[bad & half, 0] = p + rng.integers(0, 10, int(np.sum(bad & half)))
+        out[bad & ~half, 1] = (inst + rng.integers(0, 10, int(np.sum(bad & ~half)))).astype(np.uint32)
+    return out
+
+
+def eval_records(rng: np.random.Generator, sc: dict, n: int, bad_fraction: float = 0.0) -> np.ndarray:
+    """(n, 5) uint32 NRCEvalRecord words: dst, then the packed input."""
+    r = np.empty((n, 5), np.uint32)
+    r[:, 0] = rng.integers(0, 2**32, n, dtype=np.uint64).astype(np.uint32)
+    r[:, 1:] = packed_inputs(rng, sc, n, bad_fraction)
+    return r
+
+
+def packed_train_records(rng: np.random.Generator, sc: dict, n: int) -> np.ndarray:
+    """(n, 10) 32-bit words of NRCTrainRecord: bias rgb, factor rgb (float32), packed input."""
+    r = np.empty((n, 10), np.uint32)
+    f = r.view(np.float32)
+    f[:, 0:3] = rng.lognormal(0, 1, (n, 3))
+    f[:, 3:6] = rng.uniform(0, 1, (n, 3))
+    r[:, 6:] = packed_inputs(rng, sc, n)
+    return r
