@@ -377,6 +377,40 @@ def batched_leg(evals, trains, steps=50):
     }
 
 
+# ------------------------------------------------------------ precision leg --
+def precision_leg(evals, trains, eval_cnt, train_cnt, steps=500):
+    """The same 1080p frame with a BF16 cache (bf16 weights, features,
+    activations and gradients; fp32 master weights and moments)."""
+    import torch
+
+    from vknrc_gb300 import Cache
+
+    out = torch.empty((Q, 3), dtype=torch.float32, device="cuda")
+    with Cache(seed=1234, learning_rate=1e-3, beta2=0.99, precision=1) as c:
+        for k in range(5):
+            c.frame(evals[k % len(evals)], eval_cnt, out, trains[k % len(trains)], train_cnt)
+        s, m, e = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        ms_inf = []
+        s.record()
+        for k in range(steps):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record()
+            c.infer(evals[k % len(evals)], eval_cnt, out)
+            b.record()
+            c.train_batches(trains[k % len(trains)], train_cnt, write_use_last=True)
+            ms_inf.append((a, b))
+        e.record()
+        torch.cuda.synchronize()
+        if c.error() != 0:
+            raise RuntimeError("device error in the bf16 leg")
+        frame_s = s.elapsed_time(e) / 1e3 / steps
+        inf_s = statistics.mean(a.elapsed_time(b) for a, b in ms_inf) / 1e3
+    return {"ms_per_frame": frame_s * 1e3, "queries_per_s": Q / frame_s, "train_records_per_s": B * R / frame_s,
+            "infer_ms": inf_s * 1e3, "steps": steps,
+            "accuracy": "tests/test_gpu_precision.py: query error and 1000-step loss against the FP64 oracle"}
+
+
 # --------------------------------------------------------------- serving leg --
 SERVE_RES = [(1280, 720), (1920, 1080), (2560, 1440)]
 
@@ -611,6 +645,8 @@ def ours_arm(args, world, rank, local):
     if plain is not None:
         result["plain_fp16"] = {"queries_per_s": plain, "what": "nrc_encode + 6 torch fp16 GEMMs (cuBLAS), infer only",
                                 "fused_infer_queries_per_s": Q / infer_s}
+    if rank == 0 and world == 1 and not args.no_batched:
+        result["precision"] = {"bf16": precision_leg(evals, trains, eval_cnt, train_cnt)}
     if rank == 0 and world == 1 and not args.no_batched:
         result["batched"] = batched_leg(evals, trains)
     if rank == 0 and world == 1 and not args.no_serving:

@@ -92,7 +92,18 @@ typedef struct nrc_config {
                                order, so results are run-to-run identical either way */
   uint32_t track_loss;      /* 1: accumulate the relative-L2 loss (check path, FP64 sum) */
   uint64_t seed;            /* He initialisation seed */
+  uint32_t precision;       /* nrc_precision: the 16-bit format of weights and operands */
 } nrc_config;
+
+/* Precision forms. FP16 is the reference's (fp16 weights, features and
+ * activations, fp32 accumulation). BF16 keeps the same fp32 master weights and
+ * Adam moments but stores the weight vectors and runs every operand (features,
+ * activations, gradients) in bf16: a wider range (no fp16 overflow of the
+ * relative-L2 gradient) for 3 fewer mantissa bits. For a BF16 context the
+ * 16-bit vectors of nrc_get_weights / nrc_set_weights / nrc_get_device_buffers
+ * hold bf16 bit patterns, and the fp16-feature calls (nrc_encode,
+ * nrc_infer_encoded) return NRC_ERROR_INVALID_ARGUMENT. */
+typedef enum nrc_precision { NRC_PRECISION_FP16 = 0, NRC_PRECISION_BF16 = 1 } nrc_precision;
 
 typedef enum nrc_status {
   NRC_OK = 0,
@@ -292,7 +303,8 @@ NRC_API int nrc_infer_many(const nrc_query_job* jobs, uint32_t njobs, const uint
 NRC_API int nrc_train_many(const nrc_train_job* jobs, uint32_t njobs, const uint32_t* ctas, void* stream);
 
 /* CTA split that nrc_infer_many / nrc_train_many use when `ctas` is NULL, for
- * one launch of at most 32 jobs: writes njobs entries to out_ctas. */
+ * one launch of at most 32 jobs of one precision: writes njobs entries to
+ * out_ctas. (A batched call runs FP16 and BF16 contexts in separate launches.) */
 NRC_API int nrc_plan_query_ctas(const nrc_query_job* jobs, uint32_t njobs, uint32_t* out_ctas);
 NRC_API int nrc_plan_train_ctas(const nrc_train_job* jobs, uint32_t njobs, uint32_t* out_ctas);
 

@@ -27,6 +27,27 @@ float oracle_f16_to_f32(uint16_t b) {
   return (float)h;
 }
 
+/* bf16: the upper half of an fp32, rounded to nearest even (NaN kept quiet). */
+uint16_t oracle_f32_to_bf16(float x) {
+  uint32_t u;
+  memcpy(&u, &x, 4);
+  if ((u & 0x7FFFFFFFu) > 0x7F800000u) return (uint16_t)((u >> 16) | 0x40u);
+  u += 0x7FFFu + ((u >> 16) & 1u);
+  return (uint16_t)(u >> 16);
+}
+
+float oracle_bf16_to_f32(uint16_t b) {
+  const uint32_t u = (uint32_t)b << 16;
+  float x;
+  memcpy(&x, &u, 4);
+  return x;
+}
+
+/* The 16-bit storage format of a precision form: 0 fp16 (the reference's), 1 bf16. */
+static inline uint16_t to16(float x, int fmt) { return fmt ? oracle_f32_to_bf16(x) : oracle_f32_to_f16(x); }
+static inline float from16(uint16_t b, int fmt) { return fmt ? oracle_bf16_to_f32(b) : oracle_f16_to_f32(b); }
+static inline float round16(float x, int fmt) { return from16(to16(x, fmt), fmt); }
+
 /* ------------------------------------------------------------- exp -- */
 /* e^x by Cody & Waite argument reduction (x = k ln2 + r, ln2 split into a
  * 16-bit-exact high part and a low correction) and the degree-7 Taylor
@@ -101,7 +122,7 @@ static inline void oneblob4(float x, float* o) {
  *   [0,12) pos.x freq 2^0..2^11, [12,24) pos.y, [24,36) pos.z,
  *   [36,40) ob(dir.u), [40,44) ob(dir.v), [44,48) ob(normal.u), [48,52) ob(normal.v),
  *   [52,56) ob(1 - e^-roughness), [56,59) diffuse, [59,62) specular, 62, 63 = 1. */
-void oracle_encode(const float* records, int64_t n, uint16_t* enc) {
+void oracle_encode_fmt(const float* records, int64_t n, uint16_t* enc, int fmt) {
   for (int64_t i = 0; i < n; ++i) {
     const float* r = records + ORACLE_IN_FLOATS * i;
     float f[64];
@@ -117,9 +138,11 @@ void oracle_encode(const float* records, int64_t n, uint16_t* enc) {
     for (int c = 0; c < 6; ++c) f[56 + c] = r[8 + c];
     f[62] = 1.0f;
     f[63] = 1.0f;
-    for (int c = 0; c < 64; ++c) enc[64 * i + c] = oracle_f32_to_f16(f[c]);
+    for (int c = 0; c < 64; ++c) enc[64 * i + c] = to16(f[c], fmt);
   }
 }
+
+void oracle_encode(const float* records, int64_t n, uint16_t* enc) { oracle_encode_fmt(records, n, enc, 0); }
 
 /* ----------------------------------------------------------- threads -- */
 typedef void (*range_fn)(void* ctx, int64_t begin, int64_t end, int tid);
@@ -164,19 +187,21 @@ typedef struct {
   float w5t[64][3];
   double wtd[5][64][64];
   double w5td[64][3];
+  int fmt; /* 16-bit format of weights, inputs and stored activations/gradients */
 } wcache;
 
-static void load_weights(const uint16_t* w, wcache* c) {
+static void load_weights(const uint16_t* w, wcache* c, int fmt) {
+  c->fmt = fmt;
   for (int l = 0; l < 5; ++l)
     for (int o = 0; o < 64; ++o)
       for (int i = 0; i < 64; ++i) {
-        const float v = oracle_f16_to_f32(w[l * 4096 + o * 64 + i]);
+        const float v = from16(w[l * 4096 + o * 64 + i], fmt);
         c->wt[l][i][o] = v;
         c->wtd[l][i][o] = v;
       }
   for (int o = 0; o < 3; ++o)
     for (int i = 0; i < 64; ++i) {
-      const float v = oracle_f16_to_f32(w[5 * 4096 + o * 64 + i]);
+      const float v = from16(w[5 * 4096 + o * 64 + i], fmt);
       c->w5t[i][o] = v;
       c->w5td[i][o] = v;
     }
@@ -185,7 +210,7 @@ static void load_weights(const uint16_t* w, wcache* c) {
 /* One record forward, fp16 activations, fp32 sums. acts[l] receives the input of
  * layer l (l = 0..5), out the three fp32 outputs (no clamp). */
 static void fwd_f32(const wcache* c, const uint16_t* e, float acts[6][64], float out[3]) {
-  for (int i = 0; i < 64; ++i) acts[0][i] = oracle_f16_to_f32(e[i]);
+  for (int i = 0; i < 64; ++i) acts[0][i] = from16(e[i], c->fmt);
   for (int l = 0; l < 5; ++l) {
     float z[64];
     for (int o = 0; o < 64; ++o) z[o] = 0.0f;
@@ -193,7 +218,7 @@ static void fwd_f32(const wcache* c, const uint16_t* e, float acts[6][64], float
       const float a = acts[l][i];
       for (int o = 0; o < 64; ++o) z[o] += c->wt[l][i][o] * a;
     }
-    for (int o = 0; o < 64; ++o) acts[l + 1][o] = oracle_f16_to_f32(oracle_f32_to_f16(z[o] > 0.0f ? z[o] : 0.0f));
+    for (int o = 0; o < 64; ++o) acts[l + 1][o] = round16(z[o] > 0.0f ? z[o] : 0.0f, c->fmt);
   }
   out[0] = out[1] = out[2] = 0.0f;
   for (int i = 0; i < 64; ++i)
@@ -201,7 +226,7 @@ static void fwd_f32(const wcache* c, const uint16_t* e, float acts[6][64], float
 }
 
 static void fwd_f64(const wcache* c, const uint16_t* e, double acts[6][64], double out[3]) {
-  for (int i = 0; i < 64; ++i) acts[0][i] = oracle_f16_to_f32(e[i]);
+  for (int i = 0; i < 64; ++i) acts[0][i] = from16(e[i], c->fmt);
   for (int l = 0; l < 5; ++l) {
     double z[64];
     for (int o = 0; o < 64; ++o) z[o] = 0.0;
@@ -237,20 +262,28 @@ static void fwd64_range(void* p, int64_t b, int64_t e, int tid) {
   for (int64_t i = b; i < e; ++i) fwd_f64(x->c, x->enc + 64 * i, acts, x->out64 + 3 * i);
 }
 
-void oracle_forward_f32(const uint16_t* w, const uint16_t* enc, int64_t n, float* out, int nthreads) {
+void oracle_forward_f32_fmt(const uint16_t* w, const uint16_t* enc, int64_t n, float* out, int nthreads, int fmt) {
   wcache* c = (wcache*)malloc(sizeof(wcache));
-  load_weights(w, c);
+  load_weights(w, c, fmt);
   fwd_ctx x = {c, enc, out, NULL};
   parallel_for(n, nthreads, fwd32_range, &x);
   free(c);
 }
 
-void oracle_forward_f64(const uint16_t* w, const uint16_t* enc, int64_t n, double* out, int nthreads) {
+void oracle_forward_f32(const uint16_t* w, const uint16_t* enc, int64_t n, float* out, int nthreads) {
+  oracle_forward_f32_fmt(w, enc, n, out, nthreads, 0);
+}
+
+void oracle_forward_f64_fmt(const uint16_t* w, const uint16_t* enc, int64_t n, double* out, int nthreads, int fmt) {
   wcache* c = (wcache*)malloc(sizeof(wcache));
-  load_weights(w, c);
+  load_weights(w, c, fmt);
   fwd_ctx x = {c, enc, NULL, out};
   parallel_for(n, nthreads, fwd64_range, &x);
   free(c);
+}
+
+void oracle_forward_f64(const uint16_t* w, const uint16_t* enc, int64_t n, double* out, int nthreads) {
+  oracle_forward_f64_fmt(w, enc, n, out, nthreads, 0);
 }
 
 /* ------------------------------------------------------------ train -- */
@@ -304,7 +337,7 @@ static void train_range(void* p, int64_t b, int64_t e, int tid) {
       loss_grad_f32(o32, t, x->loss_scale, d);
       for (int k = 0; k < 3; ++k) {
         out[k] = o32[k];
-        g[k] = oracle_f16_to_f32(oracle_f32_to_f16(d[k])); /* packed to fp16, NN_nv.glsl:185-186 */
+        g[k] = round16(d[k], c->fmt); /* packed to 16 bits, NN_nv.glsl:185-186 */
       }
     } else {
       fwd_f64(c, x->enc + 64 * r, acts, out);
@@ -326,7 +359,7 @@ static void train_range(void* p, int64_t b, int64_t e, int tid) {
       for (int k = 0; k < 3; ++k) s += g[k] * c->w5td[i][k];
       /* ReLU mask; NaN sums are zeroed as the reference's NaN-mask trick does (NN_nv.glsl:240-243) */
       gn[i] = (acts[5][i] > 0.0 && s == s) ? s : 0.0;
-      if (x->mode == 0) gn[i] = oracle_f16_to_f32(oracle_f32_to_f16((float)gn[i]));
+      if (x->mode == 0) gn[i] = round16((float)gn[i], c->fmt);
     }
     for (int l = 4; l >= 0; --l) {
       for (int o = 0; o < 64; ++o) g[o] = gn[o];
@@ -341,7 +374,7 @@ static void train_range(void* p, int64_t b, int64_t e, int tid) {
         double s = 0.0;
         for (int o = 0; o < 64; ++o) s += g[o] * c->wtd[l][i][o];
         gn[i] = (acts[l][i] > 0.0 && s == s) ? s : 0.0; /* NN_nv.glsl:272-277 */
-        if (x->mode == 0) gn[i] = oracle_f16_to_f32(oracle_f32_to_f16((float)gn[i]));
+        if (x->mode == 0) gn[i] = round16((float)gn[i], c->fmt);
       }
     }
   }
@@ -386,13 +419,19 @@ static void train_grad_cached(const wcache* c, const uint16_t* enc, const float*
   free(x);
 }
 
+void oracle_train_grad_fmt(const uint16_t* w, const uint16_t* enc, const float* target, int64_t n,
+                           float loss_scale, int mode, double* grad, double* grad_abs, double* loss_sum,
+                           int nthreads, int fmt) {
+  wcache* c = (wcache*)malloc(sizeof(wcache));
+  load_weights(w, c, fmt);
+  train_grad_cached(c, enc, target, n, loss_scale, mode, grad, grad_abs, loss_sum, nthreads);
+  free(c);
+}
+
 void oracle_train_grad(const uint16_t* w, const uint16_t* enc, const float* target, int64_t n,
                        float loss_scale, int mode, double* grad, double* grad_abs, double* loss_sum,
                        int nthreads) {
-  wcache* c = (wcache*)malloc(sizeof(wcache));
-  load_weights(w, c);
-  train_grad_cached(c, enc, target, n, loss_scale, mode, grad, grad_abs, loss_sum, nthreads);
-  free(c);
+  oracle_train_grad_fmt(w, enc, target, n, loss_scale, mode, grad, grad_abs, loss_sum, nthreads, 0);
 }
 
 /* The FP64 oracle's training loop keeps its weights in FP64: the same gradient
@@ -401,6 +440,7 @@ void oracle_train_grad(const uint16_t* w, const uint16_t* enc, const float* targ
 void oracle_train_grad_w64(const double* w, const uint16_t* enc, const float* target, int64_t n,
                            float loss_scale, double* grad, double* loss_sum, int nthreads) {
   wcache* c = (wcache*)malloc(sizeof(wcache));
+  c->fmt = 0; /* inputs are fp16 features */
   for (int l = 0; l < 5; ++l)
     for (int o = 0; o < 64; ++o)
       for (int i = 0; i < 64; ++i) {
@@ -431,8 +471,8 @@ uint32_t oracle_prepare(uint32_t count, const oracle_hparams* hp, oracle_opt_sta
 
 /* nrc_optimize.comp:32-54, with its EMA formula kept as written:
  * ema = (1 - a)/eta_t * w + a * eta_{t-1} * ema, eta_t = 1 - a^t. */
-void oracle_adam(float* entries, const float* grad, uint32_t count, const oracle_opt_state* st,
-                 const oracle_hparams* hp, uint16_t* w16, uint16_t* use16, int use_ema) {
+void oracle_adam_fmt(float* entries, const float* grad, uint32_t count, const oracle_opt_state* st,
+                     const oracle_hparams* hp, uint16_t* w16, uint16_t* use16, int use_ema, int fmt) {
   if (count == 0) return;
   const float b1 = hp->beta1, b2 = hp->beta2;
   const float omb1 = 1.0f - b1, omb2 = 1.0f - b2;
@@ -453,9 +493,14 @@ void oracle_adam(float* entries, const float* grad, uint32_t count, const oracle
     e[1] = v;
     e[2] = w;
     e[3] = ema;
-    w16[i] = oracle_f32_to_f16(w);
-    if (use16) use16[i] = oracle_f32_to_f16(use_ema ? ema : w);
+    w16[i] = to16(w, fmt);
+    if (use16) use16[i] = to16(use_ema ? ema : w, fmt);
   }
+}
+
+void oracle_adam(float* entries, const float* grad, uint32_t count, const oracle_opt_state* st,
+                 const oracle_hparams* hp, uint16_t* w16, uint16_t* use16, int use_ema) {
+  oracle_adam_fmt(entries, grad, count, st, hp, w16, use16, use_ema, 0);
 }
 
 /* ------------------------------------------------ query destinations -- */

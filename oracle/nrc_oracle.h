@@ -83,9 +83,22 @@ uint32_t oracle_prepare(uint32_t count, const oracle_hparams* hp, oracle_opt_sta
  * fp16 of (use_ema ? ema : w). No-op when count == 0. */
 void oracle_adam(float* entries, const float* grad, uint32_t count, const oracle_opt_state* st,
                  const oracle_hparams* hp, uint16_t* w16, uint16_t* use16, int use_ema);
+void oracle_adam_fmt(float* entries, const float* grad, uint32_t count, const oracle_opt_state* st,
+                     const oracle_hparams* hp, uint16_t* w16, uint16_t* use16, int use_ema, int fmt);
 
 void oracle_scatter(const float* pred, const uint32_t* dst, int64_t n, float* bias_factor_r, const float* factor_gb,
                     uint32_t width, uint32_t height, float* const* train, const uint32_t* train_cap);
+
+/* Precision forms: the same computations with every 16-bit quantity (weights,
+ * encoded features, stored activations and gradients, the fp16 weight copies
+ * Adam writes) in format fmt: 0 fp16 (the reference's), 1 bf16. */
+uint16_t oracle_f32_to_bf16(float x);
+float oracle_bf16_to_f32(uint16_t b);
+void oracle_encode_fmt(const float* records, int64_t n, uint16_t* enc, int fmt);
+void oracle_forward_f32_fmt(const uint16_t* w, const uint16_t* enc, int64_t n, float* out, int nthreads, int fmt);
+void oracle_forward_f64_fmt(const uint16_t* w, const uint16_t* enc, int64_t n, double* out, int nthreads, int fmt);
+void oracle_train_grad_fmt(const uint16_t* w, const uint16_t* enc, const float* target, int64_t n, float loss_scale,
+                           int mode, double* grad, double* grad_abs, double* loss_sum, int nthreads, int fmt);
 
 /* Scene buffers for oracle_unpack, the host mirror of nrc_scene (include/nrc.h);
  * pointers are host pointers. */

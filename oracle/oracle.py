@@ -33,6 +33,11 @@ def lib() -> ctypes.CDLL:
         _lib = ctypes.CDLL(LIB_PATH)
         vp, i64, i32, f32 = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_float
         _lib.oracle_encode.argtypes = [vp, i64, vp]
+        _lib.oracle_encode_fmt.argtypes = [vp, i64, vp, i32]
+        _lib.oracle_forward_f32_fmt.argtypes = [vp, vp, i64, vp, i32, i32]
+        _lib.oracle_forward_f64_fmt.argtypes = [vp, vp, i64, vp, i32, i32]
+        _lib.oracle_train_grad_fmt.argtypes = [vp, vp, vp, i64, f32, i32, vp, vp, vp, i32, i32]
+        _lib.oracle_adam_fmt.argtypes = [vp, vp, ctypes.c_uint32, vp, vp, vp, vp, i32, i32]
         _lib.oracle_sph_encode.argtypes = [vp, i64, vp]
         _lib.oracle_forward_f32.argtypes = [vp, vp, i64, vp, i32]
         _lib.oracle_forward_f64.argtypes = [vp, vp, i64, vp, i32]
@@ -70,11 +75,11 @@ def _c(a, dtype):
     return np.ascontiguousarray(a, dtype=dtype)
 
 
-def encode(records: np.ndarray) -> np.ndarray:
-    """records (n, 14) float32 -> (n, 64) uint16 fp16 bit patterns."""
+def encode(records: np.ndarray, fmt: int = 0) -> np.ndarray:
+    """records (n, 14) float32 -> (n, 64) uint16 bit patterns: fp16 (fmt 0) or bf16 (fmt 1)."""
     r = _c(records, np.float32).reshape(-1, 14)
     out = np.empty((r.shape[0], 64), np.uint16)
-    lib().oracle_encode(_p(r), r.shape[0], _p(out))
+    lib().oracle_encode_fmt(_p(r), r.shape[0], _p(out), fmt)
     return out
 
 
@@ -89,32 +94,33 @@ def expf(x: float) -> float:
     return lib().oracle_expf(x)
 
 
-def forward_f32(weights: np.ndarray, enc: np.ndarray, nthreads: int = 1) -> np.ndarray:
+def forward_f32(weights: np.ndarray, enc: np.ndarray, nthreads: int = 1, fmt: int = 0) -> np.ndarray:
     w = _c(weights, np.uint16)
     e = _c(enc, np.uint16).reshape(-1, 64)
     out = np.empty((e.shape[0], 3), np.float32)
-    lib().oracle_forward_f32(_p(w), _p(e), e.shape[0], _p(out), nthreads)
+    lib().oracle_forward_f32_fmt(_p(w), _p(e), e.shape[0], _p(out), nthreads, fmt)
     return out
 
 
-def forward_f64(weights: np.ndarray, enc: np.ndarray, nthreads: int = 1) -> np.ndarray:
+def forward_f64(weights: np.ndarray, enc: np.ndarray, nthreads: int = 1, fmt: int = 0) -> np.ndarray:
     w = _c(weights, np.uint16)
     e = _c(enc, np.uint16).reshape(-1, 64)
     out = np.empty((e.shape[0], 3), np.float64)
-    lib().oracle_forward_f64(_p(w), _p(e), e.shape[0], _p(out), nthreads)
+    lib().oracle_forward_f64_fmt(_p(w), _p(e), e.shape[0], _p(out), nthreads, fmt)
     return out
 
 
-def train_grad(weights, enc, target, loss_scale=1.0, mode=0, nthreads=1, want_abs=False):
-    """Returns (grad[P] float64 sum over records, grad_abs or None, loss_sum)."""
+def train_grad(weights, enc, target, loss_scale=1.0, mode=0, nthreads=1, want_abs=False, fmt=0):
+    """Returns (grad[P] float64 sum over records, grad_abs or None, loss_sum).
+    fmt: 16-bit format of weights, features and stored activations (0 fp16, 1 bf16)."""
     w = _c(weights, np.uint16)
     e = _c(enc, np.uint16).reshape(-1, 64)
     t = _c(target, np.float32).reshape(-1, 3)
     g = np.zeros(P, np.float64)
     a = np.zeros(P, np.float64) if want_abs else None
     loss = ctypes.c_double(0.0)
-    lib().oracle_train_grad(_p(w), _p(e), _p(t), e.shape[0], loss_scale, mode, _p(g),
-                            _p(a) if a is not None else None, ctypes.byref(loss), nthreads)
+    lib().oracle_train_grad_fmt(_p(w), _p(e), _p(t), e.shape[0], loss_scale, mode, _p(g),
+                                _p(a) if a is not None else None, ctypes.byref(loss), nthreads, fmt)
     return g, a, loss.value
 
 
@@ -226,12 +232,12 @@ class Optimizer:
     def prepare(self, count: int) -> int:
         return lib().oracle_prepare(count, ctypes.byref(self.hp), ctypes.byref(self.state))
 
-    def adam(self, grad32: np.ndarray, count: int, write_use: bool = True, use_ema: bool = False):
+    def adam(self, grad32: np.ndarray, count: int, write_use: bool = True, use_ema: bool = False, fmt: int = 0):
         g = _c(grad32, np.float32)
         w16 = np.zeros(P, np.uint16)
         use16 = np.zeros(P, np.uint16) if write_use else None
-        lib().oracle_adam(_p(self.entries), _p(g), count, ctypes.byref(self.state), ctypes.byref(self.hp),
-                          _p(w16), _p(use16) if use16 is not None else None, int(use_ema))
+        lib().oracle_adam_fmt(_p(self.entries), _p(g), count, ctypes.byref(self.state), ctypes.byref(self.hp),
+                              _p(w16), _p(use16) if use16 is not None else None, int(use_ema), fmt)
         return w16, use16
 
 

@@ -14,6 +14,7 @@
 
 struct nrc_context {
   nrc_config cfg;
+  bool bf16 = false;  // precision form: 16-bit vectors and operands in bf16
   int device = 0;
   int num_sms = 0;
   void* block = nullptr;  // one device allocation, carved below
@@ -94,14 +95,24 @@ void he_init(uint64_t seed, float* w) {
   for (int i = 0; i < kParams; ++i) w[i] = norm(rng);
 }
 
-uint16_t f32_to_f16_bits(float x) {
-  const __half h = __float2half_rn(x);
+uint16_t f32_to_16_bits(float x, bool bf16) {
   uint16_t b;
-  std::memcpy(&b, &h, 2);
+  if (bf16) {
+    const __nv_bfloat16 h = __float2bfloat16_rn(x);
+    std::memcpy(&b, &h, 2);
+  } else {
+    const __half h = __float2half_rn(x);
+    std::memcpy(&b, &h, 2);
+  }
   return b;
 }
 
-float f16_bits_to_f32(uint16_t b) {
+float bits16_to_f32(uint16_t b, bool bf16) {
+  if (bf16) {
+    __nv_bfloat16 h;
+    std::memcpy(&h, &b, 2);
+    return __bfloat162float(h);
+  }
   __half h;
   std::memcpy(&h, &b, 2);
   return __half2float(h);
@@ -113,7 +124,7 @@ int upload_init(nrc_context* c, uint64_t seed) {
   std::vector<uint16_t> w16(kParams);
   std::vector<nrc_optimizer_entry> ent(kParams);
   for (int i = 0; i < kParams; ++i) {
-    w16[i] = f32_to_f16_bits(w[i]);
+    w16[i] = f32_to_16_bits(w[i], c->bf16);
     ent[i] = nrc_optimizer_entry{0.0f, 0.0f, w[i], w[i]};
   }
   const nrc_optimizer_state st{0u, 1.0f, 1.0f, 1.0f, 0.0f};
@@ -184,7 +195,8 @@ int nrc_create(const nrc_config* cfg_in, nrc_context** out) {
   nrc_config cfg;
   if (cfg_in) cfg = *cfg_in;
   else nrc_default_config(&cfg);
-  if (cfg.train_batch_size == 0 || !(cfg.learning_rate >= 0.0f) || !(cfg.loss_scale != 0.0f))
+  if (cfg.train_batch_size == 0 || !(cfg.learning_rate >= 0.0f) || !(cfg.loss_scale != 0.0f) ||
+      (cfg.precision != NRC_PRECISION_FP16 && cfg.precision != NRC_PRECISION_BF16))
     return NRC_ERROR_INVALID_ARGUMENT;
   int dev = 0, count = 0;
   cudaError_t e = cudaGetDeviceCount(&count);
@@ -199,6 +211,7 @@ int nrc_create(const nrc_config* cfg_in, nrc_context** out) {
   nrc_context* c = new (std::nothrow) nrc_context();
   if (c == nullptr) return NRC_ERROR_OUT_OF_MEMORY;
   c->cfg = cfg;
+  c->bf16 = cfg.precision == NRC_PRECISION_BF16;
   c->device = dev;
   c->num_sms = prop.multiProcessorCount;
   const size_t o_w16 = 0;
@@ -272,6 +285,7 @@ int nrc_encode(nrc_context* c, const nrc_input* in, const uint32_t* d_count, uin
   if (capacity == 0) return NRC_OK;
   if (in == nullptr || d_count == nullptr || out == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
   if (!aligned16(in) || !aligned16(out)) return NRC_ERROR_MISALIGNED;
+  if (c->bf16) return NRC_ERROR_INVALID_ARGUMENT;  // the stand-alone encoding writes fp16 features
   return from_cuda(nrc::launch_encode(in, d_count, capacity, out, c->num_sms, static_cast<cudaStream_t>(stream)));
 }
 
@@ -306,7 +320,7 @@ int nrc_infer(nrc_context* c, const nrc_input* in, const uint32_t* d_count, uint
   q.out = out;
   q.clamp = 1;
   return from_cuda(nrc::launch_infer(in, false, d_count, capacity, weight_map_of(c, weight_set), q, c->err,
-                                     c->num_sms, static_cast<cudaStream_t>(stream)));
+                                     c->num_sms, static_cast<cudaStream_t>(stream), c->bf16));
 }
 
 // Checks a destination set and copies it into the kernel's output description.
@@ -346,7 +360,7 @@ int nrc_infer_scatter(nrc_context* c, const nrc_input* in, const uint32_t* d_dst
   q.clamp = 1;
   q.dst = d_dst;
   return from_cuda(nrc::launch_infer(in, false, d_count, capacity, weight_map_of(c, weight_set), q, c->err,
-                                     c->num_sms, static_cast<cudaStream_t>(stream)));
+                                     c->num_sms, static_cast<cudaStream_t>(stream), c->bf16));
 }
 
 int nrc_infer_encoded(nrc_context* c, const uint16_t* enc, const uint32_t* d_count, uint32_t capacity, float* out,
@@ -360,6 +374,7 @@ int nrc_infer_encoded(nrc_context* c, const uint16_t* enc, const uint32_t* d_cou
   nrc::QueryOut q = {};
   q.out = out;
   q.clamp = 0;
+  if (c->bf16) return NRC_ERROR_INVALID_ARGUMENT;  // pre-encoded inputs are fp16 features
   return from_cuda(nrc::launch_infer(enc, true, d_count, capacity, weight_map_of(c, weight_set), q, c->err,
                                      c->num_sms, static_cast<cudaStream_t>(stream)));
 }
@@ -386,6 +401,7 @@ static nrc::TrainParams train_params(nrc_context* c, int steps, int mode) {
   p.loss_acc = (g.track_loss && mode == nrc::kTrainStep) ? c->loss_acc : nullptr;
   p.loss_count = (g.track_loss && mode == nrc::kTrainStep) ? c->loss_count : nullptr;
   p.err = c->err;
+  p.bf16 = c->bf16 ? 1 : 0;
   return p;
 }
 
@@ -569,6 +585,38 @@ void plan_train(const nrc_train_job* jobs, uint32_t n, int sms, uint32_t* out) {
   split_ctas(w, cap, n, static_cast<uint32_t>(sms), out);
 }
 
+// The launches of a batched call: jobs of one operand format (fp16 first,
+// then bf16), at most 32 per launch, in job order; jobs that `skip` rejects are
+// left out. With explicit CTA counts each launch must fit in the SMs.
+template <typename Job>
+int launch_groups(const Job* jobs, uint32_t n, const uint32_t* ctas, int sms, bool (*skip)(const Job&),
+                  std::vector<std::vector<uint32_t>>* out) {
+  out->clear();
+  for (int bf16 = 0; bf16 < 2; ++bf16) {
+    std::vector<uint32_t> cur;
+    for (uint32_t j = 0; j < n; ++j) {
+      if (skip(jobs[j]) || jobs[j].ctx->bf16 != (bf16 != 0)) continue;
+      cur.push_back(j);
+      if (cur.size() == kMaxJobsPerLaunch) {
+        out->push_back(cur);
+        cur.clear();
+      }
+    }
+    if (!cur.empty()) out->push_back(cur);
+  }
+  for (const auto& grp : *out) {
+    if (grp.size() > static_cast<size_t>(sms)) return NRC_ERROR_INVALID_ARGUMENT;
+    if (ctas == nullptr) continue;
+    uint64_t sum = 0;
+    for (uint32_t j : grp) sum += ctas[j];
+    if (sum > static_cast<uint64_t>(sms)) return NRC_ERROR_INVALID_ARGUMENT;
+  }
+  return NRC_OK;
+}
+
+bool query_skip(const nrc_query_job& q) { return q.capacity == 0; }  // nothing to answer
+bool train_skip(const nrc_train_job&) { return false; }
+
 }  // namespace
 
 extern "C" {
@@ -593,34 +641,23 @@ int nrc_infer_many(const nrc_query_job* jobs, uint32_t n, const uint32_t* ctas, 
   int s = check_jobs(jobs, n, query_job_check);
   if (s != NRC_OK) return s;
   const int sms = device_sms();
-  if (ctas != nullptr) {
-    uint32_t sum = 0;
-    for (uint32_t j = 0; j < n; ++j) {
+  if (ctas != nullptr)
+    for (uint32_t j = 0; j < n; ++j)
       if (ctas[j] == 0) return NRC_ERROR_INVALID_ARGUMENT;
-      if (j % kMaxJobsPerLaunch == 0) sum = 0;
-      sum += ctas[j];
-      if (sum > static_cast<uint32_t>(sms)) return NRC_ERROR_INVALID_ARGUMENT;
-    }
-  }
+  std::vector<std::vector<uint32_t>> groups;
+  if ((s = launch_groups(jobs, n, ctas, sms, query_skip, &groups)) != NRC_OK) return s;
   nrc::InferJob ij[kMaxJobsPerLaunch];
   uint32_t g[kMaxJobsPerLaunch];
-  const nrc_query_job* sel[kMaxJobsPerLaunch];
   nrc_query_job kept[kMaxJobsPerLaunch];
-  for (uint32_t base = 0; base < n; base += kMaxJobsPerLaunch) {
-    const uint32_t m = std::min(n - base, kMaxJobsPerLaunch);
-    uint32_t k = 0;
-    for (uint32_t j = 0; j < m; ++j) {
-      const nrc_query_job& q = jobs[base + j];
-      if (q.capacity == 0) continue;  // nothing to answer
-      kept[k] = q;
-      sel[k] = &jobs[base + j];
-      if (ctas != nullptr) g[k] = ctas[base + j];
-      ++k;
+  for (const auto& grp : groups) {
+    const uint32_t k = static_cast<uint32_t>(grp.size());
+    for (uint32_t j = 0; j < k; ++j) {
+      kept[j] = jobs[grp[j]];
+      if (ctas != nullptr) g[j] = ctas[grp[j]];
     }
-    if (k == 0) continue;
     if (ctas == nullptr) plan_query(kept, k, sms, g);
     for (uint32_t j = 0; j < k; ++j) {
-      const nrc_query_job& q = *sel[j];
+      const nrc_query_job& q = kept[j];
       ij[j] = nrc::InferJob{};
       ij[j].wmap = *weight_map_of(q.ctx, q.weight_set);
       ij[j].input = q.inputs;
@@ -630,7 +667,8 @@ int nrc_infer_many(const nrc_query_job* jobs, uint32_t n, const uint32_t* ctas, 
       ij[j].q.out = q.out_rgb;
       ij[j].q.clamp = 1;
     }
-    const cudaError_t e = nrc::launch_infer_many(ij, static_cast<int>(k), g, static_cast<cudaStream_t>(stream));
+    const cudaError_t e = nrc::launch_infer_many(ij, static_cast<int>(k), g, static_cast<cudaStream_t>(stream),
+                                                 kept[0].ctx->bf16);
     if (e != cudaSuccess) return from_cuda(e);
   }
   return NRC_OK;
@@ -640,26 +678,23 @@ int nrc_train_many(const nrc_train_job* jobs, uint32_t n, const uint32_t* ctas, 
   int s = check_jobs(jobs, n, train_job_check);
   if (s != NRC_OK) return s;
   const int sms = device_sms();
-  if (ctas != nullptr) {
-    uint32_t sum = 0;
-    for (uint32_t j = 0; j < n; ++j) {
+  if (ctas != nullptr)
+    for (uint32_t j = 0; j < n; ++j)
       if (ctas[j] == 0 || ctas[j] > nrc::train_grid(nrc::TrainParams{}, sms)) return NRC_ERROR_INVALID_ARGUMENT;
-      if (j % kMaxJobsPerLaunch == 0) sum = 0;
-      sum += ctas[j];
-      if (sum > static_cast<uint32_t>(sms)) return NRC_ERROR_INVALID_ARGUMENT;
-    }
-  }
-  if (std::min(n, kMaxJobsPerLaunch) > static_cast<uint32_t>(sms)) return NRC_ERROR_INVALID_ARGUMENT;
+  std::vector<std::vector<uint32_t>> groups;
+  if ((s = launch_groups(jobs, n, ctas, sms, train_skip, &groups)) != NRC_OK) return s;
   std::vector<nrc::TrainJob> tj(kMaxJobsPerLaunch);
   uint32_t g[kMaxJobsPerLaunch];
-  for (uint32_t base = 0; base < n; base += kMaxJobsPerLaunch) {
-    const uint32_t m = std::min(n - base, kMaxJobsPerLaunch);
-    if (ctas == nullptr)
-      plan_train(jobs + base, m, sms, g);
-    else
-      for (uint32_t j = 0; j < m; ++j) g[j] = ctas[base + j];
+  nrc_train_job kept[kMaxJobsPerLaunch];
+  for (const auto& grp : groups) {
+    const uint32_t m = static_cast<uint32_t>(grp.size());
     for (uint32_t j = 0; j < m; ++j) {
-      const nrc_train_job& t = jobs[base + j];
+      kept[j] = jobs[grp[j]];
+      if (ctas != nullptr) g[j] = ctas[grp[j]];
+    }
+    if (ctas == nullptr) plan_train(kept, m, sms, g);
+    for (uint32_t j = 0; j < m; ++j) {
+      const nrc_train_job& t = kept[j];
       nrc::TrainParams p = train_params(t.ctx, t.nbatches, nrc::kTrainStep);
       for (int b = 0; b < t.nbatches; ++b)
         p.batch[b] = nrc::TrainBatch{t.records[b], t.d_counts[b], t.capacity,
@@ -731,7 +766,8 @@ int nrc_screen(const float* color, float* accum, uint32_t width, uint32_t height
 // Blob layout (little-endian): a 64-byte header, then the step state padded to
 // 32 bytes, the Adam entries, the training weights and the rendering weights.
 //   0 magic "NRCCKPT1" | 8 version | 12 parameter count | 16 batch cap |
-//   20 lr, beta1, beta2, eps, ema alpha, loss scale (f32) | 44 use_ema |
+//   20 lr, beta1, beta2, eps, ema alpha, loss scale (f32) | 44 use_ema (bit 0),
+//   precision (bits 8..15) |
 //   48 payload bytes (u64) | 56 FNV-1a 64 of the payload
 namespace {
 constexpr size_t kCkptHeader = 64;
@@ -771,7 +807,8 @@ int nrc_save_checkpoint(nrc_context* c, void* blob, size_t bytes) {
   std::memcpy(b + 8, u, 12);
   const float f[6] = {g.learning_rate, g.beta1, g.beta2, g.epsilon, g.ema_alpha, g.loss_scale};
   std::memcpy(b + 20, f, 24);
-  std::memcpy(b + 44, &g.use_ema_weights, 4);
+  const uint32_t flags = (g.use_ema_weights ? 1u : 0u) | (g.precision << 8);  // use_ema bit 0, precision bits 8..15
+  std::memcpy(b + 44, &flags, 4);
   const uint64_t pb = kCkptPayload, h = fnv1a(pay, kCkptPayload);
   std::memcpy(b + 48, &pb, 8);
   std::memcpy(b + 56, &h, 8);
@@ -794,10 +831,13 @@ int nrc_load_checkpoint(nrc_context* c, const void* blob, size_t bytes) {
       pb != kCkptPayload || fnv1a(pay, kCkptPayload) != h)
     return NRC_ERROR_BAD_CHECKPOINT;
   float f[6];
-  uint32_t use_ema = 0;
+  uint32_t flags = 0;
   std::memcpy(f, b + 20, 24);
-  std::memcpy(&use_ema, b + 44, 4);
-  if (u[2] == 0 || !(f[5] != 0.0f)) return NRC_ERROR_BAD_CHECKPOINT;
+  std::memcpy(&flags, b + 44, 4);
+  if (u[2] == 0 || !(f[5] != 0.0f) || (flags & ~0xFF01u) != 0) return NRC_ERROR_BAD_CHECKPOINT;
+  // the blob's 16-bit vectors must be in this context's format
+  if ((flags >> 8) != c->cfg.precision) return NRC_ERROR_INVALID_ARGUMENT;
+  const uint32_t use_ema = flags & 1u;
   cudaError_t e = cudaDeviceSynchronize();
   if (e == cudaSuccess) e = cudaMemcpy(c->state, pay, sizeof(nrc_optimizer_state), cudaMemcpyHostToDevice);
   if (e == cudaSuccess)
@@ -836,7 +876,7 @@ int nrc_set_weights(nrc_context* c, const uint16_t* host) {
     e = cudaMemcpy(ent.data(), c->entries, kParams * sizeof(nrc_optimizer_entry), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return from_cuda(e);
   for (int i = 0; i < kParams; ++i) {
-    const float w = f16_bits_to_f32(host[i]);
+    const float w = bits16_to_f32(host[i], c->bf16);
     ent[i].weight = w;
     ent[i].ema_weight = w;
   }

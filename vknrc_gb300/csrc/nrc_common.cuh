@@ -4,6 +4,7 @@
 #pragma once
 #include <cstdint>
 #include <cuda.h>
+#include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
 #include "../../include/nrc.h"
@@ -117,14 +118,16 @@ __device__ __forceinline__ void enc_qcdf_x2(float edge4_lo, float edge4_hi, floa
   c_hi = __saturatef(c_hi);
 }
 
-// NRCOneBlob4Encode (NRCRecord.glsl:58-63), packed to two f16x2 words.
+// NRCOneBlob4Encode (NRCRecord.glsl:58-63), packed to two 16-bit pair words
+// (fp16, or bf16 for the bf16 precision form).
+template <bool kBF16>
 __device__ __forceinline__ void enc_oneblob4(float x, uint32_t& w0, uint32_t& w1) {
   float f0, f1, f2, f3;
   enc_qcdf_x2(0.0f, 1.0f, x, f0, f1);
   enc_qcdf_x2(2.0f, 3.0f, x, f2, f3);
   const float f4 = enc_qcdf(4.0f, x);
-  w0 = pack_f16x2(__fsub_rn(f1, f0), __fsub_rn(f2, f1));
-  w1 = pack_f16x2(__fsub_rn(f3, f2), __fsub_rn(f4, f3));
+  w0 = pack2<kBF16>(__fsub_rn(f1, f0), __fsub_rn(f2, f1));
+  w1 = pack2<kBF16>(__fsub_rn(f3, f2), __fsub_rn(f4, f3));
 }
 
 // e^x by Cody-Waite reduction and a degree-7 Taylor polynomial (the same
@@ -147,18 +150,18 @@ __device__ __forceinline__ float enc_expf(float x) {
 }
 
 // Frequency features k0 .. k0+2n-1 of one coordinate -> n words.
-template <int K0, int N>
+template <int K0, int N, bool kBF16>
 __device__ __forceinline__ void enc_freq(float p, uint32_t* o) {
   if (fabsf(p) < 0x1p100f) {
 #pragma unroll
     for (int i = 0; i < N; ++i)
-      o[i] = pack_f16x2(enc_tri_h(p, 0.5f * static_cast<float>(1 << (K0 + 2 * i))),
-                        enc_tri_h(p, 0.5f * static_cast<float>(1 << (K0 + 2 * i + 1))));
+      o[i] = pack2<kBF16>(enc_tri_h(p, 0.5f * static_cast<float>(1 << (K0 + 2 * i))),
+                          enc_tri_h(p, 0.5f * static_cast<float>(1 << (K0 + 2 * i + 1))));
   } else {
 #pragma unroll
     for (int i = 0; i < N; ++i)
-      o[i] = pack_f16x2(enc_tri(p, static_cast<float>(1 << (K0 + 2 * i))),
-                        enc_tri(p, static_cast<float>(1 << (K0 + 2 * i + 1))));
+      o[i] = pack2<kBF16>(enc_tri(p, static_cast<float>(1 << (K0 + 2 * i))),
+                          enc_tri(p, static_cast<float>(1 << (K0 + 2 * i + 1))));
   }
 }
 
@@ -168,29 +171,32 @@ __device__ __forceinline__ void enc_freq(float p, uint32_t* o) {
 // features 32..63 = pos.z frequencies 8..11, the five one-blob groups, diffuse,
 // specular and the two constant ones. Word j holds features 2j (low half) and
 // 2j+1 of its half.
+template <bool kBF16 = false>
 __device__ __forceinline__ void encode_half0(const float (&r)[kInFloats], uint32_t* e) {
-  enc_freq<0, 6>(r[0], e + 0);
-  enc_freq<0, 6>(r[1], e + 6);
-  enc_freq<0, 4>(r[2], e + 12);
+  enc_freq<0, 6, kBF16>(r[0], e + 0);
+  enc_freq<0, 6, kBF16>(r[1], e + 6);
+  enc_freq<0, 4, kBF16>(r[2], e + 12);
 }
 
+template <bool kBF16 = false>
 __device__ __forceinline__ void encode_half1(const float (&r)[kInFloats], uint32_t* e) {
-  enc_freq<8, 2>(r[2], e + 0);
-  enc_oneblob4(r[3], e[2], e[3]);
-  enc_oneblob4(r[4], e[4], e[5]);
-  enc_oneblob4(r[5], e[6], e[7]);
-  enc_oneblob4(r[6], e[8], e[9]);
-  enc_oneblob4(__fsub_rn(1.0f, enc_expf(-r[7])), e[10], e[11]);
-  e[12] = pack_f16x2(r[8], r[9]);
-  e[13] = pack_f16x2(r[10], r[11]);
-  e[14] = pack_f16x2(r[12], r[13]);
-  e[15] = pack_f16x2(1.0f, 1.0f);
+  enc_freq<8, 2, kBF16>(r[2], e + 0);
+  enc_oneblob4<kBF16>(r[3], e[2], e[3]);
+  enc_oneblob4<kBF16>(r[4], e[4], e[5]);
+  enc_oneblob4<kBF16>(r[5], e[6], e[7]);
+  enc_oneblob4<kBF16>(r[6], e[8], e[9]);
+  enc_oneblob4<kBF16>(__fsub_rn(1.0f, enc_expf(-r[7])), e[10], e[11]);
+  e[12] = pack2<kBF16>(r[8], r[9]);
+  e[13] = pack2<kBF16>(r[10], r[11]);
+  e[14] = pack2<kBF16>(r[12], r[13]);
+  e[15] = pack2<kBF16>(1.0f, 1.0f);
 }
 
-// The whole record: 14 fp32 -> 64 fp16 as 32 words.
+// The whole record: 14 fp32 -> 64 16-bit features as 32 words.
+template <bool kBF16 = false>
 __device__ __forceinline__ void encode_input(const float (&r)[kInFloats], uint32_t (&e)[32]) {
-  encode_half0(r, e);
-  encode_half1(r, e + 16);
+  encode_half0<kBF16>(r, e);
+  encode_half1<kBF16>(r, e + 16);
 }
 
 // Device-side error word bits (read back by nrc_get_error).

@@ -105,7 +105,8 @@ __device__ __forceinline__ void scatter_query(const QueryOut& Q, uint32_t dst, f
 // plain query path is compiled without the destination load and epilogue.
 // One launch serves up to N caches: CTAs [group_start[j], group_start[j+1])
 // answer cache j's queries with its weights; with N = 1 the group is the grid.
-template <bool kEncoded, bool kScatter, int N>
+// kBF16: weights, features and activations in bf16 instead of fp16.
+template <bool kEncoded, bool kScatter, int N, bool kBF16>
 __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_constant__ InferLaunch<N> L) {
   int job = 0;
   while (job + 1 < L.njobs && blockIdx.x >= L.group_start[job + 1]) ++job;
@@ -161,7 +162,7 @@ __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_co
   const uint32_t a_col = tmem + s * kSlotCols, d_col = a_col + 32;  // lane-0 addresses of the slot
   const uint32_t lane_off = static_cast<uint32_t>(q * 32) << 16;
   const uint64_t wdesc = sdesc_sw128(smem_u32(smem_w), 16, 1024);  // layer l: + l * 512
-  const uint32_t id64 = idesc_f16_f32(128, 64, 0, 0), id16 = idesc_f16_f32(128, 16, 0, 0);
+  const uint32_t id64 = idesc_16_f32(128, 64, 0, 0, kBF16), id16 = idesc_16_f32(128, 16, 0, 0, kBF16);
   uint8_t* stage0 = smem_rec + (s * 2 + 0) * kRecTileBytes;
   const nrc_input* rec_in = static_cast<const nrc_input*>(input);
   auto tile_of = [&](uint32_t it) { return (it * G + rank) * kSlots + s; };
@@ -204,7 +205,7 @@ __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_co
       }
       // the stage may be refilled once all 128 threads have read it
       mbar_arrive(&B.rec_empty[b]);
-      encode_input(r, e);
+      encode_input<kBF16>(r, e);
       if (leader && tile_of(it + 2) < num_tiles) {
         if (!mbar_wait(&B.rec_empty[b], (it >> 1) & 1, kWaitLimitNs))
           atomicOr(err, kErrTimeout);
@@ -257,11 +258,11 @@ __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_co
         uint32_t v[32], p[32];
         tmem_ld32(d_col + lane_off, v);
 #pragma unroll
-        for (int j = 0; j < 16; ++j) p[j] = pack_relu_f16x2(__uint_as_float(v[2 * j]), __uint_as_float(v[2 * j + 1]));
+        for (int j = 0; j < 16; ++j) p[j] = pack2_relu<kBF16>(__uint_as_float(v[2 * j]), __uint_as_float(v[2 * j + 1]));
         tmem_ld32(d_col + lane_off + 32, v);
 #pragma unroll
         for (int j = 0; j < 16; ++j)
-          p[16 + j] = pack_relu_f16x2(__uint_as_float(v[2 * j]), __uint_as_float(v[2 * j + 1]));
+          p[16 + j] = pack2_relu<kBF16>(__uint_as_float(v[2 * j]), __uint_as_float(v[2 * j + 1]));
         tmem_st32(a_col + lane_off, p);
         tc_fence_before();
         mbar_arrive(&B.a_ready);
@@ -296,7 +297,7 @@ __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_co
   }
 }
 
-template <bool kEncoded, bool kScatter, int N>
+template <bool kEncoded, bool kScatter, int N, bool kBF16>
 cudaError_t launch(const InferLaunch<N>& L, uint32_t grid, cudaStream_t stream) {
   cudaLaunchAttribute attr;
   attr.id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -308,22 +309,25 @@ cudaError_t launch(const InferLaunch<N>& L, uint32_t grid, cudaStream_t stream) 
   cfg.stream = stream;
   cfg.attrs = &attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, infer_kernel<kEncoded, kScatter, N>, L);
+  return cudaLaunchKernelEx(&cfg, infer_kernel<kEncoded, kScatter, N, kBF16>, L);
 }
 
-template <bool kEncoded, bool kScatter, int N>
+template <bool kEncoded, bool kScatter, int N, bool kBF16>
 cudaError_t set_smem() {
-  return cudaFuncSetAttribute(infer_kernel<kEncoded, kScatter, N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              kSmemBytes);
+  return cudaFuncSetAttribute(infer_kernel<kEncoded, kScatter, N, kBF16>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
 }
 
 }  // namespace
 
 cudaError_t configure_infer_kernels() {
-  cudaError_t e = set_smem<true, false, 1>();
-  if (e == cudaSuccess) e = set_smem<false, false, 1>();
-  if (e == cudaSuccess) e = set_smem<false, true, 1>();
-  if (e == cudaSuccess) e = set_smem<false, false, kMaxInferJobs>();
+  cudaError_t e = set_smem<true, false, 1, false>();
+  if (e == cudaSuccess) e = set_smem<false, false, 1, false>();
+  if (e == cudaSuccess) e = set_smem<false, true, 1, false>();
+  if (e == cudaSuccess) e = set_smem<false, false, kMaxInferJobs, false>();
+  if (e == cudaSuccess) e = set_smem<false, false, 1, true>();
+  if (e == cudaSuccess) e = set_smem<false, true, 1, true>();
+  if (e == cudaSuccess) e = set_smem<false, false, kMaxInferJobs, true>();
   return e;
 }
 
@@ -339,7 +343,7 @@ uint32_t infer_grid(uint32_t capacity, int num_sms) {
 
 cudaError_t launch_infer(const void* input, bool encoded, const uint32_t* d_count, uint32_t capacity,
                          const CUtensorMap* wmap, const QueryOut& q, uint32_t* err, int num_sms,
-                         cudaStream_t stream) {
+                         cudaStream_t stream, bool bf16) {
   const uint32_t grid = infer_grid(capacity, num_sms);
   if (grid == 0) return cudaSuccess;
   InferLaunch<1> L;
@@ -352,12 +356,14 @@ cudaError_t launch_infer(const void* input, bool encoded, const uint32_t* d_coun
   L.group_start[0] = 0;
   L.group_start[1] = grid;
   L.njobs = 1;
-  if (encoded) return launch<true, false>(L, grid, stream);
-  if (q.dst != nullptr) return launch<false, true>(L, grid, stream);
-  return launch<false, false>(L, grid, stream);
+  if (encoded) return bf16 ? cudaErrorInvalidValue : launch<true, false, 1, false>(L, grid, stream);
+  if (q.dst != nullptr)
+    return bf16 ? launch<false, true, 1, true>(L, grid, stream) : launch<false, true, 1, false>(L, grid, stream);
+  return bf16 ? launch<false, false, 1, true>(L, grid, stream) : launch<false, false, 1, false>(L, grid, stream);
 }
 
-cudaError_t launch_infer_many(const InferJob* jobs, int njobs, const uint32_t* group_size, cudaStream_t stream) {
+cudaError_t launch_infer_many(const InferJob* jobs, int njobs, const uint32_t* group_size, cudaStream_t stream,
+                              bool bf16) {
   if (njobs < 1 || njobs > kMaxInferJobs) return cudaErrorInvalidValue;
   static InferLaunch<kMaxInferJobs> L;  // host staging of the kernel parameters (copied at launch)
   static std::mutex m;
@@ -371,7 +377,8 @@ cudaError_t launch_infer_many(const InferJob* jobs, int njobs, const uint32_t* g
   }
   L.group_start[njobs] = grid;
   L.njobs = njobs;
-  return launch<false, false>(L, grid, stream);
+  return bf16 ? launch<false, false, kMaxInferJobs, true>(L, grid, stream)
+              : launch<false, false, kMaxInferJobs, false>(L, grid, stream);
 }
 
 }  // namespace nrc

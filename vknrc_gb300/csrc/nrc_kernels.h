@@ -31,9 +31,11 @@ struct QueryOut {
   uint32_t train_cap[NRC_TRAIN_BATCH_COUNT];
 };
 
+// bf16: the weights and the operands are bf16 (the bf16 precision form); the
+// pre-encoded input path is fp16 only.
 cudaError_t launch_infer(const void* input, bool encoded, const uint32_t* d_count, uint32_t capacity,
                          const CUtensorMap* wmap, const QueryOut& q, uint32_t* err, int num_sms,
-                         cudaStream_t stream);
+                         cudaStream_t stream, bool bf16 = false);
 
 // One cache's share of a query launch.
 struct InferJob {
@@ -60,7 +62,8 @@ constexpr int kMaxInferJobs = 32;  // caches per batched query launch
 uint32_t infer_grid(uint32_t capacity, int num_sms);
 // One launch answering njobs caches' record queries (dense rgb output, no
 // destination words), group_size[j] >= 1 CTAs for job j, sum <= SMs.
-cudaError_t launch_infer_many(const InferJob* jobs, int njobs, const uint32_t* group_size, cudaStream_t stream);
+cudaError_t launch_infer_many(const InferJob* jobs, int njobs, const uint32_t* group_size, cudaStream_t stream,
+                              bool bf16 = false);
 
 // One launch of the persistent trainer: up to NRC_TRAIN_BATCH_COUNT chained
 // batches, each a fused gradient pass followed by the optimizer step (mode
@@ -93,6 +96,7 @@ struct TrainParams {
   double* loss_acc;  // optional check-path loss sum
   unsigned long long* loss_count;
   uint32_t* err;
+  int bf16;          // weights and operands in bf16 (host side: selects the kernel)
 };
 
 // One cache's share of a training launch: its weight tensor map and parameters.

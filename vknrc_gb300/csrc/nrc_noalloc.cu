@@ -80,7 +80,8 @@ extern "C" NRC_API int nrc_train_noalloc(uint16_t* d_weights, uint16_t* d_use_we
                                          const nrc_train_record* d_records, uint32_t* d_count, uint32_t capacity,
                                          const nrc_config* cfg, uint32_t* d_error, void* stream) {
   if (cfg == nullptr || d_weights == nullptr || d_entries == nullptr || d_state == nullptr || d_count == nullptr ||
-      (capacity > 0 && d_records == nullptr) || cfg->train_batch_size == 0 || !(cfg->loss_scale != 0.0f))
+      (capacity > 0 && d_records == nullptr) || cfg->train_batch_size == 0 || !(cfg->loss_scale != 0.0f) ||
+      (cfg->precision != NRC_PRECISION_FP16 && cfg->precision != NRC_PRECISION_BF16))
     return NRC_ERROR_INVALID_ARGUMENT;
   if (!aligned16(d_weights) || !aligned16(d_entries) || (d_records && !aligned16(d_records)) ||
       (d_use_weights && (reinterpret_cast<uintptr_t>(d_use_weights) & 1u)))
@@ -112,6 +113,7 @@ extern "C" NRC_API int nrc_train_noalloc(uint16_t* d_weights, uint16_t* d_use_we
   p.ema_alpha = cfg->ema_alpha;
   p.loss_scale = cfg->loss_scale;
   p.use_ema = cfg->use_ema_weights != 0;
+  p.bf16 = cfg->precision == NRC_PRECISION_BF16 ? 1 : 0;
   p.entries = d_entries;
   p.state = d_state;
   p.w16 = reinterpret_cast<__half*>(d_weights);

@@ -129,6 +129,29 @@ __device__ __forceinline__ uint32_t relu_mask_f16x2(uint32_t g, uint32_t a) {
   return g & __hgt2_mask(a2, __float2half2_rn(0.0f)) & ~__hneu2_mask(g2, g2);
 }
 
+// The same on bf16 pairs, on the bit patterns: a half is kept where the
+// activation is greater than zero (sign clear, non-zero, not NaN) and the
+// gradient is not NaN.
+__device__ __forceinline__ uint32_t relu_mask_bf16x2(uint32_t g, uint32_t a) {
+  uint32_t keep = 0;
+#pragma unroll
+  for (int h = 0; h < 32; h += 16) {
+    const uint32_t ah = (a >> h) & 0xFFFFu, gh = (g >> h) & 0xFFFFu;
+    if (ah != 0u && ah <= 0x7F80u && (gh & 0x7FFFu) <= 0x7F80u) keep |= 0xFFFFu << h;
+  }
+  return g & keep;
+}
+
+template <bool kBF16>
+__device__ __forceinline__ uint32_t relu_mask2(uint32_t g, uint32_t a) {
+  return kBF16 ? relu_mask_bf16x2(g, a) : relu_mask_f16x2(g, a);
+}
+
+template <bool kBF16>
+__device__ __forceinline__ uint16_t to16(float x) {
+  return kBF16 ? __bfloat16_as_ushort(__float2bfloat16_rn(x)) : __half_as_ushort(__float2half_rn(x));
+}
+
 // Write half h (32 inputs) of one layer's final weight gradient from TMEM to the
 // CTA's partial slot. M=64 accumulator layout: output row 16q+t lives in TMEM
 // lane 32q+t (t < 16), so lanes 0..15 of each warp own one output row.
@@ -192,10 +215,11 @@ struct AdamHyper {
   int use_ema;
 };
 
+template <bool kBF16>
 __device__ __forceinline__ void adam_one(int i, float gsum, uint32_t n, const nrc_optimizer_state& st,
                                          const AdamHyper& hp, nrc_optimizer_entry& e,
-                                         nrc_optimizer_entry* __restrict__ entries, __half* __restrict__ w16,
-                                         __half* __restrict__ use16) {
+                                         nrc_optimizer_entry* __restrict__ entries, uint16_t* __restrict__ w16,
+                                         uint16_t* __restrict__ use16) {
   float g = __fdiv_rn(__fdiv_rn(gsum, static_cast<float>(n)), hp.loss_scale);
   if (isnan(g) || isinf(g)) g = 0.0f;
   const float m = __fmaf_rn(hp.beta1, e.m, __fmul_rn(__fsub_rn(1.0f, hp.beta1), g));
@@ -211,15 +235,17 @@ __device__ __forceinline__ void adam_one(int i, float gsum, uint32_t n, const nr
   e.weight = w;
   e.ema_weight = ema;
   entries[i] = e;
-  w16[i] = __float2half_rn(w);
-  if (use16 != nullptr) use16[i] = __float2half_rn(hp.use_ema ? ema : w);
+  w16[i] = to16<kBF16>(w);
+  if (use16 != nullptr) use16[i] = to16<kBF16>(hp.use_ema ? ema : w);
 }
 
 // One launch trains up to N caches: CTAs [group_start[j], group_start[j+1])
 // form cache j's group, which runs the whole schedule below on its own (its own
 // grid barrier, partial slots and parameter slices). With N = 1 the group is the
 // grid.
-template <int N>
+// kBF16: weights, activations and gradients in bf16 instead of fp16 (the master
+// weights and moments are fp32 either way).
+template <int N, bool kBF16>
 __global__ void __launch_bounds__(kTrainThreads, 1) train_steps_kernel(const __grid_constant__ TrainLaunch<N> L) {
   int job = 0;
   while (job + 1 < L.njobs && blockIdx.x >= L.group_start[job + 1]) ++job;
@@ -360,9 +386,9 @@ __global__ void __launch_bounds__(kTrainThreads, 1) train_steps_kernel(const __g
     }
     uint32_t e[16];
     if (h == 0)
-      encode_half0(r, e);
+      encode_half0<kBF16>(r, e);
     else
-      encode_half1(r, e);
+      encode_half1<kBF16>(r, e);
     if (!valid) {
 #pragma unroll
       for (int k = 0; k < 16; ++k) e[k] = 0u;
@@ -396,10 +422,10 @@ __global__ void __launch_bounds__(kTrainThreads, 1) train_steps_kernel(const __g
       // ---------------------------------------------------- MMA issuer --
       // The whole warp runs the schedule (converged, so descriptors stay
       // warp-uniform); one elected lane issues each group of MMAs.
-      const uint32_t id_fwd = idesc_f16_f32(128, 64, 0, 0);
-      const uint32_t id_out = idesc_f16_f32(128, 16, 0, 0);
-      const uint32_t id_dw = idesc_f16_f32(64, 64, 1, 1);
-      const uint32_t id_da = idesc_f16_f32(128, 64, 0, 1);
+      const uint32_t id_fwd = idesc_16_f32(128, 64, 0, 0, kBF16);
+      const uint32_t id_out = idesc_16_f32(128, 16, 0, 0, kBF16);
+      const uint32_t id_dw = idesc_16_f32(64, 64, 1, 1, kBF16);
+      const uint32_t id_da = idesc_16_f32(128, 64, 0, 1, kBF16);
       const uint32_t dcol = tmem + kDCol, acol = tmem + kACol;
       // descriptor bases; +1 in the address field = 16 bytes
       const uint64_t dk_w = sdesc_sw128(smem_u32(smem_w), 16, 1024);    // K-major W_l: + l*512 + 2j
@@ -483,7 +509,7 @@ __global__ void __launch_bounds__(kTrainThreads, 1) train_steps_kernel(const __g
           tmem_ld32(d_lane, v);
 #pragma unroll
           for (int j = 0; j < 16; ++j)
-            p[j] = pack_relu_f16x2(__uint_as_float(v[2 * j]), __uint_as_float(v[2 * j + 1]));
+            p[j] = pack2_relu<kBF16>(__uint_as_float(v[2 * j]), __uint_as_float(v[2 * j + 1]));
           tmem_st16(a_lane, p);
           store_half(act + (l + 1) * kActBytes, row, h, p);
           publish();
@@ -508,8 +534,8 @@ __global__ void __launch_bounds__(kTrainThreads, 1) train_steps_kernel(const __g
             const float d1 = __fdiv_rn(__fmul_rn(s2, __fsub_rn(p1, target[1])), den);
             const float d2 = __fdiv_rn(__fmul_rn(s2, __fsub_rn(p2, target[2])), den);
             if (valid) {
-              gw[0] = pack_f16x2(d0, d1);
-              gw[1] = pack_f16x2(d2, 0.0f);
+              gw[0] = pack2<kBF16>(d0, d1);
+              gw[1] = pack2<kBF16>(d2, 0.0f);
               if (P.loss_acc != nullptr) {
                 const double dd = static_cast<double>(den);
                 const double e0 = static_cast<double>(p0) - target[0], e1 = static_cast<double>(p1) - target[1],
@@ -531,7 +557,7 @@ __global__ void __launch_bounds__(kTrainThreads, 1) train_steps_kernel(const __g
           tmem_ld32(d_lane, v);
 #pragma unroll
           for (int j = 0; j < 16; ++j)
-            gw[j] = relu_mask_f16x2(pack_f16x2(__uint_as_float(v[2 * j]), __uint_as_float(v[2 * j + 1])), aw[j]);
+            gw[j] = relu_mask2<kBF16>(pack2<kBF16>(__uint_as_float(v[2 * j]), __uint_as_float(v[2 * j + 1])), aw[j]);
           tmem_st16(a_lane, gw);
           store_half(gbuf + ((6 - l) & 1) * kActBytes, row, h, gw);
           publish();
@@ -594,7 +620,7 @@ __global__ void __launch_bounds__(kTrainThreads, 1) train_steps_kernel(const __g
       // as (s0 + s1) + (s2 + s3): a fixed order, so runs are identical. Thread
       // `part` then owns parameter 4 * column + part.
       const uint32_t part = threadIdx.x & 3;
-      __half* use16 = bt.write_use ? P.use16 : nullptr;
+      uint16_t* use16 = bt.write_use ? reinterpret_cast<uint16_t*>(P.use16) : nullptr;
       for (uint32_t cb = 0; cb < ncols; cb += kTrainThreads / 4) {
         const uint32_t cc = cb + (threadIdx.x >> 2);
         float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -619,7 +645,7 @@ __global__ void __launch_bounds__(kTrainThreads, 1) train_steps_kernel(const __g
           const uint32_t k = 4 * cc + part;  // parameter index within the slice
           if (P.mode == kTrainStep) {
             nrc_optimizer_entry e = cached ? ecache[k] : P.entries[4 * c0 + k];
-            adam_one(4 * c0 + k, gsum, n, st, hp, e, P.entries, P.w16, use16);
+            adam_one<kBF16>(4 * c0 + k, gsum, n, st, hp, e, P.entries, reinterpret_cast<uint16_t*>(P.w16), use16);
             if (cached) ecache[k] = e;
           } else
             P.grad_out[4 * c0 + k] = gsum;
@@ -678,7 +704,7 @@ __global__ void __launch_bounds__(kTrainThreads, 1) train_steps_kernel(const __g
 }
 
 template <int N>
-cudaError_t launch(const TrainLaunch<N>& L, uint32_t grid, cudaStream_t stream) {
+cudaError_t launch(const TrainLaunch<N>& L, uint32_t grid, cudaStream_t stream, bool bf16) {
   cudaLaunchAttribute attr;
   attr.id = cudaLaunchAttributeCooperative;
   attr.val.cooperative = 1;
@@ -689,17 +715,20 @@ cudaError_t launch(const TrainLaunch<N>& L, uint32_t grid, cudaStream_t stream) 
   cfg.stream = stream;
   cfg.attrs = &attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, train_steps_kernel<N>, L);
+  return bf16 ? cudaLaunchKernelEx(&cfg, train_steps_kernel<N, true>, L)
+              : cudaLaunchKernelEx(&cfg, train_steps_kernel<N, false>, L);
 }
 
 }  // namespace
 
 cudaError_t configure_train_kernels() {
-  cudaError_t e =
-      cudaFuncSetAttribute(train_steps_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTrainSmemBytes);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(train_steps_kernel<kMaxTrainJobs>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             kTrainSmemBytes);
+  const void* k[4] = {reinterpret_cast<const void*>(train_steps_kernel<1, false>),
+                      reinterpret_cast<const void*>(train_steps_kernel<kMaxTrainJobs, false>),
+                      reinterpret_cast<const void*>(train_steps_kernel<1, true>),
+                      reinterpret_cast<const void*>(train_steps_kernel<kMaxTrainJobs, true>)};
+  cudaError_t e = cudaSuccess;
+  for (int i = 0; i < 4 && e == cudaSuccess; ++i)
+    e = cudaFuncSetAttribute(k[i], cudaFuncAttributeMaxDynamicSharedMemorySize, kTrainSmemBytes);
   return e;
 }
 
@@ -721,7 +750,7 @@ cudaError_t launch_train(const TrainParams& p, const CUtensorMap* wmap, int max_
   L.group_start[0] = 0;
   L.group_start[1] = grid;
   L.njobs = 1;
-  return launch(L, grid, stream);
+  return launch(L, grid, stream, p.bf16 != 0);
 }
 
 cudaError_t launch_train_many(const TrainJob* jobs, int njobs, const uint32_t* group_size, cudaStream_t stream) {
@@ -732,6 +761,7 @@ cudaError_t launch_train_many(const TrainJob* jobs, int njobs, const uint32_t* g
   uint32_t grid = 0;
   for (int j = 0; j < njobs; ++j) {
     if (jobs[j].p.steps < 1 || jobs[j].p.steps > NRC_TRAIN_BATCH_COUNT) return cudaErrorInvalidValue;
+    if (jobs[j].p.bf16 != jobs[0].p.bf16) return cudaErrorInvalidValue;  // one operand format per launch
     if (group_size[j] < 1 || group_size[j] > kMaxTrainCtas) return cudaErrorInvalidConfiguration;
     L.job[j] = jobs[j];
     L.group_start[j] = grid;
@@ -739,7 +769,7 @@ cudaError_t launch_train_many(const TrainJob* jobs, int njobs, const uint32_t* g
   }
   L.group_start[njobs] = grid;
   L.njobs = njobs;
-  return launch(L, grid, stream);
+  return launch(L, grid, stream, jobs[0].p.bf16 != 0);
 }
 
 }  // namespace nrc

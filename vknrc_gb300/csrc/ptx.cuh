@@ -238,6 +238,11 @@ __host__ __device__ constexpr uint32_t idesc_f16_f32(uint32_t M, uint32_t N, uin
                                                       uint32_t b_mn_major) {
   return (1u << 4) | (a_mn_major << 15) | (b_mn_major << 16) | ((N >> 3) << 17) | ((M >> 4) << 24);
 }
+// kind::f16 with A and B both bf16 (A and B formats, bits 7..9 and 10..12, = 1).
+__host__ __device__ constexpr uint32_t idesc_16_f32(uint32_t M, uint32_t N, uint32_t a_mn_major, uint32_t b_mn_major,
+                                                     bool bf16) {
+  return idesc_f16_f32(M, N, a_mn_major, b_mn_major) | (bf16 ? ((1u << 7) | (1u << 10)) : 0u);
+}
 
 // D[tmem] (+)= A[smem desc] * B[smem desc]
 __device__ __forceinline__ void mma_ss(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
@@ -288,6 +293,28 @@ __device__ __forceinline__ uint32_t pack_f16x2(float lo, float hi) {
   uint32_t r;
   asm("cvt.rn.f16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
   return r;
+}
+
+// The same conversions to bf16x2 (8-bit mantissa, fp32's exponent range).
+__device__ __forceinline__ uint32_t pack_relu_bf16x2(float lo, float hi) {
+  uint32_t r;
+  asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+  return r;
+}
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
+  uint32_t r;
+  asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+  return r;
+}
+
+// Operand format of the 16-bit path: fp16 (the reference's) or bf16.
+template <bool kBF16>
+__device__ __forceinline__ uint32_t pack2(float lo, float hi) {
+  return kBF16 ? pack_bf16x2(lo, hi) : pack_f16x2(lo, hi);
+}
+template <bool kBF16>
+__device__ __forceinline__ uint32_t pack2_relu(float lo, float hi) {
+  return kBF16 ? pack_relu_bf16x2(lo, hi) : pack_relu_f16x2(lo, hi);
 }
 
 // Byte offset of 16-byte chunk `chunk` (0..7) of row `row` inside a tile of

@@ -49,7 +49,10 @@ class Config(ctypes.Structure):
                 ("beta1", ctypes.c_float), ("beta2", ctypes.c_float), ("epsilon", ctypes.c_float),
                 ("ema_alpha", ctypes.c_float), ("loss_scale", ctypes.c_float),
                 ("use_ema_weights", ctypes.c_uint32), ("deterministic", ctypes.c_uint32),
-                ("track_loss", ctypes.c_uint32), ("seed", ctypes.c_uint64)]
+                ("track_loss", ctypes.c_uint32), ("seed", ctypes.c_uint64), ("precision", ctypes.c_uint32)]
+
+
+PRECISION_FP16, PRECISION_BF16 = 0, 1
 
 
 class OptState(ctypes.Structure):
