@@ -411,6 +411,40 @@ def precision_leg(evals, trains, eval_cnt, train_cnt, steps=500):
             "accuracy": "tests/test_gpu_precision.py: query error and 1000-step loss against the FP64 oracle"}
 
 
+def fp8_leg(evals, trains, eval_cnt, train_cnt, steps=500):
+    """The 1080p query through the FP8 (E4M3) form of a cache trained for 32
+    frames, timed alone (query kernel), and the whole frame with it (FP8
+    query, four fp16 training steps, the E4M3 re-quantization)."""
+    import torch
+
+    from vknrc_gb300 import Cache
+
+    out = torch.empty((Q, 3), dtype=torch.float32, device="cuda")
+    with Cache(seed=1234, learning_rate=1e-3, beta2=0.99, fp8_inference=1) as c:
+        for k in range(32):
+            c.train_batches(trains[k % len(trains)], train_cnt, write_use_last=True)
+        for k in range(5):
+            c.infer_fp8(evals[k % len(evals)], eval_cnt, out)
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        for k in range(steps):
+            c.infer_fp8(evals[k % len(evals)], eval_cnt, out)
+        e.record()
+        torch.cuda.synchronize()
+        q_s = s.elapsed_time(e) / 1e3 / steps
+        s.record()
+        for k in range(steps):
+            c.infer_fp8(evals[k % len(evals)], eval_cnt, out)
+            c.train_batches(trains[k % len(trains)], train_cnt, write_use_last=True)
+        e.record()
+        torch.cuda.synchronize()
+        f_s = s.elapsed_time(e) / 1e3 / steps
+        if c.error() != 0:
+            raise RuntimeError("device error in the fp8 leg")
+    return {"infer_ms": q_s * 1e3, "queries_per_s": Q / q_s, "frame_ms": f_s * 1e3, "steps": steps,
+            "accuracy": "tests/test_gpu_fp8.py: query error against the FP64 oracle"}
+
+
 # --------------------------------------------------------------- serving leg --
 SERVE_RES = [(1280, 720), (1920, 1080), (2560, 1440)]
 
@@ -646,7 +680,8 @@ def ours_arm(args, world, rank, local):
         result["plain_fp16"] = {"queries_per_s": plain, "what": "nrc_encode + 6 torch fp16 GEMMs (cuBLAS), infer only",
                                 "fused_infer_queries_per_s": Q / infer_s}
     if rank == 0 and world == 1 and not args.no_batched:
-        result["precision"] = {"bf16": precision_leg(evals, trains, eval_cnt, train_cnt)}
+        result["precision"] = {"bf16": precision_leg(evals, trains, eval_cnt, train_cnt),
+                               "fp8_query": fp8_leg(evals, trains, eval_cnt, train_cnt)}
     if rank == 0 and world == 1 and not args.no_batched:
         result["batched"] = batched_leg(evals, trains)
     if rank == 0 and world == 1 and not args.no_serving:

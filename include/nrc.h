@@ -93,6 +93,7 @@ typedef struct nrc_config {
   uint32_t track_loss;      /* 1: accumulate the relative-L2 loss (check path, FP64 sum) */
   uint64_t seed;            /* He initialisation seed */
   uint32_t precision;       /* nrc_precision: the 16-bit format of weights and operands */
+  uint32_t fp8_inference;   /* 1: keep an FP8 (E4M3) copy of use_weights for nrc_infer_fp8 */
 } nrc_config;
 
 /* Precision forms. FP16 is the reference's (fp16 weights, features and
@@ -457,6 +458,27 @@ NRC_API int nrc_unpack_eval(const nrc_scene* scene, const nrc_eval_record* d_rec
  * d_out, ready for nrc_train / nrc_train_batches. */
 NRC_API int nrc_unpack_train(const nrc_scene* scene, const nrc_packed_train_record* d_records,
                              const uint32_t* d_count, uint32_t capacity, nrc_train_record* d_out, void* stream);
+
+/* FP8 precision form of the cache query (no counterpart in the reference, whose
+ * query runs in fp16). A context created with fp8_inference = 1 keeps an E4M3
+ * copy of use_weights with per-layer absmax scales: s_w = max|W_l| / 448 for
+ * the weights, s_x = max|x_l| / 448 for each layer's inputs, where max|x_l| is
+ * the largest input the training forward passes met since the scales were last
+ * set (bounded from the weights for a layer not yet observed). The scales are
+ * recomputed once per 16 optimizer steps; the E4M3 weights are re-quantized
+ * with the current scales after every training call (a small launch on the
+ * same stream), so the FP8 query always uses the latest rendering weights.
+ * Accumulation is fp32; each layer's sum is rescaled before the ReLU. */
+/* Cache query as nrc_infer with the E4M3 weights and activations. */
+NRC_API int nrc_infer_fp8(nrc_context* ctx, const nrc_input* d_inputs, const uint32_t* d_count, uint32_t capacity,
+                          float* d_out_rgb, void* stream);
+/* Recomputes the scales and re-quantizes now (stream-ordered). */
+NRC_API int nrc_fp8_refresh(nrc_context* ctx, void* stream);
+/* Host copies (synchronous): host_w8 receives NRC_PARAM_COUNT E4M3 bytes in the
+ * parameter layout, host_scales 25 floats: s_w[6], s_x[6], the per-layer
+ * epilogue factors c[6] (s_w s_x / s_x of the next layer; s_w s_x for the
+ * output layer), 1 / s_x[0], 1 / s_w[6] (as 448 / max|W_l|). Either may be NULL. */
+NRC_API int nrc_get_fp8(nrc_context* ctx, uint8_t* host_w8, float* host_scales);
 
 /* Screen pass (shader/src/screen.frag:10-31) on a headless image: `d_color` is
  * the composited rgba32f image ([height][width][4], rgb used; the bias_factor_r

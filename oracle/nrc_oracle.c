@@ -705,3 +705,142 @@ void oracle_unpack(const oracle_scene* S, const uint32_t* packed, int64_t n, int
     }
   }
 }
+
+/* ------------------------------------------------------------- fp8 -- */
+/* E4M3 (bias 7, no infinities, max 448): round to nearest even, saturated to
+ * +-448 (the GPU's cvt.rn.satfinite), NaN -> 0x7F. */
+uint8_t oracle_f32_to_e4m3(float x) {
+  if (isnan(x)) return 0x7F;
+  const uint8_t sign = signbit(x) ? 0x80 : 0;
+  float a = fabsf(x);
+  if (a > 448.0f) a = 448.0f;
+  if (a == 0.0f) return sign;
+  int e;
+  frexpf(a, &e);
+  int ex = e - 1; /* floor(log2 a) */
+  if (ex < -6) ex = -6;
+  const float q = ldexpf(1.0f, ex - 3);
+  const float r = rintf(a / q) * q; /* a / q is an exact power-of-two scaling */
+  if (r == 0.0f) return sign;
+  frexpf(r, &e);
+  ex = e - 1;
+  if (ex < -6) return (uint8_t)(sign | (int)(r / ldexpf(1.0f, -9)));
+  const int m = (int)((r / ldexpf(1.0f, ex) - 1.0f) * 8.0f);
+  return (uint8_t)(sign | ((ex + 7) << 3) | m);
+}
+
+float oracle_e4m3_to_f32(uint8_t b) {
+  const int s = b >> 7, ex = (b >> 3) & 15, m = b & 7;
+  float v;
+  if (ex == 15 && m == 7) return NAN;
+  if (ex == 0)
+    v = ldexpf((float)m, -9);
+  else
+    v = ldexpf(1.0f + (float)m / 8.0f, ex - 7);
+  return s ? -v : v;
+}
+
+/* NRCInputEncode's 64 features in fp32, before any rounding (the values
+ * oracle_encode rounds to 16 bits). */
+void oracle_encode_f32(const float* records, int64_t n, float* feats) {
+  for (int64_t i = 0; i < n; ++i) {
+    const float* r = records + ORACLE_IN_FLOATS * i;
+    float* f = feats + 64 * i;
+    for (int c = 0; c < 3; ++c) {
+      float scale = 1.0f;
+      for (int k = 0; k < 12; ++k, scale *= 2.0f) f[12 * c + k] = tri(r[c] * scale);
+    }
+    oneblob4(r[3], f + 36);
+    oneblob4(r[4], f + 40);
+    oneblob4(r[5], f + 44);
+    oneblob4(r[6], f + 48);
+    oneblob4(1.0f - oracle_expf(-r[7]), f + 52);
+    for (int c = 0; c < 6; ++c) f[56 + c] = r[8 + c];
+    f[62] = 1.0f;
+    f[63] = 1.0f;
+  }
+}
+
+/* The FP8 scales and E4M3 weights of the GPU's refresh (csrc/nrc_fp8.cu) from
+ * 16-bit rendering weights w16 (format fmt) and the activation maxima seen
+ * (0 = not seen: bounded from the previous layer). state: s_w[6], s_x[6],
+ * c[6], 1/s_x[0], 448/max|W|[6]. w8: NRC_PARAM_COUNT bytes, parameter layout. */
+void oracle_fp8_quantize(const uint16_t* w16, int fmt, const float seen[6], float* state, uint8_t* w8) {
+  float amax_w[6] = {0}, rowsum[6] = {0};
+  for (int row = 0; row < 323; ++row) {
+    const int l = row < 320 ? row / 64 : 5;
+    float s[32];
+    for (int k = 0; k < 32; ++k) {
+      const float a = fabsf(from16(w16[row * 64 + k], fmt)), b = fabsf(from16(w16[row * 64 + 32 + k], fmt));
+      s[k] = a + b;
+      const float m = a > b ? a : b;
+      if (m > amax_w[l]) amax_w[l] = m;
+    }
+    for (int off = 16; off > 0; off >>= 1) { /* the GPU's butterfly: every lane ends with the same sum */
+      float t[32];
+      for (int k = 0; k < 32; ++k) t[k] = s[k] + s[k ^ off];
+      memcpy(s, t, sizeof(t));
+    }
+    if (s[0] > rowsum[l]) rowsum[l] = s[0];
+  }
+  float ax[6], *sw = state, *sx = state + 6, *c = state + 12, *invw = state + 19;
+  for (int l = 0; l < 6; ++l) {
+    const float bound = l == 0 ? 1.0f : ax[l - 1] * rowsum[l - 1];
+    ax[l] = seen[l] > 0.0f ? seen[l] : bound;
+    if (!(ax[l] > 0.0f)) ax[l] = 1.0f;
+    float aw = amax_w[l];
+    if (!(aw > 0.0f)) aw = 1.0f;
+    sw[l] = aw / 448.0f;
+    invw[l] = 448.0f / aw;
+    sx[l] = ax[l] / 448.0f;
+  }
+  for (int l = 0; l < 5; ++l) c[l] = (sw[l] * sx[l]) / sx[l + 1];
+  c[5] = sw[5] * sx[5];
+  state[18] = 1.0f / sx[0];
+  for (int i = 0; i < ORACLE_P; ++i) {
+    const int row = i / 64, l = row < 320 ? row / 64 : 5;
+    w8[i] = oracle_f32_to_e4m3(from16(w16[i], fmt) * invw[l]);
+  }
+}
+
+/* The FP8 query: features x8 = e4m3(f * inv_sx0); per hidden layer z = sum_i
+ * w8 x8 (fp32, input order), x8' = e4m3(relu(z * c[l])); output z * c[5]
+ * (unclamped). */
+typedef struct {
+  const uint8_t* w8;
+  const float* c;
+  float inv_sx0;
+  const float* feats;
+  float* out;
+} fp8_ctx;
+
+static void fp8_range(void* p, int64_t b, int64_t e, int tid) {
+  (void)tid;
+  fp8_ctx* x = (fp8_ctx*)p;
+  for (int64_t r = b; r < e; ++r) {
+    float a[64], z[64];
+    for (int i = 0; i < 64; ++i) a[i] = oracle_e4m3_to_f32(oracle_f32_to_e4m3(x->feats[64 * r + i] * x->inv_sx0));
+    for (int l = 0; l < 5; ++l) {
+      for (int o = 0; o < 64; ++o) {
+        float s = 0.0f;
+        for (int i = 0; i < 64; ++i) s += oracle_e4m3_to_f32(x->w8[l * 4096 + o * 64 + i]) * a[i];
+        z[o] = s;
+      }
+      for (int o = 0; o < 64; ++o) {
+        const float y = z[o] * x->c[l];
+        a[o] = oracle_e4m3_to_f32(oracle_f32_to_e4m3(y > 0.0f ? y : 0.0f));
+      }
+    }
+    for (int k = 0; k < 3; ++k) {
+      float s = 0.0f;
+      for (int i = 0; i < 64; ++i) s += oracle_e4m3_to_f32(x->w8[5 * 4096 + k * 64 + i]) * a[i];
+      x->out[3 * r + k] = s * x->c[5];
+    }
+  }
+}
+
+void oracle_forward_fp8(const uint8_t* w8, const float c[6], float inv_sx0, const float* feats, int64_t n, float* out,
+                        int nthreads) {
+  fp8_ctx x = {w8, c, inv_sx0, feats, out};
+  parallel_for(n, nthreads, fp8_range, &x);
+}

@@ -100,6 +100,15 @@ void oracle_forward_f64_fmt(const uint16_t* w, const uint16_t* enc, int64_t n, d
 void oracle_train_grad_fmt(const uint16_t* w, const uint16_t* enc, const float* target, int64_t n, float loss_scale,
                            int mode, double* grad, double* grad_abs, double* loss_sum, int nthreads, int fmt);
 
+/* FP8 (E4M3) query form: conversions, fp32 features, the scales and E4M3
+ * weights of the GPU's refresh, and the FP8 forward (see nrc_oracle.c). */
+uint8_t oracle_f32_to_e4m3(float x);
+float oracle_e4m3_to_f32(uint8_t b);
+void oracle_encode_f32(const float* records, int64_t n, float* feats);
+void oracle_fp8_quantize(const uint16_t* w16, int fmt, const float seen[6], float* state, uint8_t* w8);
+void oracle_forward_fp8(const uint8_t* w8, const float c[6], float inv_sx0, const float* feats, int64_t n, float* out,
+                        int nthreads);
+
 /* Scene buffers for oracle_unpack, the host mirror of nrc_scene (include/nrc.h);
  * pointers are host pointers. */
 typedef struct oracle_material {

@@ -49,6 +49,13 @@ def lib() -> ctypes.CDLL:
         _lib.oracle_adam.argtypes = [vp, vp, ctypes.c_uint32, vp, vp, vp, vp, i32]
         _lib.oracle_screen.argtypes = [vp, vp, ctypes.c_uint32, ctypes.c_uint32, i32, ctypes.c_uint32, vp, vp]
         _lib.oracle_unpack.argtypes = [vp, vp, i64, i64, vp, i64]
+        _lib.oracle_f32_to_e4m3.argtypes = [f32]
+        _lib.oracle_f32_to_e4m3.restype = ctypes.c_uint8
+        _lib.oracle_e4m3_to_f32.argtypes = [ctypes.c_uint8]
+        _lib.oracle_e4m3_to_f32.restype = f32
+        _lib.oracle_encode_f32.argtypes = [vp, i64, vp]
+        _lib.oracle_fp8_quantize.argtypes = [vp, i32, vp, vp, vp]
+        _lib.oracle_forward_fp8.argtypes = [vp, vp, f32, vp, i64, vp, i32]
         _lib.oracle_expf.argtypes = [f32]
         _lib.oracle_expf.restype = f32
     return _lib
@@ -205,6 +212,44 @@ def unpack(sc: dict, packed_words: np.ndarray, first_word: int = 0) -> np.ndarra
     base = w[:, first_word:]
     lib().oracle_unpack(ctypes.byref(S), _p(np.ascontiguousarray(base)) if first_word else _p(w), n,
                         base.shape[1] if first_word else w.shape[1], _p(out), 14)
+    return out
+
+
+def encode_f32(records: np.ndarray) -> np.ndarray:
+    """records (n, 14) -> (n, 64) float32 features before any rounding."""
+    r = _c(records, np.float32).reshape(-1, 14)
+    out = np.empty((r.shape[0], 64), np.float32)
+    lib().oracle_encode_f32(_p(r), r.shape[0], _p(out))
+    return out
+
+
+def e4m3(x) -> np.ndarray:
+    """float32 array -> E4M3 bytes (round to nearest even, saturated)."""
+    x = np.asarray(x, np.float32).ravel()
+    return np.array([lib().oracle_f32_to_e4m3(float(v)) for v in x], np.uint8)
+
+
+def e4m3_decode(b) -> np.ndarray:
+    b = np.asarray(b, np.uint8).ravel()
+    return np.array([lib().oracle_e4m3_to_f32(int(v)) for v in b], np.float32)
+
+
+def fp8_quantize(w16: np.ndarray, fmt: int = 0, seen=None):
+    """The FP8 refresh: returns (w8 (P,) uint8, state (25,) float32: s_w[6],
+    s_x[6], c[6], 1/s_x[0], 448/max|W|[6])."""
+    w = _c(w16, np.uint16)
+    sn = _c(np.zeros(6) if seen is None else seen, np.float32)
+    st = np.empty(25, np.float32)
+    w8 = np.empty(P, np.uint8)
+    lib().oracle_fp8_quantize(_p(w), fmt, _p(sn), _p(st), _p(w8))
+    return w8, st
+
+
+def forward_fp8(w8: np.ndarray, c, inv_sx0: float, feats: np.ndarray, nthreads: int = 1) -> np.ndarray:
+    f = _c(feats, np.float32).reshape(-1, 64)
+    cc = _c(c, np.float32)
+    out = np.empty((f.shape[0], 3), np.float32)
+    lib().oracle_forward_fp8(_p(_c(w8, np.uint8)), _p(cc), float(inv_sx0), _p(f), f.shape[0], _p(out), nthreads)
     return out
 
 

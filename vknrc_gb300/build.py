@@ -17,7 +17,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libnrc.so")
-SOURCES = ["nrc_api.cu", "nrc_infer.cu", "nrc_train.cu", "nrc_encode.cu", "nrc_noalloc.cu", "nrc_server.cu", "nrc_screen.cu", "nrc_unpack.cu"]
+SOURCES = ["nrc_api.cu", "nrc_infer.cu", "nrc_train.cu", "nrc_encode.cu", "nrc_noalloc.cu", "nrc_server.cu", "nrc_screen.cu", "nrc_unpack.cu", "nrc_fp8.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibility=hidden", "-I", os.path.join(ROOT, "include")]
 

@@ -30,6 +30,10 @@ struct nrc_context {
   unsigned long long* loss_count = nullptr;
   CUtensorMap map_w16;    // TMA views of the two fp16 weight vectors
   CUtensorMap map_use16;
+  bool fp8 = false;       // FP8 query form on: activation absmax gathered, E4M3 copy refreshed
+  uint8_t* w8 = nullptr;  // E4M3 rendering weights, 323 rows x 128 bytes (bytes 64..127 zero)
+  nrc::Fp8State* fp8s = nullptr;
+  CUtensorMap map_w8;
 };
 
 namespace nrc {
@@ -57,10 +61,12 @@ cudaError_t make_weight_map(CUtensorMap* map, const void* w16) {
 
 size_t context_device_bytes(const nrc_context* c) { return c->block_bytes; }
 
+constexpr size_t kW8Bytes = size_t(kWeightRows) * 128;
+
 size_t context_device_bytes_for(int num_sms) {
   auto up = [](size_t x) { return (x + 255) & ~size_t(255); };
   return 2 * up(kParams * 2) + up(kParams * sizeof(nrc_optimizer_entry)) + up(sizeof(nrc_optimizer_state)) + 512 +
-         up(size_t(num_sms) * kParams * sizeof(float));
+         up(kW8Bytes) + up(sizeof(Fp8State)) + up(size_t(num_sms) * kParams * sizeof(float));
 }
 
 }  // namespace nrc
@@ -136,6 +142,14 @@ int upload_init(nrc_context* c, uint64_t seed) {
     return from_cuda(e);
   if ((e = cudaMemcpy(c->state, &st, sizeof(st), cudaMemcpyHostToDevice)) != cudaSuccess) return from_cuda(e);
   return NRC_OK;
+}
+
+// The FP8 query form's refresh after the rendering weights changed: re-quantize
+// (and recompute the scales when forced or in a new 16-step epoch).
+int fp8_refresh(nrc_context* c, int force, cudaStream_t stream) {
+  if (!c->fp8) return NRC_OK;
+  return from_cuda(nrc::launch_fp8_refresh(reinterpret_cast<const uint16_t*>(c->use16), c->bf16, c->state, c->fp8s,
+                                           c->w8, force, stream));
 }
 
 int check_ctx(nrc_context* c) {
@@ -220,7 +234,9 @@ int nrc_create(const nrc_config* cfg_in, nrc_context** out) {
   const size_t o_st = o_ent + up256(kParams * sizeof(nrc_optimizer_entry));
   const size_t o_err = o_st + up256(sizeof(nrc_optimizer_state));
   const size_t o_loss = o_err + 256;
-  const size_t o_part = o_loss + 256;
+  const size_t o_w8 = o_loss + 256;
+  const size_t o_fp8 = o_w8 + up256(nrc::kW8Bytes);
+  const size_t o_part = o_fp8 + up256(sizeof(nrc::Fp8State));
   const size_t part_bytes = up256(size_t(c->num_sms) * kParams * sizeof(float));
   const size_t total = o_part + part_bytes;
   if ((e = cudaMalloc(&c->block, total)) != cudaSuccess) {
@@ -238,14 +254,20 @@ int nrc_create(const nrc_config* cfg_in, nrc_context** out) {
   c->loss_count = reinterpret_cast<unsigned long long*>(b + o_loss + 8);
   c->sync = reinterpret_cast<uint32_t*>(b + o_err + 64);
   c->partials = reinterpret_cast<float*>(b + o_part);
+  c->w8 = b + o_w8;
+  c->fp8s = reinterpret_cast<nrc::Fp8State*>(b + o_fp8);
+  c->fp8 = cfg.fp8_inference != 0;
   if ((e = nrc::make_weight_map(&c->map_w16, c->w16)) != cudaSuccess ||
       (e = nrc::make_weight_map(&c->map_use16, c->use16)) != cudaSuccess ||
-      (e = cudaMemset(c->err, 0, 256 + 256)) != cudaSuccess) {
+      (e = nrc::make_weight_map(&c->map_w8, c->w8)) != cudaSuccess ||  // same geometry: 128-byte rows
+      (e = cudaMemset(c->err, 0, 256 + 256)) != cudaSuccess ||
+      (e = cudaMemset(c->w8, 0, o_part - o_w8)) != cudaSuccess) {
     cudaFree(c->block);
     delete c;
     return from_cuda(e);
   }
   s = upload_init(c, cfg.seed);
+  if (s == NRC_OK) s = fp8_refresh(c, 1, nullptr);
   if (s == NRC_OK) s = from_cuda(cudaDeviceSynchronize());
   if (s != NRC_OK) {
     cudaFree(c->block);
@@ -274,6 +296,7 @@ int nrc_reset(nrc_context* c, uint64_t seed) {
   cudaDeviceSynchronize();
   c->cfg.seed = seed;
   s = upload_init(c, seed);
+  if (s == NRC_OK) s = fp8_refresh(c, 1, nullptr);
   if (s == NRC_OK) s = from_cuda(cudaDeviceSynchronize());
   return s;
 }
@@ -402,6 +425,7 @@ static nrc::TrainParams train_params(nrc_context* c, int steps, int mode) {
   p.loss_count = (g.track_loss && mode == nrc::kTrainStep) ? c->loss_count : nullptr;
   p.err = c->err;
   p.bf16 = c->bf16 ? 1 : 0;
+  p.amax = (c->fp8 && mode == nrc::kTrainStep) ? c->fp8s->amax_x : nullptr;
   return p;
 }
 
@@ -413,7 +437,8 @@ int nrc_train(nrc_context* c, const nrc_train_record* rec, uint32_t* d_count, ui
   if (rec != nullptr && !aligned16(rec)) return NRC_ERROR_MISALIGNED;
   nrc::TrainParams p = train_params(c, 1, nrc::kTrainStep);
   p.batch[0] = nrc::TrainBatch{rec, d_count, capacity, write_use_weights != 0};
-  return from_cuda(nrc::launch_train(p, &c->map_w16, c->num_sms, static_cast<cudaStream_t>(stream)));
+  s = from_cuda(nrc::launch_train(p, &c->map_w16, c->num_sms, static_cast<cudaStream_t>(stream)));
+  return s == NRC_OK ? fp8_refresh(c, 0, static_cast<cudaStream_t>(stream)) : s;
 }
 
 int nrc_gradient(nrc_context* c, const nrc_train_record* rec, const uint32_t* d_count, uint32_t capacity,
@@ -443,7 +468,8 @@ int nrc_train_batches(nrc_context* c, const nrc_train_record* const* recs, uint3
   nrc::TrainParams p = train_params(c, nbatches, nrc::kTrainStep);
   for (int b = 0; b < nbatches; ++b)
     p.batch[b] = nrc::TrainBatch{recs[b], counts[b], capacity, (write_use_last != 0 && b == nbatches - 1) ? 1 : 0};
-  return from_cuda(nrc::launch_train(p, &c->map_w16, c->num_sms, static_cast<cudaStream_t>(stream)));
+  s = from_cuda(nrc::launch_train(p, &c->map_w16, c->num_sms, static_cast<cudaStream_t>(stream)));
+  return s == NRC_OK ? fp8_refresh(c, 0, static_cast<cudaStream_t>(stream)) : s;
 }
 
 int nrc_frame(nrc_context* c, const nrc_input* eval_in, const uint32_t* d_eval_count, uint32_t eval_capacity,
@@ -704,8 +730,51 @@ int nrc_train_many(const nrc_train_job* jobs, uint32_t n, const uint32_t* ctas, 
     }
     const cudaError_t e = nrc::launch_train_many(tj.data(), static_cast<int>(m), g, static_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return from_cuda(e);
+    for (uint32_t j = 0; j < m; ++j)
+      if ((s = fp8_refresh(kept[j].ctx, 0, static_cast<cudaStream_t>(stream))) != NRC_OK) return s;
   }
   return NRC_OK;
+}
+
+// ------------------------------------------------------------------- fp8 --
+int nrc_infer_fp8(nrc_context* c, const nrc_input* in, const uint32_t* d_count, uint32_t capacity, float* out,
+                  void* stream) {
+  int s = check_ctx(c);
+  if (s != NRC_OK) return s;
+  if (!c->fp8) return NRC_ERROR_INVALID_ARGUMENT;  // created without fp8_inference
+  if (capacity == 0) return NRC_OK;
+  if (in == nullptr || d_count == nullptr || out == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  if (!aligned16(in) || (reinterpret_cast<uintptr_t>(out) & 3u)) return NRC_ERROR_MISALIGNED;
+  return from_cuda(nrc::launch_infer_fp8(in, d_count, capacity, &c->map_w8, c->fp8s, out, c->err, c->num_sms,
+                                         static_cast<cudaStream_t>(stream)));
+}
+
+int nrc_fp8_refresh(nrc_context* c, void* stream) {
+  int s = check_ctx(c);
+  if (s != NRC_OK) return s;
+  if (!c->fp8) return NRC_ERROR_INVALID_ARGUMENT;
+  return fp8_refresh(c, 1, static_cast<cudaStream_t>(stream));
+}
+
+int nrc_get_fp8(nrc_context* c, uint8_t* host_w8, float* host_scales) {
+  int s = check_ctx(c);
+  if (s != NRC_OK) return s;
+  if (!c->fp8) return NRC_ERROR_INVALID_ARGUMENT;
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess && host_w8)
+    e = cudaMemcpy2D(host_w8, 64, c->w8, 128, 64, nrc::kWeightRows, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && host_scales) {
+    nrc::Fp8State st;
+    e = cudaMemcpy(&st, c->fp8s, sizeof(st), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) {
+      std::memcpy(host_scales, st.scale_w, 6 * 4);
+      std::memcpy(host_scales + 6, st.scale_x, 6 * 4);
+      std::memcpy(host_scales + 12, st.c, 6 * 4);
+      host_scales[18] = st.inv_sx0;
+      std::memcpy(host_scales + 19, st.inv_w, 6 * 4);
+    }
+  }
+  return from_cuda(e);
 }
 
 // ---------------------------------------------------------------- unpack --
@@ -854,7 +923,8 @@ int nrc_load_checkpoint(nrc_context* c, const void* blob, size_t bytes) {
   c->cfg.ema_alpha = f[4];
   c->cfg.loss_scale = f[5];
   c->cfg.use_ema_weights = use_ema;
-  return NRC_OK;
+  s = fp8_refresh(c, 1, nullptr);
+  return s == NRC_OK ? from_cuda(cudaDeviceSynchronize()) : s;
 }
 
 int nrc_get_weights(nrc_context* c, int which, uint16_t* host) {
@@ -884,7 +954,9 @@ int nrc_set_weights(nrc_context* c, const uint16_t* host) {
           cudaSuccess &&
       (e = cudaMemcpy(c->w16, host, kParams * 2, cudaMemcpyHostToDevice)) == cudaSuccess)
     e = cudaMemcpy(c->use16, host, kParams * 2, cudaMemcpyHostToDevice);
-  return from_cuda(e);
+  if (e != cudaSuccess) return from_cuda(e);
+  s = fp8_refresh(c, 1, nullptr);
+  return s == NRC_OK ? from_cuda(cudaDeviceSynchronize()) : s;
 }
 
 int nrc_get_optimizer(nrc_context* c, nrc_optimizer_state* st, nrc_optimizer_entry* ent) {

@@ -199,6 +199,39 @@ __device__ __forceinline__ void encode_input(const float (&r)[kInFloats], uint32
   encode_half1<kBF16>(r, e + 16);
 }
 
+// The same features in E4M3 for the FP8 query: feature k, multiplied by inv_s
+// (448 / the features' absmax scale), rounded to nearest even and saturated,
+// in byte k % 4 of word k / 4 (words 0..15 of e).
+__device__ __forceinline__ void encode_input_e4m3(const float (&r)[kInFloats], float inv_s, uint32_t (&e)[32]) {
+  auto q4 = [&](float a, float b, float c, float d) {
+    return pack4_e4m3(__fmul_rn(a, inv_s), __fmul_rn(b, inv_s), __fmul_rn(c, inv_s), __fmul_rn(d, inv_s));
+  };
+  // triangle-wave frequency k of coordinate p (the two forms agree; see enc_tri_h)
+  auto tri = [](float p, int k) {
+    return fabsf(p) < 0x1p100f ? enc_tri_h(p, 0.5f * static_cast<float>(1 << k))
+                               : enc_tri(p, static_cast<float>(1 << k));
+  };
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int w = 0; w < 3; ++w)
+      e[3 * c + w] = q4(tri(r[c], 4 * w), tri(r[c], 4 * w + 1), tri(r[c], 4 * w + 2), tri(r[c], 4 * w + 3));
+  auto blob = [&](float x) {
+    float f0, f1, f2, f3;
+    enc_qcdf_x2(0.0f, 1.0f, x, f0, f1);
+    enc_qcdf_x2(2.0f, 3.0f, x, f2, f3);
+    const float f4 = enc_qcdf(4.0f, x);
+    return q4(__fsub_rn(f1, f0), __fsub_rn(f2, f1), __fsub_rn(f3, f2), __fsub_rn(f4, f3));
+  };
+  e[9] = blob(r[3]);
+  e[10] = blob(r[4]);
+  e[11] = blob(r[5]);
+  e[12] = blob(r[6]);
+  e[13] = blob(__fsub_rn(1.0f, enc_expf(-r[7])));
+  e[14] = q4(r[8], r[9], r[10], r[11]);
+  e[15] = q4(r[12], r[13], 1.0f, 1.0f);
+}
+
 // Device-side error word bits (read back by nrc_get_error).
 constexpr uint32_t kErrTimeout = 1u;
 

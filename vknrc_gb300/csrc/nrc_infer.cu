@@ -105,9 +105,14 @@ __device__ __forceinline__ void scatter_query(const QueryOut& Q, uint32_t dst, f
 // plain query path is compiled without the destination load and epilogue.
 // One launch serves up to N caches: CTAs [group_start[j], group_start[j+1])
 // answer cache j's queries with its weights; with N = 1 the group is the grid.
-// kBF16: weights, features and activations in bf16 instead of fp16.
-template <bool kEncoded, bool kScatter, int N, bool kBF16>
+// kFmt: operand format of weights, features and activations: 0 fp16 (the
+// reference's), 1 bf16, 2 E4M3 (the FP8 query: two K = 32 MMAs per layer, each
+// layer's fp32 sum multiplied by its scale constant before the ReLU and the
+// conversion; the weights keep the 128-byte rows of the 16-bit layout, K bytes
+// 64..127 being zero and never read).
+template <bool kEncoded, bool kScatter, int N, int kFmt>
 __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_constant__ InferLaunch<N> L) {
+  constexpr bool kBF16 = kFmt == 1, kF8 = kFmt == 2;
   int job = 0;
   while (job + 1 < L.njobs && blockIdx.x >= L.group_start[job + 1]) ++job;
   const InferJob& J = L.job[job];
@@ -142,6 +147,7 @@ __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_co
   griddep_wait();
   griddep_launch_dependents();
   const uint32_t n = min(*J.d_count, J.capacity);
+  const float inv_sx0 = kF8 ? J.fp8->inv_sx0 : 1.0f;  // written by the preceding refresh launch
   const uint32_t num_tiles = (n + kTile - 1) / kTile;
   if (warp == 0) {
     tmem_alloc(tmem_slot, 512);
@@ -205,7 +211,11 @@ __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_co
       }
       // the stage may be refilled once all 128 threads have read it
       mbar_arrive(&B.rec_empty[b]);
-      encode_input<kBF16>(r, e);
+      if (kF8) {
+        encode_input_e4m3(r, inv_sx0, e);
+      } else {
+        encode_input<kBF16>(r, e);
+      }
       if (leader && tile_of(it + 2) < num_tiles) {
         if (!mbar_wait(&B.rec_empty[b], (it >> 1) & 1, kWaitLimitNs))
           atomicOr(err, kErrTimeout);
@@ -230,8 +240,12 @@ __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_co
       }
     }
     __syncwarp();  // reconverge before the warp-collective TMEM store
-    // layer-0 A operand: fp16 features, column pair (2j, 2j+1) in word j
-    tmem_st32(a_col + lane_off, e);
+    // layer-0 A operand: 16-bit features, column pair (2j, 2j+1) in word j, or
+    // E4M3 features 4j..4j+3 in word j
+    if (kF8)
+      tmem_st16(a_col + lane_off, e);
+    else
+      tmem_st32(a_col + lane_off, e);
     tc_fence_before();
     mbar_arrive(&B.a_ready);
 #pragma unroll 1
@@ -242,7 +256,13 @@ __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_co
           ph_a ^= 1u;  // counts issued layers; ph_d counts observed completions
           tc_fence_after();
           if (elect_one()) {
-            issue_layer(d_col, a_col, wdesc + static_cast<uint64_t>(l * 512), l < 5 ? id64 : id16);
+            const uint64_t wl = wdesc + static_cast<uint64_t>(l * 512);
+            if (kF8) {
+              mma_ts_f8(d_col, a_col + 0, wl + 0, l < 5 ? id64 : id16, 0u);
+              mma_ts_f8(d_col, a_col + 8, wl + 2, l < 5 ? id64 : id16, 1u);
+            } else {
+              issue_layer(d_col, a_col, wl, l < 5 ? id64 : id16);
+            }
             mma_commit(&B.d_ready);
           }
           __syncwarp();
@@ -250,11 +270,27 @@ __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_co
       }
       // load the destination word while the output layer's MMAs run
       if (kScatter && l == 5 && row < static_cast<int>(rows_valid)) qdst = __ldg(Q.dst + grow);
+      const float cl = kF8 ? J.fp8->c[l] : 1.0f;  // the layer's scale constant (FP8 query)
       ok = ok && warp_all(mbar_wait(&B.d_ready, ph_d, kWaitLimitNs));
       if (!ok) break;
       ph_d ^= 1u;
       tc_fence_after();
-      if (l < 5) {
+      if (kF8 && l < 5) {
+        uint32_t v[32], p[16];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          tmem_ld32(d_col + lane_off + 32 * h, v);
+#pragma unroll
+          for (int j = 0; j < 8; ++j)
+            p[8 * h + j] = pack4_relu_e4m3(__fmul_rn(__uint_as_float(v[4 * j]), cl),
+                                           __fmul_rn(__uint_as_float(v[4 * j + 1]), cl),
+                                           __fmul_rn(__uint_as_float(v[4 * j + 2]), cl),
+                                           __fmul_rn(__uint_as_float(v[4 * j + 3]), cl));
+        }
+        tmem_st16(a_col + lane_off, p);
+        tc_fence_before();
+        mbar_arrive(&B.a_ready);
+      } else if (l < 5) {
         uint32_t v[32], p[32];
         tmem_ld32(d_col + lane_off, v);
 #pragma unroll
@@ -274,7 +310,7 @@ __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_co
             float* dst = Q.out + grow * 3;
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-              const float v = __uint_as_float(o4[c]);
+              const float v = kF8 ? __fmul_rn(__uint_as_float(o4[c]), cl) : __uint_as_float(o4[c]);
               dst[c] = Q.clamp ? fmaxf(v, 0.0f) : v;
             }
           }
@@ -297,7 +333,7 @@ __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_co
   }
 }
 
-template <bool kEncoded, bool kScatter, int N, bool kBF16>
+template <bool kEncoded, bool kScatter, int N, int kFmt>
 cudaError_t launch(const InferLaunch<N>& L, uint32_t grid, cudaStream_t stream) {
   cudaLaunchAttribute attr;
   attr.id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -309,25 +345,26 @@ cudaError_t launch(const InferLaunch<N>& L, uint32_t grid, cudaStream_t stream) 
   cfg.stream = stream;
   cfg.attrs = &attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, infer_kernel<kEncoded, kScatter, N, kBF16>, L);
+  return cudaLaunchKernelEx(&cfg, infer_kernel<kEncoded, kScatter, N, kFmt>, L);
 }
 
-template <bool kEncoded, bool kScatter, int N, bool kBF16>
+template <bool kEncoded, bool kScatter, int N, int kFmt>
 cudaError_t set_smem() {
-  return cudaFuncSetAttribute(infer_kernel<kEncoded, kScatter, N, kBF16>,
+  return cudaFuncSetAttribute(infer_kernel<kEncoded, kScatter, N, kFmt>,
                               cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
 }
 
 }  // namespace
 
 cudaError_t configure_infer_kernels() {
-  cudaError_t e = set_smem<true, false, 1, false>();
-  if (e == cudaSuccess) e = set_smem<false, false, 1, false>();
-  if (e == cudaSuccess) e = set_smem<false, true, 1, false>();
-  if (e == cudaSuccess) e = set_smem<false, false, kMaxInferJobs, false>();
-  if (e == cudaSuccess) e = set_smem<false, false, 1, true>();
-  if (e == cudaSuccess) e = set_smem<false, true, 1, true>();
-  if (e == cudaSuccess) e = set_smem<false, false, kMaxInferJobs, true>();
+  cudaError_t e = set_smem<true, false, 1, 0>();
+  if (e == cudaSuccess) e = set_smem<false, false, 1, 0>();
+  if (e == cudaSuccess) e = set_smem<false, true, 1, 0>();
+  if (e == cudaSuccess) e = set_smem<false, false, kMaxInferJobs, 0>();
+  if (e == cudaSuccess) e = set_smem<false, false, 1, 1>();
+  if (e == cudaSuccess) e = set_smem<false, true, 1, 1>();
+  if (e == cudaSuccess) e = set_smem<false, false, kMaxInferJobs, 1>();
+  if (e == cudaSuccess) e = set_smem<false, false, 1, 2>();
   return e;
 }
 
@@ -356,10 +393,31 @@ cudaError_t launch_infer(const void* input, bool encoded, const uint32_t* d_coun
   L.group_start[0] = 0;
   L.group_start[1] = grid;
   L.njobs = 1;
-  if (encoded) return bf16 ? cudaErrorInvalidValue : launch<true, false, 1, false>(L, grid, stream);
+  if (encoded) return bf16 ? cudaErrorInvalidValue : launch<true, false, 1, 0>(L, grid, stream);
   if (q.dst != nullptr)
-    return bf16 ? launch<false, true, 1, true>(L, grid, stream) : launch<false, true, 1, false>(L, grid, stream);
-  return bf16 ? launch<false, false, 1, true>(L, grid, stream) : launch<false, false, 1, false>(L, grid, stream);
+    return bf16 ? launch<false, true, 1, 1>(L, grid, stream) : launch<false, true, 1, 0>(L, grid, stream);
+  return bf16 ? launch<false, false, 1, 1>(L, grid, stream) : launch<false, false, 1, 0>(L, grid, stream);
+}
+
+cudaError_t launch_infer_fp8(const nrc_input* input, const uint32_t* d_count, uint32_t capacity,
+                             const CUtensorMap* w8map, const Fp8State* fp8, float* out, uint32_t* err, int num_sms,
+                             cudaStream_t stream) {
+  const uint32_t grid = infer_grid(capacity, num_sms);
+  if (grid == 0) return cudaSuccess;
+  InferLaunch<1> L;
+  L.job[0] = InferJob{};
+  L.job[0].wmap = *w8map;
+  L.job[0].input = input;
+  L.job[0].d_count = d_count;
+  L.job[0].capacity = capacity;
+  L.job[0].err = err;
+  L.job[0].q.out = out;
+  L.job[0].q.clamp = 1;
+  L.job[0].fp8 = fp8;
+  L.group_start[0] = 0;
+  L.group_start[1] = grid;
+  L.njobs = 1;
+  return launch<false, false, 1, 2>(L, grid, stream);
 }
 
 cudaError_t launch_infer_many(const InferJob* jobs, int njobs, const uint32_t* group_size, cudaStream_t stream,
@@ -377,8 +435,8 @@ cudaError_t launch_infer_many(const InferJob* jobs, int njobs, const uint32_t* g
   }
   L.group_start[njobs] = grid;
   L.njobs = njobs;
-  return bf16 ? launch<false, false, kMaxInferJobs, true>(L, grid, stream)
-              : launch<false, false, kMaxInferJobs, false>(L, grid, stream);
+  return bf16 ? launch<false, false, kMaxInferJobs, 1>(L, grid, stream)
+              : launch<false, false, kMaxInferJobs, 0>(L, grid, stream);
 }
 
 }  // namespace nrc

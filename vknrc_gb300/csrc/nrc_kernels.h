@@ -9,6 +9,24 @@
 
 namespace nrc {
 
+// FP8 (E4M3) copy of a cache's rendering weights and its per-layer scales
+// (device memory, one per context with fp8 inference on). Layer l's weights are
+// stored as e4m3(w * 448 / absmax_w[l]); its input activations as
+// e4m3(x * 448 / absmax_x[l]); the query multiplies each layer's fp32 sum by
+// c[l] = s_w[l] s_x[l] / s_x[l+1] (the output layer by s_w[5] s_x[5]) with
+// s = absmax / 448.
+struct Fp8State {
+  float scale_w[6];
+  float scale_x[6];
+  float c[6];
+  float inv_sx0;       // 448 / absmax_x[0]: features -> e4m3
+  float inv_w[6];      // 448 / absmax_w[l]
+  uint32_t amax_x[6];  // activation absmax (fp32 bits) seen by training forwards since the last scale update
+  uint32_t epoch;      // t / 16 + 1 at the last scale update (0: never)
+  uint32_t pad[4];
+};
+static_assert(sizeof(Fp8State) == 144, "Fp8State layout");
+
 // Tensor map over an fp16 parameter vector (323 rows x 64, 128-byte swizzle,
 // 64 x 16 boxes) for stage_weights_tma(). Host only; allocates nothing.
 cudaError_t make_weight_map(CUtensorMap* map, const void* w16);
@@ -45,6 +63,7 @@ struct InferJob {
   uint32_t capacity;
   uint32_t* err;
   QueryOut q;
+  const Fp8State* fp8;  // the FP8 query's scales (fp8 launches only)
 };
 
 // Kernel parameters of a query launch over up to N caches; CTAs
@@ -57,6 +76,17 @@ struct InferLaunch {
 };
 
 constexpr int kMaxInferJobs = 32;  // caches per batched query launch
+
+// The FP8 query (E4M3 weights and activations, per-layer scales) of one cache.
+cudaError_t launch_infer_fp8(const nrc_input* input, const uint32_t* d_count, uint32_t capacity,
+                             const CUtensorMap* w8map, const Fp8State* fp8, float* out, uint32_t* err, int num_sms,
+                             cudaStream_t stream);
+// Re-quantizes the fp8 weights from the 16-bit rendering weights; first
+// recomputes the scales when `force` or when the step state has entered a new
+// 16-step epoch since the last update. w8: 323 rows x 128 bytes (bytes 64..127
+// of each row stay zero).
+cudaError_t launch_fp8_refresh(const uint16_t* use16, bool bf16, const nrc_optimizer_state* st, Fp8State* fp8,
+                               uint8_t* w8, int force, cudaStream_t stream);
 
 // CTAs the query kernel uses for `capacity` records on `num_sms` SMs.
 uint32_t infer_grid(uint32_t capacity, int num_sms);
@@ -97,6 +127,7 @@ struct TrainParams {
   unsigned long long* loss_count;
   uint32_t* err;
   int bf16;          // weights and operands in bf16 (host side: selects the kernel)
+  uint32_t* amax;    // Fp8State::amax_x of a cache with fp8 inference, or null
 };
 
 // One cache's share of a training launch: its weight tensor map and parameters.

@@ -169,6 +169,14 @@ __device__ __forceinline__ void drain_dw(uint32_t lane_base, int layer, int q, i
   }
 }
 
+// Warp maximum of a non-negative value, merged into *slot (fp32 bits; non-negative
+// floats order as their bit patterns).
+__device__ __forceinline__ void amax_record(uint32_t* slot, float m) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, off));
+  if ((threadIdx.x & 31) == 0) atomicMax(slot, __float_as_uint(m));
+}
+
 __device__ __forceinline__ uint32_t ld_acquire_gpu(const uint32_t* p) {
   uint32_t v;
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
@@ -393,6 +401,14 @@ __global__ void __launch_bounds__(kTrainThreads, 1) train_steps_kernel(const __g
 #pragma unroll
       for (int k = 0; k < 16; ++k) e[k] = 0u;
     }
+    if (P.amax != nullptr && h == 1) {
+      // largest encoded feature (FP8 query scales): 1 for the frequency and
+      // one-blob features and the constants, else an albedo
+      float m = 1.0f;
+#pragma unroll
+      for (int k = 8; k < 14; ++k) m = fmaxf(m, valid ? fabsf(r[k]) : 0.0f);
+      amax_record(P.amax, m);
+    }
     tmem_st16(a_lane, e);
     store_half(act, row, h, e);
     publish();
@@ -512,6 +528,12 @@ __global__ void __launch_bounds__(kTrainThreads, 1) train_steps_kernel(const __g
             p[j] = pack2_relu<kBF16>(__uint_as_float(v[2 * j]), __uint_as_float(v[2 * j + 1]));
           tmem_st16(a_lane, p);
           store_half(act + (l + 1) * kActBytes, row, h, p);
+          if (P.amax != nullptr) {  // largest input of layer l + 1 (FP8 query scales)
+            float m = 0.0f;
+#pragma unroll
+            for (int j = 0; j < 32; ++j) m = fmaxf(m, __uint_as_float(v[j]));
+            amax_record(P.amax + l + 1, m);
+          }
           publish();
         }
         if (!ok) break;

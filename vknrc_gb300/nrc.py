@@ -34,7 +34,7 @@ EXPORTS = [
     "nrc_server_create", "nrc_server_destroy", "nrc_server_open_session", "nrc_server_close_session",
     "nrc_server_frame_buffers", "nrc_server_session_cache", "nrc_server_submit", "nrc_server_wait",
     "nrc_server_get_stats", "nrc_screen", "nrc_checkpoint_bytes", "nrc_save_checkpoint", "nrc_load_checkpoint",
-    "nrc_unpack_eval", "nrc_unpack_train",
+    "nrc_unpack_eval", "nrc_unpack_train", "nrc_infer_fp8", "nrc_fp8_refresh", "nrc_get_fp8",
 ]
 
 
@@ -49,7 +49,8 @@ class Config(ctypes.Structure):
                 ("beta1", ctypes.c_float), ("beta2", ctypes.c_float), ("epsilon", ctypes.c_float),
                 ("ema_alpha", ctypes.c_float), ("loss_scale", ctypes.c_float),
                 ("use_ema_weights", ctypes.c_uint32), ("deterministic", ctypes.c_uint32),
-                ("track_loss", ctypes.c_uint32), ("seed", ctypes.c_uint64), ("precision", ctypes.c_uint32)]
+                ("track_loss", ctypes.c_uint32), ("seed", ctypes.c_uint64), ("precision", ctypes.c_uint32),
+                ("fp8_inference", ctypes.c_uint32)]
 
 
 PRECISION_FP16, PRECISION_BF16 = 0, 1
@@ -186,6 +187,9 @@ def lib(build_if_missing: bool = True) -> ctypes.CDLL:
     L.nrc_server_wait.argtypes = [vp, u64, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]
     L.nrc_server_get_stats.argtypes = [vp, ctypes.POINTER(ServerStats), i32]
     L.nrc_screen.argtypes = [vp, vp, u32, u32, i32, u32, vp, vp, vp]
+    L.nrc_infer_fp8.argtypes = [vp, vp, vp, u32, vp, vp]
+    L.nrc_fp8_refresh.argtypes = [vp, vp]
+    L.nrc_get_fp8.argtypes = [vp, vp, vp]
     L.nrc_unpack_eval.argtypes = [ctypes.POINTER(SceneStruct), vp, vp, u32, vp, vp, vp]
     L.nrc_unpack_train.argtypes = [ctypes.POINTER(SceneStruct), vp, vp, u32, vp, vp]
     L.nrc_checkpoint_bytes.restype = ctypes.c_size_t
@@ -346,6 +350,22 @@ class Cache:
 
     def error(self) -> int:
         return lib().nrc_get_error(self.h)
+
+    def infer_fp8(self, inputs, count, out, capacity=None, stream=None):
+        cap = inputs.shape[0] if capacity is None else capacity
+        check(lib().nrc_infer_fp8(self.h, _ptr(inputs), _ptr(count), cap, _ptr(out), _stream(stream)),
+              "nrc_infer_fp8")
+
+    def fp8_refresh(self, stream=None):
+        check(lib().nrc_fp8_refresh(self.h, _stream(stream)), "nrc_fp8_refresh")
+
+    def get_fp8(self):
+        """(w8 (P,) uint8 E4M3 bytes, scales dict)."""
+        w8 = np.empty(P, np.uint8)
+        sc = np.empty(25, np.float32)
+        check(lib().nrc_get_fp8(self.h, w8.ctypes.data_as(ctypes.c_void_p), sc.ctypes.data_as(ctypes.c_void_p)),
+              "nrc_get_fp8")
+        return w8, {"scale_w": sc[0:6], "scale_x": sc[6:12], "c": sc[12:18], "inv_sx0": sc[18], "inv_w": sc[19:25]}
 
     def save_checkpoint(self) -> bytes:
         n = lib().nrc_checkpoint_bytes()
