@@ -34,6 +34,10 @@ struct nrc_context {
   uint8_t* w8 = nullptr;  // E4M3 rendering weights, 323 rows x 128 bytes (bytes 64..127 zero)
   nrc::Fp8State* fp8s = nullptr;
   CUtensorMap map_w8;
+  __half* use_next = nullptr;   // the overlapped frame's training writes use_weights here first
+  cudaStream_t side = nullptr;  // the overlapped frame's training stream
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  nrc_frame_plan plan = {0u, 0u};  // the overlapped frame's split (0, 0: default)
 };
 
 namespace nrc {
@@ -65,7 +69,7 @@ constexpr size_t kW8Bytes = size_t(kWeightRows) * 128;
 
 size_t context_device_bytes_for(int num_sms) {
   auto up = [](size_t x) { return (x + 255) & ~size_t(255); };
-  return 2 * up(kParams * 2) + up(kParams * sizeof(nrc_optimizer_entry)) + up(sizeof(nrc_optimizer_state)) + 512 +
+  return 3 * up(kParams * 2) + up(kParams * sizeof(nrc_optimizer_entry)) + up(sizeof(nrc_optimizer_state)) + 512 +
          up(kW8Bytes) + up(sizeof(Fp8State)) + up(size_t(num_sms) * kParams * sizeof(float));
 }
 
@@ -230,7 +234,8 @@ int nrc_create(const nrc_config* cfg_in, nrc_context** out) {
   c->num_sms = prop.multiProcessorCount;
   const size_t o_w16 = 0;
   const size_t o_use = o_w16 + up256(kParams * 2);
-  const size_t o_ent = o_use + up256(kParams * 2);
+  const size_t o_use2 = o_use + up256(kParams * 2);
+  const size_t o_ent = o_use2 + up256(kParams * 2);
   const size_t o_st = o_ent + up256(kParams * sizeof(nrc_optimizer_entry));
   const size_t o_err = o_st + up256(sizeof(nrc_optimizer_state));
   const size_t o_loss = o_err + 256;
@@ -247,6 +252,7 @@ int nrc_create(const nrc_config* cfg_in, nrc_context** out) {
   uint8_t* b = static_cast<uint8_t*>(c->block);
   c->w16 = reinterpret_cast<__half*>(b + o_w16);
   c->use16 = reinterpret_cast<__half*>(b + o_use);
+  c->use_next = reinterpret_cast<__half*>(b + o_use2);
   c->entries = reinterpret_cast<nrc_optimizer_entry*>(b + o_ent);
   c->state = reinterpret_cast<nrc_optimizer_state*>(b + o_st);
   c->err = reinterpret_cast<uint32_t*>(b + o_err);
@@ -285,6 +291,9 @@ int nrc_destroy(nrc_context* c) {
   if (dev != c->device) cudaSetDevice(c->device);
   cudaDeviceSynchronize();
   cudaFree(c->block);
+  if (c->side) cudaStreamDestroy(c->side);
+  if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+  if (c->ev_join) cudaEventDestroy(c->ev_join);
   if (dev >= 0 && dev != c->device) cudaSetDevice(dev);
   delete c;
   return NRC_OK;
@@ -481,6 +490,128 @@ int nrc_frame(nrc_context* c, const nrc_input* eval_in, const uint32_t* d_eval_c
   s = nrc_infer(c, eval_in, d_eval_count, eval_capacity, out, NRC_WEIGHTS_USE, stream);
   if (s != NRC_OK) return s;
   return nrc_train_batches(c, train_rec, train_counts, train_capacity, NRC_TRAIN_BATCH_COUNT, 1, stream);
+}
+
+int nrc_frame_overlapped(nrc_context* c, const nrc_input* eval_in, const uint32_t* d_eval_count, uint32_t eval_capacity,
+                         float* out, const nrc_train_record* const* train_rec, uint32_t* const* train_counts,
+                         uint32_t train_capacity, const nrc_frame_plan* plan_in, void* query_event, void* stream) {
+  int s = check_ctx(c);
+  if (s != NRC_OK) return s;
+  if (train_rec == nullptr || train_counts == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  for (int b = 0; b < NRC_TRAIN_BATCH_COUNT; ++b) {
+    if (train_counts[b] == nullptr || (train_capacity > 0 && train_rec[b] == nullptr)) return NRC_ERROR_INVALID_ARGUMENT;
+    if (train_rec[b] != nullptr && !aligned16(train_rec[b])) return NRC_ERROR_MISALIGNED;
+  }
+  if (eval_capacity > 0) {
+    if (eval_in == nullptr || d_eval_count == nullptr || out == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+    if (!aligned16(eval_in) || (reinterpret_cast<uintptr_t>(out) & 3u)) return NRC_ERROR_MISALIGNED;
+  }
+  nrc_frame_plan plan = plan_in ? *plan_in : c->plan;
+  if (plan_in == nullptr && plan.query_ctas == 0 && plan.train_ctas == 0) {
+    plan.train_ctas = static_cast<uint32_t>(c->num_sms) / 4;  // default split before any tuning
+    plan.query_ctas = static_cast<uint32_t>(c->num_sms) - plan.train_ctas;
+  }
+  const bool sequential = plan.train_ctas == 0;
+  if (!sequential && (plan.query_ctas == 0 || plan.query_ctas + plan.train_ctas > static_cast<uint32_t>(c->num_sms) ||
+                      plan.train_ctas > nrc::train_grid(nrc::TrainParams{}, c->num_sms)))
+    return NRC_ERROR_INVALID_ARGUMENT;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (!sequential && c->side == nullptr) {
+    if (cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess)
+      return NRC_ERROR_CUDA;
+  }
+  cudaStream_t ts = sequential ? st : c->side;
+  cudaError_t e = cudaSuccess;
+  if (!sequential) {
+    if ((e = cudaEventRecord(c->ev_fork, st)) != cudaSuccess || (e = cudaStreamWaitEvent(ts, c->ev_fork, 0)) != cudaSuccess)
+      return from_cuda(e);
+  }
+  // the query reads the current rendering weights ...
+  if (eval_capacity > 0) {
+    nrc::QueryOut q = {};
+    q.out = out;
+    q.clamp = 1;
+    e = nrc::launch_infer(eval_in, false, d_eval_count, eval_capacity, &c->map_use16, q, c->err,
+                          sequential ? c->num_sms : static_cast<int>(plan.query_ctas), st, c->bf16);
+    if (e != cudaSuccess) return from_cuda(e);
+  }
+  if (query_event != nullptr && (e = cudaEventRecord(static_cast<cudaEvent_t>(query_event), st)) != cudaSuccess)
+    return from_cuda(e);
+  // ... while the training writes the next ones beside them, copied in once both are done
+  nrc::TrainParams p = train_params(c, NRC_TRAIN_BATCH_COUNT, nrc::kTrainStep);
+  for (int b = 0; b < NRC_TRAIN_BATCH_COUNT; ++b)
+    p.batch[b] = nrc::TrainBatch{train_rec[b], train_counts[b], train_capacity, b == NRC_TRAIN_BATCH_COUNT - 1 ? 1 : 0};
+  p.use16 = sequential ? c->use16 : c->use_next;
+  e = nrc::launch_train(p, &c->map_w16, sequential ? c->num_sms : static_cast<int>(plan.train_ctas), ts);
+  if (e != cudaSuccess) return from_cuda(e);
+  if (!sequential) {
+    if ((e = cudaEventRecord(c->ev_join, ts)) != cudaSuccess || (e = cudaStreamWaitEvent(st, c->ev_join, 0)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(c->use16, c->use_next, kParams * 2, cudaMemcpyDeviceToDevice, st)) != cudaSuccess)
+      return from_cuda(e);
+  }
+  return fp8_refresh(c, 0, st);
+}
+
+int nrc_autotune_frame(nrc_context* c, const nrc_input* eval_in, const uint32_t* d_eval_count, uint32_t eval_capacity,
+                       float* out, const nrc_train_record* const* train_rec, uint32_t* const* train_counts,
+                       uint32_t train_capacity, nrc_frame_plan* best_out, float* best_ms) {
+  int s = check_ctx(c);
+  if (s != NRC_OK) return s;
+  // a scratch cache with this one's configuration and state: tuning trains it, not this one
+  nrc_context* t = nullptr;
+  if ((s = nrc_create(&c->cfg, &t)) != NRC_OK) return s;
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(t->w16, c->w16, kParams * 2, cudaMemcpyDeviceToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(t->use16, c->use16, kParams * 2, cudaMemcpyDeviceToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(t->entries, c->entries, kParams * sizeof(nrc_optimizer_entry), cudaMemcpyDeviceToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(t->state, c->state, sizeof(nrc_optimizer_state), cudaMemcpyDeviceToDevice);
+  cudaStream_t st = nullptr;
+  cudaEvent_t a = nullptr, b = nullptr;
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreate(&a);
+  if (e == cudaSuccess) e = cudaEventCreate(&b);
+  nrc_frame_plan best = {0u, 0u};
+  float best_t = 1e30f;
+  if (e == cudaSuccess) {
+    // candidates: the sequential frame, then training groups of 8 .. 72 CTAs beside the query
+    std::vector<nrc_frame_plan> cand = {{0u, 0u}};
+    const uint32_t sms = static_cast<uint32_t>(c->num_sms);
+    for (uint32_t tc = 8; tc <= 72 && tc < sms; tc += 8) cand.push_back({sms - tc, tc});
+    for (const nrc_frame_plan& pl : cand) {
+      for (int k = 0; k < 3 && s == NRC_OK; ++k)
+        s = nrc_frame_overlapped(t, eval_in, d_eval_count, eval_capacity, out, train_rec, train_counts,
+                                 train_capacity, &pl, nullptr, st);
+      if (s != NRC_OK) break;
+      const int reps = 10;
+      cudaEventRecord(a, st);
+      for (int k = 0; k < reps && s == NRC_OK; ++k)
+        s = nrc_frame_overlapped(t, eval_in, d_eval_count, eval_capacity, out, train_rec, train_counts,
+                                 train_capacity, &pl, nullptr, st);
+      cudaEventRecord(b, st);
+      if (s != NRC_OK || (e = cudaEventSynchronize(b)) != cudaSuccess) break;
+      float ms = 0.0f;
+      cudaEventElapsedTime(&ms, a, b);
+      ms /= reps;
+      if (ms < best_t) {
+        best_t = ms;
+        best = pl;
+      }
+    }
+  }
+  if (s == NRC_OK && e == cudaSuccess && nrc_get_error(t) != NRC_OK) s = NRC_ERROR_DEVICE_TIMEOUT;
+  if (a) cudaEventDestroy(a);
+  if (b) cudaEventDestroy(b);
+  if (st) cudaStreamDestroy(st);
+  nrc_destroy(t);
+  if (s != NRC_OK) return s;
+  if (e != cudaSuccess) return from_cuda(e);
+  c->plan = best;
+  if (best_out) *best_out = best;
+  if (best_ms) *best_ms = best_t;
+  return NRC_OK;
 }
 
 int nrc_frame_scatter(nrc_context* c, const nrc_input* eval_in, const uint32_t* d_eval_dst,

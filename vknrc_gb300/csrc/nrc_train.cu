@@ -765,7 +765,7 @@ uint32_t train_grid(const TrainParams&, int max_ctas) {
 cudaError_t launch_train(const TrainParams& p, const CUtensorMap* wmap, int max_ctas, cudaStream_t stream) {
   if (p.steps < 1 || p.steps > NRC_TRAIN_BATCH_COUNT) return cudaErrorInvalidValue;
   const uint32_t grid = train_grid(p, max_ctas);
-  if (grid < kMinTrainCtas) return cudaErrorInvalidConfiguration;
+  if (grid < 1) return cudaErrorInvalidConfiguration;
   TrainLaunch<1> L;
   L.job[0].wmap = *wmap;
   L.job[0].p = p;

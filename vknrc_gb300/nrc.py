@@ -35,6 +35,7 @@ EXPORTS = [
     "nrc_server_frame_buffers", "nrc_server_session_cache", "nrc_server_submit", "nrc_server_wait",
     "nrc_server_get_stats", "nrc_screen", "nrc_checkpoint_bytes", "nrc_save_checkpoint", "nrc_load_checkpoint",
     "nrc_unpack_eval", "nrc_unpack_train", "nrc_infer_fp8", "nrc_fp8_refresh", "nrc_get_fp8",
+    "nrc_frame_overlapped", "nrc_autotune_frame",
 ]
 
 
@@ -82,6 +83,11 @@ def scatter_targets(bias_factor_r=None, factor_gb=None, train_records: Sequence 
             t.train_records[b] = _ptr(r)
             t.train_capacity[b] = r.shape[0]
     return t
+
+
+class FramePlan(ctypes.Structure):
+    """nrc_frame_plan: CTAs of the query and of the training in an overlapped frame."""
+    _fields_ = [("query_ctas", ctypes.c_uint32), ("train_ctas", ctypes.c_uint32)]
 
 
 class QueryJob(ctypes.Structure):
@@ -187,6 +193,10 @@ def lib(build_if_missing: bool = True) -> ctypes.CDLL:
     L.nrc_server_wait.argtypes = [vp, u64, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]
     L.nrc_server_get_stats.argtypes = [vp, ctypes.POINTER(ServerStats), i32]
     L.nrc_screen.argtypes = [vp, vp, u32, u32, i32, u32, vp, vp, vp]
+    L.nrc_frame_overlapped.argtypes = [vp, vp, vp, u32, vp, ctypes.POINTER(vp), ctypes.POINTER(vp), u32,
+                                       ctypes.POINTER(FramePlan), vp, vp]
+    L.nrc_autotune_frame.argtypes = [vp, vp, vp, u32, vp, ctypes.POINTER(vp), ctypes.POINTER(vp), u32,
+                                     ctypes.POINTER(FramePlan), ctypes.POINTER(ctypes.c_float)]
     L.nrc_infer_fp8.argtypes = [vp, vp, vp, u32, vp, vp]
     L.nrc_fp8_refresh.argtypes = [vp, vp]
     L.nrc_get_fp8.argtypes = [vp, vp, vp]
@@ -314,6 +324,34 @@ class Cache:
         cnts = (ctypes.c_void_p * TRAIN_BATCH_COUNT)(*[_ptr(c) for c in train_counts])
         check(lib().nrc_frame(self.h, _ptr(eval_inputs), _ptr(eval_count), ecap, _ptr(out), recs, cnts, tcap,
                               _stream(stream)), "nrc_frame")
+
+    def frame_overlapped(self, eval_inputs, eval_count, out, train_records: Sequence, train_counts: Sequence,
+                         plan=None, query_event=None, eval_capacity=None, train_capacity=None, stream=None):
+        """nrc_frame_overlapped; plan = (query_ctas, train_ctas) or None (the tuned / default split);
+        query_event: a torch.cuda.Event recorded when the query results are complete."""
+        ecap = eval_inputs.shape[0] if eval_capacity is None else eval_capacity
+        tcap = train_records[0].shape[0] if train_capacity is None else train_capacity
+        recs = (ctypes.c_void_p * TRAIN_BATCH_COUNT)(*[_ptr(r) for r in train_records])
+        cnts = (ctypes.c_void_p * TRAIN_BATCH_COUNT)(*[_ptr(c) for c in train_counts])
+        pl = ctypes.byref(FramePlan(*plan)) if plan is not None else None
+        ev = None
+        if query_event is not None:
+            if query_event.cuda_event == 0:  # torch creates the CUDA event at its first record
+                query_event.record(stream)
+            ev = query_event.cuda_event
+        check(lib().nrc_frame_overlapped(self.h, _ptr(eval_inputs), _ptr(eval_count), ecap, _ptr(out), recs, cnts,
+                                         tcap, pl, ev, _stream(stream)), "nrc_frame_overlapped")
+
+    def autotune_frame(self, eval_inputs, eval_count, out, train_records: Sequence, train_counts: Sequence):
+        """nrc_autotune_frame: returns ((query_ctas, train_ctas), ms per frame)."""
+        recs = (ctypes.c_void_p * TRAIN_BATCH_COUNT)(*[_ptr(r) for r in train_records])
+        cnts = (ctypes.c_void_p * TRAIN_BATCH_COUNT)(*[_ptr(c) for c in train_counts])
+        best = FramePlan()
+        ms = ctypes.c_float()
+        check(lib().nrc_autotune_frame(self.h, _ptr(eval_inputs), _ptr(eval_count), eval_inputs.shape[0], _ptr(out),
+                                       recs, cnts, train_records[0].shape[0], ctypes.byref(best), ctypes.byref(ms)),
+              "nrc_autotune_frame")
+        return (best.query_ctas, best.train_ctas), ms.value
 
     # -------------------------------------------------------------- state --
     def get_weights(self, which=WEIGHTS_TRAIN) -> np.ndarray:
