@@ -38,7 +38,7 @@ static_assert(kSlots * kSlotCols <= 512, "TMEM columns");
 struct SlotBars {
   uint64_t rec_full[2];   // bulk copy of a record tile landed (tx bytes)
   uint64_t rec_empty[2];  // all 128 threads of the slot finished reading the stage
-  uint64_t a_ready;       // 128 arrivals: A operand in TMEM for the next layer
+  uint64_t a_ready;       // 4 arrivals (one per warp): A operand in TMEM for the next layer
   uint64_t d_ready;       // MMA commit: accumulator ready
 };
 static_assert(sizeof(SlotBars) * kSlots + 16 <= 512, "barrier area (+ weight barrier, TMEM slot)");
@@ -63,6 +63,13 @@ __device__ __forceinline__ void issue_record_tile(const nrc_input* __restrict__ 
 }
 
 __device__ __forceinline__ bool warp_all(bool ok) { return __all_sync(0xffffffffu, ok); }
+
+// One arrival for the whole warp once every lane has reached this point (its
+// TMEM stores complete and fenced before the warp synchronisation).
+__device__ __forceinline__ void arrive_warp(uint64_t* bar) {
+  __syncwarp();
+  if ((threadIdx.x & 31) == 0) mbar_arrive(bar);
+}
 
 // The four K-steps of one layer: D[128 x N] = A[128 x 64] (TMEM) * W^T.
 // bdesc0 addresses the layer's weight tile; each K-step advances 32 bytes
@@ -137,7 +144,7 @@ __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_co
       mbar_init(&bars[s].rec_full[1], 1);
       mbar_init(&bars[s].rec_empty[0], 128);
       mbar_init(&bars[s].rec_empty[1], 128);
-      mbar_init(&bars[s].a_ready, 128);
+      mbar_init(&bars[s].a_ready, 4);
       mbar_init(&bars[s].d_ready, 1);
     }
     mbar_init(w_full, 1);
@@ -247,7 +254,7 @@ __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_co
     else
       tmem_st32(a_col + lane_off, e);
     tc_fence_before();
-    mbar_arrive(&B.a_ready);
+    arrive_warp(&B.a_ready);
 #pragma unroll 1
     for (int l = 0; l < 6; ++l) {
       if (issuer) {
@@ -289,19 +296,16 @@ __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_co
         }
         tmem_st16(a_col + lane_off, p);
         tc_fence_before();
-        mbar_arrive(&B.a_ready);
+        arrive_warp(&B.a_ready);
       } else if (l < 5) {
-        uint32_t v[32], p[32];
-        tmem_ld32(d_col + lane_off, v);
+        // all 64 accumulator columns in one load and one wait, converted in place
+        uint32_t v[64];
+        tmem_ld64(d_col + lane_off, v);
 #pragma unroll
-        for (int j = 0; j < 16; ++j) p[j] = pack2_relu<kBF16>(__uint_as_float(v[2 * j]), __uint_as_float(v[2 * j + 1]));
-        tmem_ld32(d_col + lane_off + 32, v);
-#pragma unroll
-        for (int j = 0; j < 16; ++j)
-          p[16 + j] = pack2_relu<kBF16>(__uint_as_float(v[2 * j]), __uint_as_float(v[2 * j + 1]));
-        tmem_st32(a_col + lane_off, p);
+        for (int j = 0; j < 32; ++j) v[j] = pack2_relu<kBF16>(__uint_as_float(v[2 * j]), __uint_as_float(v[2 * j + 1]));
+        tmem_st32(a_col + lane_off, *reinterpret_cast<uint32_t(*)[32]>(v));
         tc_fence_before();
-        mbar_arrive(&B.a_ready);
+        arrive_warp(&B.a_ready);
       } else {
         uint32_t o4[4];
         tmem_ld4(d_col + lane_off, o4);

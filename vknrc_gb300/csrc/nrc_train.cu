@@ -76,7 +76,7 @@ static_assert(5 * kActBytes + 2 * kActBytes >= (kCols4 + kMaxTrainCtas) * 16, "s
 struct TrainBars {
   uint64_t rec_full[2];
   uint64_t rec_empty[2];
-  uint64_t a_ready;    // 256 arrivals: the next operand rows are in shared memory / TMEM
+  uint64_t a_ready;    // 8 arrivals (one per epilogue warp): the next operand rows are in shared memory / TMEM
   uint64_t d_ready;    // MMA commit: scratch accumulator ready
   uint64_t tile_done;  // MMA commit after the tile's last weight-gradient MMA
   uint64_t drain;
@@ -276,7 +276,7 @@ __global__ void __launch_bounds__(kTrainThreads, 1) train_steps_kernel(const __g
     mbar_init(&B->rec_full[1], 1);
     mbar_init(&B->rec_empty[0], kEpiThreads);
     mbar_init(&B->rec_empty[1], kEpiThreads);
-    mbar_init(&B->a_ready, kEpiThreads);
+    mbar_init(&B->a_ready, kEpiWarps);
     mbar_init(&B->d_ready, 1);
     mbar_init(&B->tile_done, 1);
     mbar_init(&B->drain, 1);
@@ -349,10 +349,11 @@ __global__ void __launch_bounds__(kTrainThreads, 1) train_steps_kernel(const __g
       issue_train_tile(bt.records, rank + k * G, n, stage + s * kTRecTileBytes, &B->rec_full[s]);
     }
   };
-  auto publish = [&]() {  // operand rows written: hand them to the tensor core
+  auto publish = [&]() {  // operand rows written: hand them to the tensor core, one arrival per warp
     fence_proxy_async_smem();
     tc_fence_before();
-    mbar_arrive(&B->a_ready);
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&B->a_ready);
   };
   // Epilogue warps: records of the CTA's tile `it` -> target, and the encoded
   // input act_0 in shared memory and TMEM, published to the MMA warp.
