@@ -517,6 +517,71 @@ NRC_API int nrc_fp8_refresh(nrc_context* ctx, void* stream);
  * output layer), 1 / s_x[0], 1 / s_w[6] (as 448 / max|W_l|). Either may be NULL. */
 NRC_API int nrc_get_fp8(nrc_context* ctx, uint8_t* host_w8, float* host_scales);
 
+/* ---------------------------------------------------------------------------
+ * Record producer: the reference's path tracer (shader/src/path_tracer.comp)
+ * as a CUDA kernel over a BVH built on the GPU, emitting the eval and train
+ * records the cache consumes. The reference finds primary hits with a
+ * rasterised V-buffer and later hits with Vulkan ray queries against its
+ * BLAS/TLAS; here both are ray casts through one BVH over the instanced
+ * triangles (the primary cast without the secondary rays' 4.0 range).
+ * ------------------------------------------------------------------------- */
+
+/* Primitives of one instance: the instance's triangles are scene primitives
+ * first .. first + count - 1 (the reference's instance custom index plus the
+ * BLAS primitive index, path_tracer.comp:104-106). */
+typedef struct nrc_instance_range {
+  uint32_t first_primitive, primitive_count;
+} nrc_instance_range;
+
+typedef struct nrc_bvh nrc_bvh;
+
+/* Builds a BVH over every instance's transformed triangles on the current
+ * device (Morton codes, a radix sort, a binary radix tree, bounds refitted
+ * bottom-up). d_ranges: instance_count entries in device memory. Synchronous. */
+NRC_API int nrc_bvh_build(const nrc_scene* scene, const nrc_instance_range* d_ranges, nrc_bvh** out);
+NRC_API int nrc_bvh_destroy(nrc_bvh* bvh);
+NRC_API int nrc_bvh_info(const nrc_bvh* bvh, uint32_t* triangles, uint32_t* nodes);
+
+/* Path tracer methods (path_tracer.comp:26-28). */
+enum { NRC_METHOD_NONE = 0, NRC_METHOD_NRC = 1, NRC_METHOD_CACHE = 2 };
+
+/* Camera and frame (the reference's push constants, src/rg/PathTracerPass.cpp:12-21):
+ * the primary ray of pixel (x, y) has direction normalize(look + cx side + cy up),
+ * c = ((x, y) + 0.5) / extent * 2 - 1. Pixels with x <= width / 2 use
+ * left_method, the others right_method (decided per warp, as per subgroup). */
+typedef struct nrc_trace_params {
+  float origin[3], look[3], side[3], up[3];
+  uint32_t width, height;
+  uint32_t seed;
+  uint32_t left_method, right_method;
+  float train_probability;
+} nrc_trace_params;
+
+/* Where the tracer writes: eval records (appended at *eval_count, a device
+ * counter the caller zeroes first; records past eval_capacity are dropped, the
+ * reference sizes its buffer width * height + 65536, src/VkNRCState.cpp:34-36),
+ * train records of NRC_TRAIN_BATCH_COUNT batches of NRC_TRAIN_BATCH_SIZE
+ * (appended at *train_counts[b], zeroed by the caller; counts may end above the
+ * batch size, as the reference's do, and training clamps them), and the
+ * bias_factor_r (rgba32f) / factor_gb (rg32f) images of width x height. */
+typedef struct nrc_trace_targets {
+  nrc_eval_record* eval_records;
+  uint32_t* eval_count;
+  uint32_t eval_capacity;
+  nrc_packed_train_record* train_records[NRC_TRAIN_BATCH_COUNT];
+  uint32_t* train_counts[NRC_TRAIN_BATCH_COUNT];
+  float* bias_factor_r;
+  float* factor_gb;
+} nrc_trace_targets;
+
+/* One frame of the path tracer (path_tracer.comp:377-420): per pixel a primary
+ * hit, then PathTrace or, for warps chosen for training, ExtendedPathTrace
+ * (Cook-Torrance sampling, up to 8 bounces, the reference's path-length
+ * heuristic), eval records for the cache queries and train records with their
+ * self-training ranges, and the screen's bias / factor. Stream-ordered. */
+NRC_API int nrc_path_trace(const nrc_scene* scene, const nrc_bvh* bvh, const nrc_trace_params* params,
+                           const nrc_trace_targets* targets, void* stream);
+
 /* Screen pass (shader/src/screen.frag:10-31) on a headless image: `d_color` is
  * the composited rgba32f image ([height][width][4], rgb used; the bias_factor_r
  * image after nrc_infer_scatter). With accumulate != 0 the color becomes the

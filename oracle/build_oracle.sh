@@ -6,6 +6,6 @@ HERE="$(cd "$(dirname "$0")" && pwd)"
 mkdir -p "$HERE/_build"
 CC="${CC:-gcc}"
 $CC -std=c11 -O2 -ffp-contract=off -fno-fast-math -fPIC -shared -pthread \
-  "$HERE/nrc_oracle.c" -o "$HERE/_build/liboracle.so.tmp" -lm
+  "$HERE/nrc_oracle.c" "$HERE/nrc_trace_oracle.c" -o "$HERE/_build/liboracle.so.tmp" -lm
 mv -f "$HERE/_build/liboracle.so.tmp" "$HERE/_build/liboracle.so"
 "$HERE/ref/build_ref.sh"

@@ -144,6 +144,29 @@ typedef struct oracle_scene {
 void oracle_unpack(const oracle_scene* scene, const uint32_t* packed, int64_t n, int64_t stride_words, float* out,
                    int64_t out_stride);
 
+/* Path tracer (shader/src/path_tracer.comp), nrc_trace_oracle.c. ranges: per
+ * instance {first primitive, primitive count}. Outputs as the GPU's
+ * nrc_trace_targets: eval records (5 words each, eval_capacity of them),
+ * train records (10 words each, 16384 per batch), counters (start them at 0),
+ * bias_factor_r (width x height x 4) and factor_gb (x 2) floats. */
+typedef struct oracle_trace_params {
+  float origin[3], look[3], side[3], up[3];
+  uint32_t width, height, seed, left_method, right_method;
+  float train_probability;
+} oracle_trace_params;
+
+typedef struct oracle_trace_out {
+  uint32_t* eval_records;
+  uint32_t eval_count, eval_capacity;
+  uint32_t* train_records[4];
+  uint32_t train_counts[4];
+  float* bias_factor_r;
+  float* factor_gb;
+} oracle_trace_out;
+
+void oracle_path_trace(const oracle_scene* scene, const uint32_t* ranges, const oracle_trace_params* p,
+                       oracle_trace_out* o);
+
 /* Screen pass (shader/src/screen.frag:10-31) over width x height rgba32f pixels:
  * color (rgb used) -> optional running average into accumulate (rgba32f, updated
  * in place when accumulate_on) -> Hejl 2015 filmic tone map (white 3.2) -> gamma

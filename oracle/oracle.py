@@ -49,6 +49,7 @@ def lib() -> ctypes.CDLL:
         _lib.oracle_adam.argtypes = [vp, vp, ctypes.c_uint32, vp, vp, vp, vp, i32]
         _lib.oracle_screen.argtypes = [vp, vp, ctypes.c_uint32, ctypes.c_uint32, i32, ctypes.c_uint32, vp, vp]
         _lib.oracle_unpack.argtypes = [vp, vp, i64, i64, vp, i64]
+        _lib.oracle_path_trace.argtypes = [vp, vp, vp, vp]
         _lib.oracle_f32_to_e4m3.argtypes = [f32]
         _lib.oracle_f32_to_e4m3.restype = ctypes.c_uint8
         _lib.oracle_e4m3_to_f32.argtypes = [ctypes.c_uint8]
@@ -193,11 +194,9 @@ class _Texture(ctypes.Structure):
     _fields_ = [("texels", ctypes.c_void_p), ("width", ctypes.c_uint32), ("height", ctypes.c_uint32)]
 
 
-def unpack(sc: dict, packed_words: np.ndarray, first_word: int = 0) -> np.ndarray:
-    """UnpackNRCInput (NRCRecord.glsl:97-125) on host: packed_words (n, k)
-    uint32 records whose packed input starts at column first_word. Returns
-    (n, 14) float32 nrc_input records."""
-    arrs = {k: np.ascontiguousarray(v) for k, v in sc.items() if k != "textures"}
+def _scene_struct(sc: dict):
+    """(oracle_scene, keep-alive list) for a scene dict of numpy arrays."""
+    arrs = {k: np.ascontiguousarray(v) for k, v in sc.items() if k not in ("textures", "instance_ranges")}
     texs = [np.ascontiguousarray(t) for t in sc["textures"]]
     ttab = (_Texture * max(1, len(texs)))()
     for i, t in enumerate(texs):
@@ -206,6 +205,53 @@ def unpack(sc: dict, packed_words: np.ndarray, first_word: int = 0) -> np.ndarra
                _p(arrs["materials"]), _p(arrs["material_ids"]), _p(arrs["transforms"]),
                ctypes.cast(ttab, ctypes.c_void_p), arrs["vertices"].shape[0], arrs["texcoords"].shape[0],
                arrs["materials"].shape[0], arrs["vertex_indices"].shape[0], arrs["transforms"].shape[0], len(texs))
+    return S, (arrs, texs, ttab)
+
+
+class TraceParams(ctypes.Structure):
+    _fields_ = [("origin", ctypes.c_float * 3), ("look", ctypes.c_float * 3), ("side", ctypes.c_float * 3),
+                ("up", ctypes.c_float * 3), ("width", ctypes.c_uint32), ("height", ctypes.c_uint32),
+                ("seed", ctypes.c_uint32), ("left_method", ctypes.c_uint32), ("right_method", ctypes.c_uint32),
+                ("train_probability", ctypes.c_float)]
+
+
+class _TraceOut(ctypes.Structure):
+    _fields_ = [("eval_records", ctypes.c_void_p), ("eval_count", ctypes.c_uint32),
+                ("eval_capacity", ctypes.c_uint32), ("train_records", ctypes.c_void_p * 4),
+                ("train_counts", ctypes.c_uint32 * 4), ("bias_factor_r", ctypes.c_void_p),
+                ("factor_gb", ctypes.c_void_p)]
+
+
+def path_trace(sc: dict, params: TraceParams, eval_capacity: int) -> dict:
+    """The path tracer on host (nrc_trace_oracle.c): returns eval records (k, 5)
+    uint32, train records [4 x (count, 10)] uint32 words, train counts,
+    bias_factor_r (H, W, 4) and factor_gb (H, W, 2)."""
+    S, keep = _scene_struct(sc)
+    ranges = np.ascontiguousarray(sc["instance_ranges"], np.uint32)
+    h, w = params.height, params.width
+    ev = np.zeros((eval_capacity, 5), np.uint32)
+    tr = [np.zeros((16384, 10), np.uint32) for _ in range(4)]
+    bf = np.zeros((h, w, 4), np.float32)
+    gb = np.zeros((h, w, 2), np.float32)
+    o = _TraceOut()
+    o.eval_records = ev.ctypes.data
+    o.eval_capacity = eval_capacity
+    for b in range(4):
+        o.train_records[b] = tr[b].ctypes.data
+    o.bias_factor_r = bf.ctypes.data
+    o.factor_gb = gb.ctypes.data
+    lib().oracle_path_trace(ctypes.byref(S), _p(ranges), ctypes.byref(params), ctypes.byref(o))
+    counts = [int(o.train_counts[b]) for b in range(4)]
+    return {"eval": ev[: min(o.eval_count, eval_capacity)], "eval_count": int(o.eval_count),
+            "train": [tr[b][: min(counts[b], 16384)] for b in range(4)], "train_counts": counts,
+            "bias_factor_r": bf, "factor_gb": gb}
+
+
+def unpack(sc: dict, packed_words: np.ndarray, first_word: int = 0) -> np.ndarray:
+    """UnpackNRCInput (NRCRecord.glsl:97-125) on host: packed_words (n, k)
+    uint32 records whose packed input starts at column first_word. Returns
+    (n, 14) float32 nrc_input records."""
+    S, keep = _scene_struct(sc)
     w = np.ascontiguousarray(packed_words, np.uint32)
     n = w.shape[0]
     out = np.empty((n, 14), np.float32)

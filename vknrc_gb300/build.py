@@ -17,7 +17,10 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libnrc.so")
-SOURCES = ["nrc_api.cu", "nrc_infer.cu", "nrc_train.cu", "nrc_encode.cu", "nrc_noalloc.cu", "nrc_server.cu", "nrc_screen.cu", "nrc_unpack.cu", "nrc_fp8.cu"]
+SOURCES = ["nrc_api.cu", "nrc_infer.cu", "nrc_train.cu", "nrc_encode.cu", "nrc_noalloc.cu", "nrc_server.cu", "nrc_screen.cu", "nrc_unpack.cu", "nrc_fp8.cu", "nrc_trace.cu"]
+# per-file flags: the path tracer keeps every multiply and add separate (its CPU
+# oracle repeats the same IEEE operations)
+FILE_FLAGS = {"nrc_trace.cu": ["-fmad=false"]}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibility=hidden", "-I", os.path.join(ROOT, "include")]
 
@@ -30,7 +33,7 @@ def nvcc() -> str:
 
 
 def _compile(src: str, obj: str, verbose: bool) -> str:
-    cmd = [nvcc(), *ARCH, *FLAGS, "-c", os.path.join(CSRC, src), "-o", obj]
+    cmd = [nvcc(), *ARCH, *FLAGS, *FILE_FLAGS.get(src, []), "-c", os.path.join(CSRC, src), "-o", obj]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
     r = subprocess.run(cmd, capture_output=True, text=True)

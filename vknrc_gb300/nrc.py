@@ -35,7 +35,8 @@ EXPORTS = [
     "nrc_server_frame_buffers", "nrc_server_session_cache", "nrc_server_submit", "nrc_server_wait",
     "nrc_server_get_stats", "nrc_screen", "nrc_checkpoint_bytes", "nrc_save_checkpoint", "nrc_load_checkpoint",
     "nrc_unpack_eval", "nrc_unpack_train", "nrc_infer_fp8", "nrc_fp8_refresh", "nrc_get_fp8",
-    "nrc_frame_overlapped", "nrc_autotune_frame",
+    "nrc_frame_overlapped", "nrc_autotune_frame", "nrc_bvh_build", "nrc_bvh_destroy", "nrc_bvh_info",
+    "nrc_path_trace",
 ]
 
 
@@ -88,6 +89,21 @@ def scatter_targets(bias_factor_r=None, factor_gb=None, train_records: Sequence 
 class FramePlan(ctypes.Structure):
     """nrc_frame_plan: CTAs of the query and of the training in an overlapped frame."""
     _fields_ = [("query_ctas", ctypes.c_uint32), ("train_ctas", ctypes.c_uint32)]
+
+
+class TraceParams(ctypes.Structure):
+    """nrc_trace_params: camera, frame and methods of the path tracer."""
+    _fields_ = [("origin", ctypes.c_float * 3), ("look", ctypes.c_float * 3), ("side", ctypes.c_float * 3),
+                ("up", ctypes.c_float * 3), ("width", ctypes.c_uint32), ("height", ctypes.c_uint32),
+                ("seed", ctypes.c_uint32), ("left_method", ctypes.c_uint32), ("right_method", ctypes.c_uint32),
+                ("train_probability", ctypes.c_float)]
+
+
+class TraceTargets(ctypes.Structure):
+    _fields_ = [("eval_records", ctypes.c_void_p), ("eval_count", ctypes.c_void_p), ("eval_capacity", ctypes.c_uint32),
+                ("train_records", ctypes.c_void_p * TRAIN_BATCH_COUNT),
+                ("train_counts", ctypes.c_void_p * TRAIN_BATCH_COUNT), ("bias_factor_r", ctypes.c_void_p),
+                ("factor_gb", ctypes.c_void_p)]
 
 
 class QueryJob(ctypes.Structure):
@@ -200,6 +216,11 @@ def lib(build_if_missing: bool = True) -> ctypes.CDLL:
     L.nrc_infer_fp8.argtypes = [vp, vp, vp, u32, vp, vp]
     L.nrc_fp8_refresh.argtypes = [vp, vp]
     L.nrc_get_fp8.argtypes = [vp, vp, vp]
+    L.nrc_bvh_build.argtypes = [ctypes.POINTER(SceneStruct), vp, ctypes.POINTER(vp)]
+    L.nrc_bvh_destroy.argtypes = [vp]
+    L.nrc_bvh_info.argtypes = [vp, ctypes.POINTER(u32), ctypes.POINTER(u32)]
+    L.nrc_path_trace.argtypes = [ctypes.POINTER(SceneStruct), vp, ctypes.POINTER(TraceParams),
+                                 ctypes.POINTER(TraceTargets), vp]
     L.nrc_unpack_eval.argtypes = [ctypes.POINTER(SceneStruct), vp, vp, u32, vp, vp, vp]
     L.nrc_unpack_train.argtypes = [ctypes.POINTER(SceneStruct), vp, vp, u32, vp, vp]
     L.nrc_checkpoint_bytes.restype = ctypes.c_size_t
@@ -596,7 +617,8 @@ class DeviceScene:
         def up(a):
             return torch.from_numpy(np.ascontiguousarray(a)).cuda()
 
-        self.keep = {k: up(v) for k, v in sc.items() if k != "textures"}
+        self.keep = {k: up(v) for k, v in sc.items() if k not in ("textures", "instance_ranges")}
+        self.ranges = up(sc["instance_ranges"].astype(np.uint32).view(np.int32)) if "instance_ranges" in sc else None
         self.tex = [up(t) for t in sc["textures"]]
         table = np.zeros((max(1, len(self.tex)), 2), np.uint64)
         for i, t in enumerate(self.tex):
@@ -623,3 +645,69 @@ def unpack_train(scene: DeviceScene, records, count, out_records, capacity=None,
     cap = records.shape[0] if capacity is None else capacity
     check(lib().nrc_unpack_train(ctypes.byref(scene.s), _ptr(records), _ptr(count), cap, _ptr(out_records),
                                  _stream(stream)), "nrc_unpack_train")
+
+
+# ------------------------------------------------------------- path tracer --
+class Bvh:
+    """nrc_bvh over a DeviceScene's instance ranges (built on the GPU)."""
+
+    def __init__(self, scene: "DeviceScene"):
+        h = ctypes.c_void_p()
+        check(lib().nrc_bvh_build(ctypes.byref(scene.s), _ptr(scene.ranges), ctypes.byref(h)), "nrc_bvh_build")
+        self.h = h
+
+    def info(self):
+        t, n = ctypes.c_uint32(), ctypes.c_uint32()
+        check(lib().nrc_bvh_info(self.h, ctypes.byref(t), ctypes.byref(n)), "nrc_bvh_info")
+        return t.value, n.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().nrc_bvh_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class TraceBuffers:
+    """Device outputs of nrc_path_trace for a width x height frame."""
+
+    def __init__(self, width: int, height: int, eval_capacity=None):
+        import torch
+
+        self.eval_capacity = width * height + 65536 if eval_capacity is None else eval_capacity
+        self.eval = torch.zeros((self.eval_capacity, 5), dtype=torch.int32, device="cuda")
+        self.eval_count = torch.zeros(1, dtype=torch.int32, device="cuda")
+        self.train = [torch.zeros((TRAIN_BATCH_SIZE, 10), dtype=torch.int32, device="cuda")
+                      for _ in range(TRAIN_BATCH_COUNT)]
+        self.train_counts = [torch.zeros(1, dtype=torch.int32, device="cuda") for _ in range(TRAIN_BATCH_COUNT)]
+        self.bias_factor_r = torch.zeros((height, width, 4), dtype=torch.float32, device="cuda")
+        self.factor_gb = torch.zeros((height, width, 2), dtype=torch.float32, device="cuda")
+
+    def reset(self):
+        self.eval_count.zero_()
+        for c in self.train_counts:
+            c.zero_()
+
+    def targets(self) -> TraceTargets:
+        t = TraceTargets()
+        t.eval_records = _ptr(self.eval)
+        t.eval_count = _ptr(self.eval_count)
+        t.eval_capacity = self.eval_capacity
+        for b in range(TRAIN_BATCH_COUNT):
+            t.train_records[b] = _ptr(self.train[b])
+            t.train_counts[b] = _ptr(self.train_counts[b])
+        t.bias_factor_r = _ptr(self.bias_factor_r)
+        t.factor_gb = _ptr(self.factor_gb)
+        return t
+
+
+def path_trace(scene: "DeviceScene", bvh: Bvh, params: TraceParams, buffers: TraceBuffers, stream=None) -> None:
+    """nrc_path_trace (the caller zeroes the counters: TraceBuffers.reset)."""
+    t = buffers.targets()
+    check(lib().nrc_path_trace(ctypes.byref(scene.s), bvh.h, ctypes.byref(params), ctypes.byref(t), _stream(stream)),
+          "nrc_path_trace")

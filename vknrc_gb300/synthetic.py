@@ -149,6 +149,10 @@ def scene(rng: np.random.Generator, vertices: int = 300, primitives: int = 200, 
         t[i, :, 3] = rng.uniform(-3, 3, 3)
     sc["transforms"] = t
     sc["textures"] = [rng.integers(0, 256, (h, w, 4), dtype=np.uint8) for (w, h) in texture_sizes]
+    # each instance owns a contiguous range of primitives (the reference's instance
+    # custom index + BLAS primitive index); the tracer renders these ranges
+    cuts = np.linspace(0, primitives, instances + 1).astype(np.int64)
+    sc["instance_ranges"] = np.stack([cuts[:-1], cuts[1:] - cuts[:-1]], 1).astype(np.uint32)
     return sc
 
 
