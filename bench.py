@@ -53,6 +53,7 @@ def parse_args():
     p.add_argument("--no-batched", action="store_true", help="skip the batched-caches leg")
     p.add_argument("--no-serving", action="store_true", help="skip the serving leg")
     p.add_argument("--serve-seconds", type=float, default=2.0, help="duration of the serving leg's arrivals")
+    p.add_argument("--no-render", action="store_true", help="skip the renderer-frame leg")
     return p.parse_args()
 
 
@@ -445,6 +446,72 @@ def fp8_leg(evals, trains, eval_cnt, train_cnt, steps=500):
             "accuracy": "tests/test_gpu_fp8.py: query error against the FP64 oracle"}
 
 
+# ---------------------------------------------------------------- render leg --
+def render_leg(frames=20, width=1920, height=1080):
+    """The reference's whole renderer frame on the GPU at 1080p over a seeded
+    closed room (522,254 triangles: a height-field floor, walls, an emissive ceiling panel; BVH built on the GPU): path tracer with record
+    emission, unpack of the eval and train records, the cache query with the
+    destination epilogue and four training steps, the screen pass; CUDA-event
+    time per stage."""
+    import torch
+
+    from vknrc_gb300 import Cache, nrc, synthetic as S
+
+    sc = S.terrain_scene(S.rng_for(3), n=512)
+    ds = nrc.DeviceScene(sc)
+    t0 = time.perf_counter()
+    bvh = nrc.Bvh(ds)
+    build_s = time.perf_counter() - t0
+    buf = nrc.TraceBuffers(width, height)
+    P = nrc.TraceParams()
+    P.origin[:] = (0.0, 0.3, -1.9)
+    P.look[:] = (0.0, -0.25, 1.0)
+    P.side[:] = (0.8, 0.0, 0.0)
+    P.up[:] = (0.0, 0.8 * height / width, 0.0)
+    P.width, P.height, P.left_method, P.right_method, P.train_probability = width, height, 1, 1, 0.03
+    cap = buf.eval_capacity
+    inputs = torch.zeros((cap, 14), dtype=torch.float32, device="cuda")
+    dst = torch.zeros(cap, dtype=torch.int32, device="cuda")
+    train_u = [torch.zeros((R, 20), dtype=torch.float32, device="cuda") for _ in range(B)]
+    acc = torch.zeros((height, width, 4), dtype=torch.float32, device="cuda")
+    out8 = torch.zeros((height, width, 4), dtype=torch.uint8, device="cuda")
+    names = ["trace", "unpack", "query_and_train", "screen"]
+    ms = {k: [] for k in names}
+    counts = []
+    with Cache(seed=11, learning_rate=1e-3, beta2=0.99) as c:
+        targets = nrc.scatter_targets(buf.bias_factor_r, buf.factor_gb, train_u)
+        for f in range(frames + 3):
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+            P.seed = 77 + f
+            buf.reset()
+            ev[0].record()
+            nrc.path_trace(ds, bvh, P, buf)
+            ev[1].record()
+            nrc.unpack_eval(ds, buf.eval, buf.eval_count, inputs, dst, capacity=cap)
+            for b in range(B):
+                nrc.unpack_train(ds, buf.train[b], buf.train_counts[b], train_u[b], capacity=R)
+            ev[2].record()
+            c.frame_scatter(inputs, dst, buf.eval_count, targets, buf.train_counts, eval_capacity=cap)
+            ev[3].record()
+            nrc.screen(buf.bias_factor_r, acc, f, out8)
+            ev[4].record()
+            torch.cuda.synchronize()
+            if f >= 3:
+                for i, k in enumerate(names):
+                    ms[k].append(ev[i].elapsed_time(ev[i + 1]))
+                counts.append((int(buf.eval_count.item()), [int(x.item()) for x in buf.train_counts]))
+        if c.error() != 0:
+            raise RuntimeError("device error in the render leg")
+    bvh.close()
+    per = {k: statistics.mean(v) for k, v in ms.items()}
+    return {"workload": "1080p renderer frame in a closed 522,254-triangle room: path trace + record unpack + "
+                        "query with destinations + 4 training steps + screen pass",
+            "ms_per_stage": per, "ms_per_frame": sum(per.values()), "frames": frames,
+            "eval_records_per_frame": statistics.mean(x[0] for x in counts),
+            "train_records_per_frame": statistics.mean(sum(min(t, R) for t in x[1]) for x in counts),
+            "bvh_build_s": build_s, "train_probability": 0.03}
+
+
 # --------------------------------------------------------------- serving leg --
 SERVE_RES = [(1280, 720), (1920, 1080), (2560, 1440)]
 
@@ -700,6 +767,8 @@ def ours_arm(args, world, rank, local):
         result["batched"] = batched_leg(evals, trains)
     if rank == 0 and world == 1 and not args.no_serving:
         result["serving"] = serving_leg(evals, trains, seconds=args.serve_seconds)
+    if rank == 0 and world == 1 and not args.no_render:
+        result["render"] = render_leg()
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         qps, threads, sample, _ = cpu_frame_sample(1, 2, budget_s=12.0)
         result["cpu_baseline"] = {"value": qps, "unit": "queries/s", "cores": threads, "kind": "port",

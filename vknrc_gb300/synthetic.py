@@ -196,3 +196,65 @@ def packed_train_records(rng: np.random.Generator, sc: dict, n: int) -> np.ndarr
     f[:, 3:6] = rng.uniform(0, 1, (n, 3))
     r[:, 6:] = packed_inputs(rng, sc, n)
     return r
+
+
+def terrain_scene(rng: np.random.Generator, n: int = 256, texture: int = 64) -> dict:
+    """A seeded closed room for the path tracer and the renderer frame: a
+    height-field floor (an n x n vertex grid over [-2, 2]^2 with smooth random
+    heights, 2 (n-1)^2 triangles) inside four walls and a ceiling (the room is
+    sized for the tracer's 4.0 secondary-ray range, so few paths escape),
+    an emissive ceiling panel, two instances (the room and a raised, rotated,
+    scaled copy of part of the floor), four materials of which two are
+    textured."""
+    g = np.linspace(-2.0, 2.0, n, dtype=np.float32)
+    X, Z = np.meshgrid(g, g)
+    H = np.zeros_like(X)
+    for k in range(4):
+        f = rng.uniform(0.6, 3.0) * (k + 1)
+        H += rng.uniform(0.05, 0.2) / (k + 1) * np.sin(f * X + rng.uniform(0, 6)) * np.cos(f * Z + rng.uniform(0, 6))
+    floor_v = np.stack([X, H - 0.6, Z], -1).reshape(-1, 3)
+    i = np.arange(n - 1)
+    a = (i[:, None] * n + i[None, :]).ravel()
+    quads = np.stack([a, a + 1, a + n, a + n + 1], 1)
+    floor_t = np.concatenate([quads[:, [0, 2, 1]], quads[:, [1, 2, 3]]], 0)
+    # walls and ceiling: a box x, z in [-2.05, 2.05], y in [-0.8, 1.0]; two panels of the
+    # ceiling are emitters
+    lo, hi, y0, y1 = -2.05, 2.05, -0.8, 1.0
+    box = np.array([[lo, y0, lo], [hi, y0, lo], [hi, y1, lo], [lo, y1, lo],
+                    [lo, y0, hi], [hi, y0, hi], [hi, y1, hi], [lo, y1, hi],
+                    [-0.6, y1 - 0.01, -0.6], [0.6, y1 - 0.01, -0.6], [0.6, y1 - 0.01, 0.6], [-0.6, y1 - 0.01, 0.6]],
+                   np.float32)
+    box_t = np.array([[0, 1, 2], [0, 2, 3], [4, 6, 5], [4, 7, 6], [0, 3, 7], [0, 7, 4], [1, 5, 6], [1, 6, 2],
+                      [3, 2, 6], [3, 6, 7], [8, 10, 9], [8, 11, 10]]) + floor_v.shape[0]
+    sc = {}
+    sc["vertices"] = np.concatenate([floor_v, box], 0).astype(np.float32)
+    tri = np.concatenate([floor_t, box_t], 0).astype(np.uint32)
+    sc["vertex_indices"] = tri
+    sc["texcoords"] = (sc["vertices"][:, [0, 2]] * 1.5).astype(np.float32)
+    sc["texcoord_indices"] = tri.copy()
+    mats = np.zeros((4, 16), np.float32)
+    ids = mats.view(np.uint32)
+    mats[:, 0:3] = rng.uniform(0.2, 0.9, (4, 3))
+    mats[:, 4:7] = rng.uniform(0.0, 0.5, (4, 3))
+    mats[:, 13] = [0.3, 0.7, 0.1, 0.5]  # roughness
+    mats[:, 14] = 1.5
+    mats[3, 8:11] = [6.0, 5.5, 5.0]     # the emitter
+    ids[:, 3] = [0, 0xFFFFFFFF, 1, 0xFFFFFFFF]
+    ids[:, 7] = [0xFFFFFFFF, 1, 0xFFFFFFFF, 0xFFFFFFFF]
+    ids[:, 11] = 0xFFFFFFFF
+    sc["materials"] = mats
+    p = tri.shape[0]
+    mid = rng.integers(0, 3, p).astype(np.uint32)
+    mid[floor_t.shape[0]:] = 1          # walls and ceiling
+    mid[-2:] = 3                        # the ceiling panel emits
+    sc["material_ids"] = mid
+    t = np.zeros((2, 3, 4), np.float32)
+    t[0, :, :3] = np.eye(3)
+    c, s_ = np.cos(0.6), np.sin(0.6)
+    t[1, :, :3] = np.array([[c, 0, s_], [0, 1, 0], [-s_, 0, c]]) * 0.3
+    t[1, :, 3] = [0.6, 0.1, 0.4]
+    sc["transforms"] = t
+    sc["textures"] = [rng.integers(0, 256, (texture, texture, 4), dtype=np.uint8),
+                      rng.integers(0, 256, (texture // 2, texture, 4), dtype=np.uint8)]
+    sc["instance_ranges"] = np.array([[0, p], [0, floor_t.shape[0] // 8]], np.uint32)
+    return sc
