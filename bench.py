@@ -670,31 +670,55 @@ def ours_arm(args, world, rank, local):
         raise RuntimeError(f"device error status {err} during the benchmark")
 
     # end to end through the C ABI with host buffers: H2D of each frame's records
-    # from pinned memory, the frame, D2H of the query results
+    # from pinned memory, the frame, D2H of the query results. Frames are
+    # pipelined over two device buffer sets: frame k's upload (copy stream) runs
+    # while frame k-1 computes and frame k-2's results come back (second copy
+    # stream), as a host-fed renderer would schedule them.
     E = max(1, min(args.e2e_steps, K))
     h_eval = [evals[f].cpu().pin_memory() for f in range(min(2, len(evals)))]
     h_train = [[t.cpu().pin_memory() for t in trains[f]] for f in range(min(2, len(trains)))]
-    d_eval = torch.empty_like(evals[0])
-    d_train = [torch.empty_like(trains[0][0]) for _ in range(B)]
-    h_out = torch.empty((Q, 3), dtype=torch.float32).pin_memory()
+    d_eval = [torch.empty_like(evals[0]) for _ in range(2)]
+    d_train = [[torch.empty_like(trains[0][0]) for _ in range(B)] for _ in range(2)]
+    d_out = [out, torch.empty_like(out)]
+    h_out = [torch.empty((Q, 3), dtype=torch.float32).pin_memory() for _ in range(2)]
     h2d = Q * EVAL_BYTES + B * R * TRAIN_BYTES
     d2h = Q * OUT_BYTES
+    up_s, down_s = torch.cuda.Stream(), torch.cuda.Stream()
+    ev_up = [torch.cuda.Event() for _ in range(2)]       # buffer set holds frame k's inputs
+    ev_done = [torch.cuda.Event() for _ in range(2)]     # frame k computed (inputs free, outputs ready)
+    ev_back = [torch.cuda.Event() for _ in range(2)]     # frame k's outputs are on the host
 
     def e2e_frame(k):
-        d_eval.copy_(h_eval[k % len(h_eval)], non_blocking=True)
-        for b in range(B):
-            d_train[b].copy_(h_train[k % len(h_train)][b], non_blocking=True)
-        cache.frame_overlapped(d_eval, eval_cnt, out, d_train, train_cnt)
-        h_out.copy_(out, non_blocking=True)
+        j = k % 2
+        with torch.cuda.stream(up_s):
+            up_s.wait_event(ev_done[j])  # frame k-2 no longer reads this set
+            d_eval[j].copy_(h_eval[k % len(h_eval)], non_blocking=True)
+            for b in range(B):
+                d_train[j][b].copy_(h_train[k % len(h_train)][b], non_blocking=True)
+            ev_up[j].record(up_s)
+        stream.wait_event(ev_up[j])
+        stream.wait_event(ev_back[j])  # frame k-2's results have left d_out[j]
+        cache.frame_overlapped(d_eval[j], eval_cnt, d_out[j], d_train[j], train_cnt)
+        ev_done[j].record(stream)
+        with torch.cuda.stream(down_s):
+            down_s.wait_event(ev_done[j])
+            h_out[j].copy_(d_out[j], non_blocking=True)
+            ev_back[j].record(down_s)
 
+    for j in range(2):
+        ev_done[j].record(stream)
+        ev_back[j].record(stream)
     for k in range(3):
         e2e_frame(k)
     torch.cuda.synchronize()
     barrier(world)
     s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     s.record(stream)
+    up_s.wait_stream(stream)
+    down_s.wait_stream(stream)
     for k in range(E):
         e2e_frame(k)
+    stream.wait_stream(down_s)
     e.record(stream)
     torch.cuda.synchronize()
     e2e_s = max_over_ranks(s.elapsed_time(e) / 1e3, world)
@@ -754,7 +778,9 @@ def ours_arm(args, world, rank, local):
             "algorithmic_bytes_per_launch": Q * (EVAL_BYTES + OUT_BYTES),
         },
         "e2e": {"value": world * Q * E / e2e_s, "unit": "queries/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "steps": E},
+                "d2h_bytes_per_step": d2h, "steps": E,
+                "schedule": "pinned host buffers; frame k's H2D overlaps frame k-1's compute and frame k-2's D2H "
+                            "(bounded by the ~196 GB/s host-to-device copy rate: 121 MB per frame)"},
         "clocks": clocks,
     }
     if plain is not None:
