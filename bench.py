@@ -54,6 +54,8 @@ def parse_args():
     p.add_argument("--no-serving", action="store_true", help="skip the serving leg")
     p.add_argument("--serve-seconds", type=float, default=2.0, help="duration of the serving leg's arrivals")
     p.add_argument("--no-render", action="store_true", help="skip the renderer-frame leg")
+    p.add_argument("--cpu-budget", type=float, default=60.0,
+                   help="seconds of CPU work the reference arm samples (at least one step)")
     return p.parse_args()
 
 
@@ -221,8 +223,8 @@ def reference_arm(args, world, rank):
     if rank != 0:
         return
     warm = min(max(0, args.warmup), 3)
-    # a bounded sample (about 60 s of CPU work) so that the whole run ends within minutes
-    qps, threads, sample, frame_s = cpu_frame_sample(1, warm, budget_s=60.0)
+    # a bounded sample (about 60 s of CPU work by default) so that the whole run ends within minutes
+    qps, threads, sample, frame_s = cpu_frame_sample(1, warm, budget_s=args.cpu_budget)
     steps_run = int(sample.split(" ", 1)[0])
     line = {
         "impl": "reference", "metric": METRIC, "value": qps, "unit": "queries/s", "n_gpus": 1, "steps": steps_run,
