@@ -576,10 +576,19 @@ int nrc_autotune_frame(nrc_context* c, const nrc_input* eval_in, const uint32_t*
   nrc_frame_plan best = {0u, 0u};
   float best_t = 1e30f;
   if (e == cudaSuccess) {
-    // candidates: the sequential frame, then training groups of 8 .. 72 CTAs beside the query
+    // candidates: the sequential frame, then training groups of 8 .. 72 CTAs beside the query:
+    // multiples of 8, and the smallest group for each count of tiles per CTA (a batch's
+    // step takes as long as its busiest CTA, so e.g. 43 CTAs finish 128 tiles as soon as 48)
     std::vector<nrc_frame_plan> cand = {{0u, 0u}};
     const uint32_t sms = static_cast<uint32_t>(c->num_sms);
-    for (uint32_t tc = 8; tc <= 72 && tc < sms; tc += 8) cand.push_back({sms - tc, tc});
+    std::vector<uint32_t> groups;
+    for (uint32_t tc = 8; tc <= 72; tc += 8) groups.push_back(tc);
+    const uint32_t tiles = (train_capacity + nrc::kTile - 1) / nrc::kTile;
+    for (uint32_t k = 1; k <= 16 && tiles > 0; ++k) groups.push_back((tiles + k - 1) / k);
+    std::sort(groups.begin(), groups.end());
+    groups.erase(std::unique(groups.begin(), groups.end()), groups.end());
+    for (uint32_t tc : groups)
+      if (tc >= 8 && tc <= 72 && tc < sms) cand.push_back({sms - tc, tc});
     for (const nrc_frame_plan& pl : cand) {
       for (int k = 0; k < 3 && s == NRC_OK; ++k)
         s = nrc_frame_overlapped(t, eval_in, d_eval_count, eval_capacity, out, train_rec, train_counts,

@@ -15,7 +15,11 @@
 //     layer's weight gradient; the forward and dA MMAs take their A operand
 //     (act_l, or the gradient g_{l+1}) from tensor memory, where the epilogue
 //     writes it beside the shared-memory copy (the shared-memory form would be
-//     bound by shared-memory bandwidth at this width);
+//     bound by shared-memory bandwidth at this width). The epilogue hands the
+//     TMEM copy to the MMA warp first (a_ready) and writes the shared-memory
+//     copy after it, off the layer chain; the gradients' shared-memory copies
+//     have their own barrier (g_ready), which only the weight-gradient MMAs
+//     wait for;
 //   - dA = (g W) masked by act > 0 uses the weight tile itself as an MN-major B
 //     operand (the reference's NaN-mask trick becomes a bit mask on packed
 //     halves); it is issued before the layer's weight-gradient MMAs so the
@@ -50,7 +54,7 @@ constexpr uint32_t kActOff = kWeightSmemBytes;              // 43008
 constexpr uint32_t kGOff = kActOff + 6 * kActBytes;         // two gradient buffers
 constexpr uint32_t kStageOff = kGOff + 2 * kActBytes;
 constexpr uint32_t kTBarOff = kStageOff + 2 * kTRecTileBytes;
-constexpr uint32_t kECacheOff = kTBarOff + 128;
+constexpr uint32_t kECacheOff = kTBarOff + 256;
 static_assert(kActOff % 1024 == 0 && kGOff % 1024 == 0 && kStageOff % 16 == 0, "alignment");
 
 // TMEM columns: dW_l accumulators (M=64 layout) at 64*l, l = 0..5; scratch D at
@@ -76,7 +80,8 @@ static_assert(5 * kActBytes + 2 * kActBytes >= (kCols4 + kMaxTrainCtas) * 16, "s
 struct TrainBars {
   uint64_t rec_full[2];
   uint64_t rec_empty[2];
-  uint64_t a_ready;    // 8 arrivals (one per epilogue warp): the next operand rows are in shared memory / TMEM
+  uint64_t a_ready;    // 8 arrivals (one per epilogue warp): the next A operand is in TMEM
+  uint64_t g_ready;    // 8 arrivals: a gradient's shared-memory rows (weight-gradient operand) are written
   uint64_t d_ready;    // MMA commit: scratch accumulator ready
   uint64_t tile_done;  // MMA commit after the tile's last weight-gradient MMA
   uint64_t drain;
@@ -86,7 +91,7 @@ struct TrainBars {
   uint32_t count[NRC_TRAIN_BATCH_COUNT];  // record counts as read at launch
   nrc_optimizer_state st;                 // optimizer step state as read at launch
 };
-static_assert(sizeof(TrainBars) <= 128, "barrier area");
+static_assert(sizeof(TrainBars) <= 256, "barrier area");
 
 __device__ __forceinline__ uint8_t* align1024(uint8_t* p) {
   return reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(p) + 1023) & ~uintptr_t(1023));
@@ -277,6 +282,7 @@ __global__ void __launch_bounds__(kTrainThreads, 1) train_steps_kernel(const __g
     mbar_init(&B->rec_empty[0], kEpiThreads);
     mbar_init(&B->rec_empty[1], kEpiThreads);
     mbar_init(&B->a_ready, kEpiWarps);
+    mbar_init(&B->g_ready, kEpiWarps);
     mbar_init(&B->d_ready, 1);
     mbar_init(&B->tile_done, 1);
     mbar_init(&B->drain, 1);
@@ -332,6 +338,7 @@ __global__ void __launch_bounds__(kTrainThreads, 1) train_steps_kernel(const __g
   const uint32_t a_lane = lane_base + kACol + 16 * h;
   const uint32_t d_lane = lane_base + kDCol + 32 * h;
   uint32_t ph_a = 0, ph_d = 0;  // MMA warp / epilogue d_ready phases
+  uint32_t ph_g = 0;            // MMA warp: g_ready phase
   uint32_t ct = 0;              // tiles this CTA has processed over all batches
   uint32_t wloads = 0;          // weight loads issued to this CTA
   uint32_t barriers = 0;        // grid barriers passed
@@ -349,11 +356,20 @@ __global__ void __launch_bounds__(kTrainThreads, 1) train_steps_kernel(const __g
       issue_train_tile(bt.records, rank + k * G, n, stage + s * kTRecTileBytes, &B->rec_full[s]);
     }
   };
-  auto publish = [&]() {  // operand rows written: hand them to the tensor core, one arrival per warp
-    fence_proxy_async_smem();
+  // The next MMA's A operand is in TMEM: hand it to the MMA warp, one arrival
+  // per warp. Shared-memory rows written after this (the weight-gradient
+  // operands) are published by the next release_smem.
+  auto release_tmem = [&]() {
     tc_fence_before();
     __syncwarp();
     if (lane == 0) mbar_arrive(&B->a_ready);
+  };
+  // Every shared-memory operand row this thread wrote so far (activations, the
+  // gradient just stored) is visible to the tensor core: one arrival per warp.
+  auto release_smem = [&]() {
+    fence_proxy_async_smem();
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&B->g_ready);
   };
   // Epilogue warps: records of the CTA's tile `it` -> target, and the encoded
   // input act_0 in shared memory and TMEM, published to the MMA warp.
@@ -411,8 +427,8 @@ __global__ void __launch_bounds__(kTrainThreads, 1) train_steps_kernel(const __g
       amax_record(P.amax, m);
     }
     tmem_st16(a_lane, e);
-    store_half(act, row, h, e);
-    publish();
+    release_tmem();
+    store_half(act, row, h, e);  // read by dW_0 at the end of the backward pass
     return true;
   };
 
@@ -475,8 +491,8 @@ __global__ void __launch_bounds__(kTrainThreads, 1) train_steps_kernel(const __g
         // backward: g_{l+1} lives in gradient buffer (5 - l) & 1
         for (int l = 5; l >= 0 && ok; --l) {
           const uint64_t gb = static_cast<uint64_t>(((5 - l) & 1) * 1024);
-          if (elect_one()) {
-            if (l > 0) {
+          if (l > 0) {
+            if (elect_one()) {
               // dA_l = g W_l  (K = 64 outputs, or 16 for the padded output layer)
               const uint64_t wm = dm_w + static_cast<uint64_t>(l * 512);
               mma_ts(dcol, acol + 0, wm + 0, id_da, 0u);
@@ -487,6 +503,15 @@ __global__ void __launch_bounds__(kTrainThreads, 1) train_steps_kernel(const __g
               }
               mma_commit(&B->d_ready);
             }
+            __syncwarp();
+          }
+          // the weight gradient reads g_{l+1}'s shared-memory rows (and act_l),
+          // written after the TMEM copy that dA_l reads
+          ok = warp_all(mbar_wait(&B->g_ready, ph_g, kWaitLimitNs));
+          if (!ok) break;
+          ph_g ^= 1u;
+          tc_fence_after();
+          if (elect_one()) {
             // dW_l += g^T act_l   (M = 64 outputs, N = 64 inputs, K = 128 records);
             // complete by the next d_ready (or tile_done for l = 0)
             const uint64_t ga = dm_g + gb, ab = dm_act + static_cast<uint64_t>(l * 1024);
@@ -528,14 +553,14 @@ __global__ void __launch_bounds__(kTrainThreads, 1) train_steps_kernel(const __g
           for (int j = 0; j < 16; ++j)
             p[j] = pack2_relu<kBF16>(__uint_as_float(v[2 * j]), __uint_as_float(v[2 * j + 1]));
           tmem_st16(a_lane, p);
-          store_half(act + (l + 1) * kActBytes, row, h, p);
+          release_tmem();
+          store_half(act + (l + 1) * kActBytes, row, h, p);  // read by dW_{l+1}
           if (P.amax != nullptr) {  // largest input of layer l + 1 (FP8 query scales)
             float m = 0.0f;
 #pragma unroll
             for (int j = 0; j < 32; ++j) m = fmaxf(m, __uint_as_float(v[j]));
             amax_record(P.amax + l + 1, m);
           }
-          publish();
         }
         if (!ok) break;
         // output + relative-L2 luminance loss gradient (NN_nv.glsl:178-196), fp16;
@@ -569,21 +594,23 @@ __global__ void __launch_bounds__(kTrainThreads, 1) train_steps_kernel(const __g
             }
             tmem_st16(a_lane, gw);  // dA_5 reads K = 16 (A words 0..7)
           }
-          store_half(gbuf, row, h, gw);
-          publish();
+          release_tmem();
+          store_half(gbuf, row, h, gw);  // read by dW_5
+          release_smem();                // (with act_0 .. act_5)
         }
         // backward: g_l = fp16((g_{l+1} W_l) masked by act_l > 0), l = 5..1
         for (int l = 5; l >= 1; --l) {
-          if (!wait_d()) break;
           uint32_t aw[16], gw[16], v[32];
-          load_half(act + l * kActBytes, row, h, aw);
+          load_half(act + l * kActBytes, row, h, aw);  // the mask rows, while dA_l runs
+          if (!wait_d()) break;
           tmem_ld32(d_lane, v);
 #pragma unroll
           for (int j = 0; j < 16; ++j)
             gw[j] = relu_mask2<kBF16>(pack2<kBF16>(__uint_as_float(v[2 * j]), __uint_as_float(v[2 * j + 1])), aw[j]);
           tmem_st16(a_lane, gw);
-          store_half(gbuf + ((6 - l) & 1) * kActBytes, row, h, gw);
-          publish();
+          release_tmem();
+          store_half(gbuf + ((6 - l) & 1) * kActBytes, row, h, gw);  // read by dW_{l-1}
+          release_smem();
           // dA_l completing means dW_{l+1} (issued before it) is complete too;
           // on the CTA's last tile it is final: write it out while the chain goes on.
           if (last && l <= 4) drain_dw(lane_base, l + 1, q, h, lane, my_partial);
