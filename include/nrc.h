@@ -233,35 +233,41 @@ NRC_API int nrc_frame(nrc_context* ctx, const nrc_input* d_eval_inputs, const ui
               float* d_out_rgb, const nrc_train_record* const* d_train_records, uint32_t* const* d_train_counts,
               uint32_t train_capacity, void* stream);
 
-/* Split of the SMs for nrc_frame_overlapped: query_ctas for the query,
- * train_ctas for the training, query_ctas + train_ctas <= SMs. train_ctas = 0
- * runs the frame sequentially (both on every SM). */
+/* Split of the SMs for nrc_frame_overlapped: train_ctas for the training,
+ * query_ctas (query_ctas + train_ctas <= SMs) for the query CTAs that run
+ * beside it from the start; the query's other CTAs start on the training's SMs
+ * as it finishes. train_ctas = 0 runs the frame sequentially (both on every
+ * SM). */
 typedef struct nrc_frame_plan {
   uint32_t query_ctas, train_ctas;
 } nrc_frame_plan;
 
-/* nrc_frame with the query and the training run at the same time on disjoint
- * SMs. The reference's frame reads use_weights in its query and writes them in
- * its last training step (src/rg/NRCRenderGraph.cpp:52, :77); here the training
- * writes them into a second buffer of the context, copied into use_weights
- * (a 41 KB device copy on `stream`) once both the query and the training are
- * done. The query therefore reads exactly the weights it reads in nrc_frame,
- * and use_weights change only at the end of the call, as there. The training
- * runs with plan->train_ctas CTAs, so its gradient sums are grouped as
- * nrc_train_many with that count groups them.
+/* nrc_frame with the query and the training run at the same time. The
+ * reference's frame reads use_weights in its query and writes them in its last
+ * training step (src/rg/NRCRenderGraph.cpp:52, :77); here the training writes
+ * them into a second buffer of the context, copied into use_weights (41 KB) by
+ * whichever of the two kernels finishes last, once both are done. The
+ * query therefore reads exactly the weights it reads in nrc_frame, and
+ * use_weights change only at the end of the call, as there. The training runs
+ * with plan->train_ctas CTAs, so its gradient sums are grouped as
+ * nrc_train_many with that count groups them. It is launched first on
+ * `stream`; the query follows as a dependent launch that starts once every
+ * training CTA runs, takes its record tiles from a counter of the context, and
+ * so also fills the training's SMs when the training ends (one frame at a time
+ * per context).
  * plan NULL: the context's tuned plan (nrc_autotune_frame), else a quarter of
  * the SMs for the training. query_event (a cudaEvent_t, may be NULL) is recorded
- * on `stream` when the query results are complete, before the training is
- * (a renderer can start its screen pass on it). The training runs on a stream
- * of the context joined back into `stream`, so the call can be captured in a
- * CUDA graph like the others. */
+ * on `stream` after the query: it completes with the frame's two kernels. Both
+ * kernels run on `stream`, so the call can be captured in a CUDA graph like the
+ * others. */
 NRC_API int nrc_frame_overlapped(nrc_context* ctx, const nrc_input* d_eval_inputs, const uint32_t* d_eval_count,
                                  uint32_t eval_capacity, float* d_out_rgb, const nrc_train_record* const* d_train_records,
                                  uint32_t* const* d_train_counts, uint32_t train_capacity, const nrc_frame_plan* plan,
                                  void* query_event, void* stream);
 
 /* Autotuner of the overlapped frame: times the sequential frame and training
- * groups of 8, 16, ..., 72 CTAs beside the query on this workload (on a scratch
+ * groups of 8, 16, ..., 72 CTAs, and the smallest group for each count of
+ * record tiles per CTA, beside the query on this workload (on a scratch
  * copy of the cache, which it then frees; `d_out_rgb` and the counts are written
  * as a frame writes them), keeps the fastest split as the context's plan and
  * returns it with its time per frame. Synchronous. */

@@ -1,7 +1,8 @@
 """The overlapped frame (nrc_frame_overlapped): the query of a frame and its
-four training steps on disjoint SMs at the same time, the training's new
-rendering weights staged and copied in at the end, and the autotuner that
-picks the split.
+four training steps at the same time (the training on its CTAs, the query's
+tiles handed out by a counter to CTAs beside it and, as it finishes, on its
+SMs), the training's new rendering weights staged and copied in by the kernel
+that finishes last, and the autotuner that picks the split.
 
 The query reads the same use_weights as in the sequential frame, so its
 answers are the same bit for bit; the training with a group of train_ctas

@@ -25,6 +25,7 @@ struct nrc_context {
   nrc_optimizer_state* state = nullptr;
   float* partials = nullptr;  // one weight-gradient vector per training CTA
   uint32_t* sync = nullptr;   // grid-barrier counter of the trainer
+  uint32_t* tiles = nullptr;  // tile and exit counters of the overlapped frame's query
   uint32_t* err = nullptr;
   double* loss_acc = nullptr;
   unsigned long long* loss_count = nullptr;
@@ -35,8 +36,6 @@ struct nrc_context {
   nrc::Fp8State* fp8s = nullptr;
   CUtensorMap map_w8;
   __half* use_next = nullptr;   // the overlapped frame's training writes use_weights here first
-  cudaStream_t side = nullptr;  // the overlapped frame's training stream
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   nrc_frame_plan plan = {0u, 0u};  // the overlapped frame's split (0, 0: default)
 };
 
@@ -259,6 +258,7 @@ int nrc_create(const nrc_config* cfg_in, nrc_context** out) {
   c->loss_acc = reinterpret_cast<double*>(b + o_loss);
   c->loss_count = reinterpret_cast<unsigned long long*>(b + o_loss + 8);
   c->sync = reinterpret_cast<uint32_t*>(b + o_err + 64);
+  c->tiles = reinterpret_cast<uint32_t*>(b + o_err + 128);
   c->partials = reinterpret_cast<float*>(b + o_part);
   c->w8 = b + o_w8;
   c->fp8s = reinterpret_cast<nrc::Fp8State*>(b + o_fp8);
@@ -291,9 +291,6 @@ int nrc_destroy(nrc_context* c) {
   if (dev != c->device) cudaSetDevice(c->device);
   cudaDeviceSynchronize();
   cudaFree(c->block);
-  if (c->side) cudaStreamDestroy(c->side);
-  if (c->ev_fork) cudaEventDestroy(c->ev_fork);
-  if (c->ev_join) cudaEventDestroy(c->ev_join);
   if (dev >= 0 && dev != c->device) cudaSetDevice(dev);
   delete c;
   return NRC_OK;
@@ -516,41 +513,51 @@ int nrc_frame_overlapped(nrc_context* c, const nrc_input* eval_in, const uint32_
                       plan.train_ctas > nrc::train_grid(nrc::TrainParams{}, c->num_sms)))
     return NRC_ERROR_INVALID_ARGUMENT;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  if (!sequential && c->side == nullptr) {
-    if (cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess)
-      return NRC_ERROR_CUDA;
-  }
-  cudaStream_t ts = sequential ? st : c->side;
   cudaError_t e = cudaSuccess;
-  if (!sequential) {
-    if ((e = cudaEventRecord(c->ev_fork, st)) != cudaSuccess || (e = cudaStreamWaitEvent(ts, c->ev_fork, 0)) != cudaSuccess)
+  nrc::QueryOut q = {};
+  q.out = out;
+  q.clamp = 1;
+  nrc::TrainParams p = train_params(c, NRC_TRAIN_BATCH_COUNT, nrc::kTrainStep);
+  for (int b = 0; b < NRC_TRAIN_BATCH_COUNT; ++b)
+    p.batch[b] = nrc::TrainBatch{train_rec[b], train_counts[b], train_capacity, b == NRC_TRAIN_BATCH_COUNT - 1 ? 1 : 0};
+  if (sequential) {
+    // the query with the current rendering weights, then the training, which writes them
+    if (eval_capacity > 0) {
+      e = nrc::launch_infer(eval_in, false, d_eval_count, eval_capacity, &c->map_use16, q, c->err, c->num_sms, st,
+                            c->bf16);
+      if (e != cudaSuccess) return from_cuda(e);
+    }
+    if (query_event != nullptr && (e = cudaEventRecord(static_cast<cudaEvent_t>(query_event), st)) != cudaSuccess)
       return from_cuda(e);
+    p.use16 = c->use16;
+    e = nrc::launch_train(p, &c->map_w16, c->num_sms, st);
+    if (e != cudaSuccess) return from_cuda(e);
+    return fp8_refresh(c, 0, st);
   }
-  // the query reads the current rendering weights ...
+  // Overlapped: the training first, on plan.train_ctas SMs, writing the new
+  // rendering weights to a staging buffer; behind it in the stream the query,
+  // a grid over every SM that takes its tiles from a counter and starts as soon
+  // as all training CTAs run (programmatic dependence, no wait for the
+  // training's end): plan.query_ctas of its CTAs start beside the training and
+  // the others on the training's SMs as it finishes.
+  // The staged weights are copied into use_weights by whichever of the two
+  // kernels finishes last (its last CTA out), so no copy waits between frames.
+  nrc::FrameJoin join = {};
+  join.counter = c->tiles + 2;
+  join.src = reinterpret_cast<const uint4*>(c->use_next);
+  join.dst = reinterpret_cast<uint4*>(c->use16);
+  join.arrivals = eval_capacity > 0 ? 2u : 1u;
+  p.use16 = c->use_next;
+  p.join = join;
+  e = nrc::launch_train(p, &c->map_w16, static_cast<int>(plan.train_ctas), st);
+  if (e != cudaSuccess) return from_cuda(e);
   if (eval_capacity > 0) {
-    nrc::QueryOut q = {};
-    q.out = out;
-    q.clamp = 1;
-    e = nrc::launch_infer(eval_in, false, d_eval_count, eval_capacity, &c->map_use16, q, c->err,
-                          sequential ? c->num_sms : static_cast<int>(plan.query_ctas), st, c->bf16);
+    e = nrc::launch_infer_frame(eval_in, d_eval_count, eval_capacity, &c->map_use16, q, c->err, c->tiles, join,
+                                nrc::infer_grid(eval_capacity, c->num_sms), st, c->bf16);
     if (e != cudaSuccess) return from_cuda(e);
   }
   if (query_event != nullptr && (e = cudaEventRecord(static_cast<cudaEvent_t>(query_event), st)) != cudaSuccess)
     return from_cuda(e);
-  // ... while the training writes the next ones beside them, copied in once both are done
-  nrc::TrainParams p = train_params(c, NRC_TRAIN_BATCH_COUNT, nrc::kTrainStep);
-  for (int b = 0; b < NRC_TRAIN_BATCH_COUNT; ++b)
-    p.batch[b] = nrc::TrainBatch{train_rec[b], train_counts[b], train_capacity, b == NRC_TRAIN_BATCH_COUNT - 1 ? 1 : 0};
-  p.use16 = sequential ? c->use16 : c->use_next;
-  e = nrc::launch_train(p, &c->map_w16, sequential ? c->num_sms : static_cast<int>(plan.train_ctas), ts);
-  if (e != cudaSuccess) return from_cuda(e);
-  if (!sequential) {
-    if ((e = cudaEventRecord(c->ev_join, ts)) != cudaSuccess || (e = cudaStreamWaitEvent(st, c->ev_join, 0)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(c->use16, c->use_next, kParams * 2, cudaMemcpyDeviceToDevice, st)) != cudaSuccess)
-      return from_cuda(e);
-  }
   return fp8_refresh(c, 0, st);
 }
 

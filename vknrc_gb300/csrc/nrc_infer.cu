@@ -34,12 +34,14 @@ constexpr uint32_t kBarOff = kRecSmemOff + kSlots * 2 * kRecTileBytes;
 constexpr uint32_t kSmemBytes = kBarOff + 512 + 1024;  // + alignment slack
 static_assert(kWeightSmemBytes % 1024 == 0, "weight tiles 1024-aligned");
 static_assert(kSlots * kSlotCols <= 512, "TMEM columns");
+static_assert(kJoinChunks * 16 == kParams * 2, "join copy covers the weights");
 
 struct SlotBars {
   uint64_t rec_full[2];   // bulk copy of a record tile landed (tx bytes)
   uint64_t rec_empty[2];  // all 128 threads of the slot finished reading the stage
   uint64_t a_ready;       // 4 arrivals (one per warp): A operand in TMEM for the next layer
   uint64_t d_ready;       // MMA commit: accumulator ready
+  uint32_t tile[2];       // dynamic tiles: the tile (or end mark) whose records land in stage b
 };
 static_assert(sizeof(SlotBars) * kSlots + 16 <= 512, "barrier area (+ weight barrier, TMEM slot)");
 
@@ -119,6 +121,7 @@ __device__ __forceinline__ void scatter_query(const QueryOut& Q, uint32_t dst, f
 // 64..127 being zero and never read).
 template <bool kEncoded, bool kScatter, int N, int kFmt>
 __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_constant__ InferLaunch<N> L) {
+
   constexpr bool kBF16 = kFmt == 1, kF8 = kFmt == 2;
   int job = 0;
   while (job + 1 < L.njobs && blockIdx.x >= L.group_start[job + 1]) ++job;
@@ -138,6 +141,8 @@ __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_co
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
+  // dynamic tiles (single-cache record queries with a tile counter)
+  const bool dyn = N == 1 && !kEncoded && J.tiles != nullptr;
   if (threadIdx.x == 0) {
     for (int s = 0; s < kSlots; ++s) {
       mbar_init(&bars[s].rec_full[0], 1);
@@ -150,8 +155,9 @@ __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_co
     mbar_init(w_full, 1);
     mbar_fence_init();
   }
-  // Everything below may read what the preceding kernel in the stream wrote.
-  griddep_wait();
+  // Everything below may read what the preceding kernel in the stream wrote
+  // (unless this launch reads nothing of it: no_wait).
+  if (!J.no_wait) griddep_wait();
   griddep_launch_dependents();
   const uint32_t n = min(*J.d_count, J.capacity);
   const float inv_sx0 = kF8 ? J.fp8->inv_sx0 : 1.0f;  // written by the preceding refresh launch
@@ -180,16 +186,33 @@ __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_co
   const nrc_input* rec_in = static_cast<const nrc_input*>(input);
   auto tile_of = [&](uint32_t it) { return (it * G + rank) * kSlots + s; };
 
-  if (!kEncoded && leader) {
-    for (uint32_t b = 0; b < 2; ++b)
-      if (tile_of(b) < num_tiles)
-        issue_record_tile(rec_in, tile_of(b), n, stage0 + b * kRecTileBytes, &B.rec_full[b]);
-  }
+  // The copy of the slot's tile into record stage b; with dynamic tiles the
+  // tile comes from the counter and is published with the stage (an end mark,
+  // a plain arrival, once the tiles are exhausted).
+  auto fill_stage = [&](uint32_t b, uint32_t static_tile) {
+    if (dyn) {
+      const uint32_t t = atomicAdd(J.tiles, 1u);
+      B.tile[b] = t;
+      if (t < num_tiles)
+        issue_record_tile(rec_in, t, n, stage0 + b * kRecTileBytes, &B.rec_full[b]);
+      else
+        mbar_arrive(&B.rec_full[b]);
+    } else if (static_tile < num_tiles) {
+      issue_record_tile(rec_in, static_tile, n, stage0 + b * kRecTileBytes, &B.rec_full[b]);
+    }
+  };
+  if (!kEncoded && leader)
+    for (uint32_t b = 0; b < 2; ++b) fill_stage(b, tile_of(b));
   bool ok = true;
   uint32_t ph_d = 0, ph_a = 0;
   if (issuer) ok = warp_all(mbar_wait(w_full, 0, kWaitLimitNs));  // before this slot's first MMA
   for (uint32_t it = 0; ok; ++it) {
-    const uint32_t tile = tile_of(it);
+    uint32_t tile = tile_of(it);
+    if (dyn) {  // the slot's next tile (or the end mark) arrives with its record stage
+      ok = warp_all(mbar_wait(&B.rec_full[it & 1], (it >> 1) & 1, kWaitLimitNs));
+      if (!ok) break;
+      tile = *reinterpret_cast<volatile uint32_t*>(&B.tile[it & 1]);
+    }
     if (tile >= num_tiles) break;
     const uint32_t rows_valid = min(static_cast<uint32_t>(kTile), n - tile * kTile);
     const size_t grow = static_cast<size_t>(tile) * kTile + row;
@@ -198,8 +221,10 @@ __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_co
     if (!kEncoded) {
       const uint32_t b = it & 1;
       uint8_t* stage = stage0 + b * kRecTileBytes;
-      ok = warp_all(mbar_wait(&B.rec_full[b], (it >> 1) & 1, kWaitLimitNs));
-      if (!ok) break;
+      if (!dyn) {
+        ok = warp_all(mbar_wait(&B.rec_full[b], (it >> 1) & 1, kWaitLimitNs));
+        if (!ok) break;
+      }
       const uint32_t bulk = rows_valid == kTile ? kRecTileBytes : ((rows_valid * kRecBytes) & ~15u);
       float r[kInFloats];
       if (row < static_cast<int>(rows_valid)) {
@@ -223,11 +248,11 @@ __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_co
       } else {
         encode_input<kBF16>(r, e);
       }
-      if (leader && tile_of(it + 2) < num_tiles) {
+      if (leader && (dyn || tile_of(it + 2) < num_tiles)) {
         if (!mbar_wait(&B.rec_empty[b], (it >> 1) & 1, kWaitLimitNs))
           atomicOr(err, kErrTimeout);
         else
-          issue_record_tile(rec_in, tile_of(it + 2), n, stage, &B.rec_full[b]);
+          fill_stage(b, tile_of(it + 2));
       }
     } else {
       const uint16_t* enc_in = static_cast<const uint16_t*>(input);
@@ -335,6 +360,22 @@ __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_co
     tc_fence_after();
     tmem_dealloc(tmem, 512);
   }
+  // dynamic tiles: the last CTA out, when every CTA has taken its last tile,
+  // returns the counters to zero for the next launch and joins the frame
+  if (dyn) {
+    uint32_t* last = tmem_slot;  // free once TMEM is released
+    if (threadIdx.x == 0) {
+      __threadfence();
+      *last = atomicAdd(J.tiles + 1, 1u) == gridDim.x - 1 ? 1u : 0u;
+      if (*last != 0u) {
+        atomicExch(J.tiles, 0u);
+        atomicExch(J.tiles + 1, 0u);
+        __threadfence();
+      }
+    }
+    __syncthreads();
+    if (*last != 0u && J.join.counter != nullptr) frame_join(J.join, last + 1);
+  }
 }
 
 template <bool kEncoded, bool kScatter, int N, int kFmt>
@@ -388,6 +429,7 @@ cudaError_t launch_infer(const void* input, bool encoded, const uint32_t* d_coun
   const uint32_t grid = infer_grid(capacity, num_sms);
   if (grid == 0) return cudaSuccess;
   InferLaunch<1> L;
+  L.job[0] = InferJob{};
   L.job[0].wmap = *wmap;
   L.job[0].input = input;
   L.job[0].d_count = d_count;
@@ -398,6 +440,29 @@ cudaError_t launch_infer(const void* input, bool encoded, const uint32_t* d_coun
   L.group_start[1] = grid;
   L.njobs = 1;
   if (encoded) return bf16 ? cudaErrorInvalidValue : launch<true, false, 1, 0>(L, grid, stream);
+  if (q.dst != nullptr)
+    return bf16 ? launch<false, true, 1, 1>(L, grid, stream) : launch<false, true, 1, 0>(L, grid, stream);
+  return bf16 ? launch<false, false, 1, 1>(L, grid, stream) : launch<false, false, 1, 0>(L, grid, stream);
+}
+
+cudaError_t launch_infer_frame(const nrc_input* input, const uint32_t* d_count, uint32_t capacity,
+                               const CUtensorMap* wmap, const QueryOut& q, uint32_t* err, uint32_t* tiles,
+                               const FrameJoin& join, uint32_t grid, cudaStream_t stream, bool bf16) {
+  if (grid == 0 || tiles == nullptr) return cudaErrorInvalidValue;
+  InferLaunch<1> L;
+  L.job[0] = InferJob{};
+  L.job[0].wmap = *wmap;
+  L.job[0].input = input;
+  L.job[0].d_count = d_count;
+  L.job[0].capacity = capacity;
+  L.job[0].err = err;
+  L.job[0].q = q;
+  L.job[0].tiles = tiles;
+  L.job[0].no_wait = 1;
+  L.job[0].join = join;
+  L.group_start[0] = 0;
+  L.group_start[1] = grid;
+  L.njobs = 1;
   if (q.dst != nullptr)
     return bf16 ? launch<false, true, 1, 1>(L, grid, stream) : launch<false, true, 1, 0>(L, grid, stream);
   return bf16 ? launch<false, false, 1, 1>(L, grid, stream) : launch<false, false, 1, 0>(L, grid, stream);

@@ -55,6 +55,42 @@ cudaError_t launch_infer(const void* input, bool encoded, const uint32_t* d_coun
                          const CUtensorMap* wmap, const QueryOut& q, uint32_t* err, int num_sms,
                          cudaStream_t stream, bool bf16 = false);
 
+// The overlapped frame's join of its two kernels: the last CTA of each adds
+// one to *counter, and the one that brings it to `arrivals` copies the staged
+// rendering weights src -> dst (kParams 16-bit words: 2,584 x 16 bytes) and
+// returns the counter to zero. No CTA waits for the other kernel. counter
+// null: no join.
+struct FrameJoin {
+  uint32_t* counter;
+  const uint4* src;
+  uint4* dst;
+  uint32_t arrivals;
+};
+
+constexpr uint32_t kJoinChunks = 2584;  // 16-byte chunks of the 20,672 16-bit weights
+
+#ifdef __CUDACC__
+// FrameJoin, called by every thread of its kernel's last CTA (after the
+// kernel's writes are complete and fenced by the CTA that made them).
+// `slot`: a shared-memory word for the CTA's decision.
+__device__ __forceinline__ void frame_join(const FrameJoin& j, uint32_t* slot) {
+  if (threadIdx.x == 0) {
+    __threadfence();
+    *slot = atomicAdd(j.counter, 1u) == j.arrivals - 1 ? 1u : 0u;
+    __threadfence();
+  }
+  __syncthreads();
+  if (*slot != 0u) {
+    for (uint32_t i = threadIdx.x; i < kJoinChunks; i += blockDim.x) j.dst[i] = j.src[i];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      atomicExch(j.counter, 0u);
+    }
+  }
+}
+#endif
+
 // One cache's share of a query launch.
 struct InferJob {
   CUtensorMap wmap;
@@ -64,6 +100,15 @@ struct InferJob {
   uint32_t* err;
   QueryOut q;
   const Fp8State* fp8;  // the FP8 query's scales (fp8 launches only)
+  // Dynamic tiles (single-cache record queries): tiles[0] hands out the next
+  // tile, tiles[1] counts exiting CTAs (both zero between launches; the last
+  // CTA resets them). Null: each CTA takes a fixed share of the tiles.
+  uint32_t* tiles;
+  // 1: start without waiting for the preceding grid in the stream (the
+  // overlapped frame's query, launched behind the training it runs beside,
+  // reads nothing that training writes).
+  uint32_t no_wait;
+  FrameJoin join;  // dynamic tiles only: joined by the last CTA out
 };
 
 // Kernel parameters of a query launch over up to N caches; CTAs
@@ -90,6 +135,14 @@ cudaError_t launch_fp8_refresh(const uint16_t* use16, bool bf16, const nrc_optim
 
 // CTAs the query kernel uses for `capacity` records on `num_sms` SMs.
 uint32_t infer_grid(uint32_t capacity, int num_sms);
+// The overlapped frame's query: `grid` CTAs taking tiles from the counter
+// pair `tiles` (zero between launches), started without waiting for the
+// preceding grid (the training launched just before it on `stream`, which
+// signals its dependents once all of its CTAs run): the CTAs that find no free
+// SM start on the training's SMs as it finishes.
+cudaError_t launch_infer_frame(const nrc_input* input, const uint32_t* d_count, uint32_t capacity,
+                               const CUtensorMap* wmap, const QueryOut& q, uint32_t* err, uint32_t* tiles,
+                               const FrameJoin& join, uint32_t grid, cudaStream_t stream, bool bf16);
 // One launch answering njobs caches' record queries (dense rgb output, no
 // destination words), group_size[j] >= 1 CTAs for job j, sum <= SMs.
 cudaError_t launch_infer_many(const InferJob* jobs, int njobs, const uint32_t* group_size, cudaStream_t stream,
@@ -128,6 +181,7 @@ struct TrainParams {
   uint32_t* err;
   int bf16;          // weights and operands in bf16 (host side: selects the kernel)
   uint32_t* amax;    // Fp8State::amax_x of a cache with fp8 inference, or null
+  FrameJoin join;    // joined by the last CTA out
 };
 
 // One cache's share of a training launch: its weight tensor map and parameters.

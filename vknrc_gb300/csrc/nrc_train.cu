@@ -295,6 +295,11 @@ __global__ void __launch_bounds__(kTrainThreads, 1) train_steps_kernel(const __g
   }
   // Everything below may read what the preceding kernel in the stream wrote.
   griddep_wait();
+  // A dependent launch may start once every CTA of this cooperative grid runs
+  // (the overlapped frame's query, which reads nothing this launch writes and
+  // fills the SMs this grid leaves free); dependents that read this launch's
+  // results wait for its completion in their own griddepcontrol.wait.
+  griddep_launch_dependents();
 
   // This CTA's slice [c0, c1) of float4 gradient columns in the optimizer phase;
   // its optimizer entries stay in shared memory for the whole launch (only this
@@ -745,11 +750,18 @@ __global__ void __launch_bounds__(kTrainThreads, 1) train_steps_kernel(const __g
   // resets it and the exit counter (sync[1]).
   if (threadIdx.x == 0) {
     __threadfence();
-    if (atomicAdd(P.sync + 1, 1u) == G - 1) {
+    B->sync_ok = atomicAdd(P.sync + 1, 1u) == G - 1 ? 1u : 0u;
+    if (B->sync_ok != 0u) {
       atomicExch(P.sync, 0u);
       atomicExch(P.sync + 1, 0u);
       __threadfence();
     }
+  }
+  // the overlapped frame: the group's last CTA out joins the frame (every CTA's
+  // weight writes are complete and fenced by now)
+  if (P.join.counter != nullptr) {
+    __syncthreads();
+    if (B->sync_ok != 0u) frame_join(P.join, &B->tmem_base);
   }
 }
 
