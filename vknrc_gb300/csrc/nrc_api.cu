@@ -36,7 +36,8 @@ struct nrc_context {
   nrc::Fp8State* fp8s = nullptr;
   CUtensorMap map_w8;
   __half* use_next = nullptr;   // the overlapped frame's training writes use_weights here first
-  nrc_frame_plan plan = {0u, 0u};  // the overlapped frame's split (0, 0: default)
+  nrc_frame_plan plan = {0u, 0u};  // the overlapped frame's split, once tuned
+  bool plan_tuned = false;         // nrc_autotune_frame has set `plan` (which may be sequential)
 };
 
 namespace nrc {
@@ -504,7 +505,7 @@ int nrc_frame_overlapped(nrc_context* c, const nrc_input* eval_in, const uint32_
     if (!aligned16(eval_in) || (reinterpret_cast<uintptr_t>(out) & 3u)) return NRC_ERROR_MISALIGNED;
   }
   nrc_frame_plan plan = plan_in ? *plan_in : c->plan;
-  if (plan_in == nullptr && plan.query_ctas == 0 && plan.train_ctas == 0) {
+  if (plan_in == nullptr && !c->plan_tuned) {
     plan.train_ctas = static_cast<uint32_t>(c->num_sms) / 4;  // default split before any tuning
     plan.query_ctas = static_cast<uint32_t>(c->num_sms) - plan.train_ctas;
   }
@@ -625,6 +626,7 @@ int nrc_autotune_frame(nrc_context* c, const nrc_input* eval_in, const uint32_t*
   if (s != NRC_OK) return s;
   if (e != cudaSuccess) return from_cuda(e);
   c->plan = best;
+  c->plan_tuned = true;
   if (best_out) *best_out = best;
   if (best_ms) *best_ms = best_t;
   return NRC_OK;
