@@ -246,7 +246,7 @@ typedef struct nrc_frame_plan {
  * reference's frame reads use_weights in its query and writes them in its last
  * training step (src/rg/NRCRenderGraph.cpp:52, :77); here the training writes
  * them into a second buffer of the context, copied into use_weights (41 KB) by
- * whichever of the two kernels finishes last, once both are done. The
+ * the query's last CTA once both kernels are done. The
  * query therefore reads exactly the weights it reads in nrc_frame, and
  * use_weights change only at the end of the call, as there. The training runs
  * with plan->train_ctas CTAs, so its gradient sums are grouped as

@@ -374,7 +374,15 @@ __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_co
       }
     }
     __syncthreads();
-    if (*last != 0u && J.join.counter != nullptr) frame_join(J.join, last + 1);
+    if (*last != 0u) {
+      // A launch that started without waiting for the preceding grid (the
+      // overlapped frame's training) completes only after it: the last CTA
+      // waits for that grid here, so that whatever follows this query in the
+      // stream also follows the training. The training is resident (this grid
+      // launched once all of its CTAs ran) and never waits for the query.
+      if (J.no_wait) griddep_wait();
+      if (J.join.counter != nullptr) frame_join(J.join, last + 1);
+    }
   }
 }
 

@@ -55,11 +55,12 @@ cudaError_t launch_infer(const void* input, bool encoded, const uint32_t* d_coun
                          const CUtensorMap* wmap, const QueryOut& q, uint32_t* err, int num_sms,
                          cudaStream_t stream, bool bf16 = false);
 
-// The overlapped frame's join of its two kernels: the last CTA of each adds
-// one to *counter, and the one that brings it to `arrivals` copies the staged
-// rendering weights src -> dst (kParams 16-bit words: 2,584 x 16 bytes) and
-// returns the counter to zero. No CTA waits for the other kernel. counter
-// null: no join.
+// The overlapped frame's copy of the staged rendering weights src -> dst
+// (kParams 16-bit words: 2,584 x 16 bytes), made by the last CTA out of the
+// kernel that ends the frame (the query, after its wait for the training grid;
+// the training when the frame has no query). Each arrival adds one to
+// *counter, the one that brings it to `arrivals` copies and returns the
+// counter to zero. counter null: no copy.
 struct FrameJoin {
   uint32_t* counter;
   const uint4* src;

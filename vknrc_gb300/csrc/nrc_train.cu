@@ -767,16 +767,22 @@ __global__ void __launch_bounds__(kTrainThreads, 1) train_steps_kernel(const __g
 
 template <int N>
 cudaError_t launch(const TrainLaunch<N>& L, uint32_t grid, cudaStream_t stream, bool bf16) {
-  cudaLaunchAttribute attr;
-  attr.id = cudaLaunchAttributeCooperative;
-  attr.val.cooperative = 1;
+  // Cooperative (the grid barrier needs every CTA resident) and a programmatic
+  // dependent of the preceding kernel: the launch is issued before that kernel
+  // ends, its CTAs take SMs as the preceding kernel's CTAs leave, and
+  // griddepcontrol.wait holds them until it has completed.
+  cudaLaunchAttribute attr[2];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[1].val.programmaticStreamSerializationAllowed = 1;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
   cfg.blockDim = dim3(kTrainThreads);
   cfg.dynamicSmemBytes = kTrainSmemBytes;
   cfg.stream = stream;
-  cfg.attrs = &attr;
-  cfg.numAttrs = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 2;
   return bf16 ? cudaLaunchKernelEx(&cfg, train_steps_kernel<N, true>, L)
               : cudaLaunchKernelEx(&cfg, train_steps_kernel<N, false>, L);
 }
