@@ -883,7 +883,8 @@ def ours_arm(args, world, rank, local):
         "e2e": {"value": world * Q * E / e2e_s, "unit": "queries/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "steps": E,
                 "schedule": "pinned host buffers; frame k's H2D overlaps frame k-1's compute and frame k-2's D2H "
-                            "(bounded by the ~196 GB/s host-to-device copy rate: 121 MB per frame)"},
+                            "(bounded by the host-to-device link: 121 MB per frame at the ~210 GB/s that both the copy engine "
+                            "and SM loads from mapped pinned memory reach)"},
         "clocks": clocks,
     }
     if plain is not None:
