@@ -103,3 +103,32 @@ def test_overlapped_frame_graph_replays(cuda):
         assert np.array_equal(a.get_optimizer()[1], b.get_optimizer()[1])
         assert np.array_equal(a.get_weights(0), b.get_weights(0))
         assert b.error() == 0
+
+
+@pytest.mark.parametrize("queries", ["none", "zero"])
+def test_overlapped_frame_without_queries_publishes_the_weights(cuda, queries):
+    """No query launched (capacity 0: the training's last CTA copies the staged
+    rendering weights) or a query with no records (the query's last CTA copies
+    them after its wait for the training): use_weights match the grouped
+    training's either way."""
+    import torch
+
+    from vknrc_gb300 import Cache, nrc
+    from vknrc_gb300 import synthetic as S
+
+    _, recs = _frame_data(150, q=1000)
+    with Cache(seed=151) as a, Cache(seed=151) as b:
+        for k in range(2):
+            if queries == "none":
+                q = torch.empty((0, 14), dtype=torch.float32, device="cuda")
+                out = torch.empty((0, 3), dtype=torch.float32, device="cuda")
+            else:
+                q = dev(S.inputs(S.rng_for(152, k), 1000))
+                out = torch.full((1000, 3), -1.0, dtype=torch.float32, device="cuda")
+            a.frame_overlapped(q, count(0), out, recs, [count(16384) for _ in range(4)], plan=(120, 32))
+            nrc.train_many([nrc.train_job(b, recs, [count(16384) for _ in range(4)])], ctas=[32])
+            assert np.array_equal(a.get_weights(0), b.get_weights(0)), k
+            assert np.array_equal(a.get_weights(1), b.get_weights(1)), k
+            if queries == "zero":
+                assert np.all(host(out) == -1.0)  # nothing answered
+        assert a.error() == 0
