@@ -70,17 +70,33 @@ def load_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
 
 
-def load_traffic():
-    """Per-launch DRAM bytes of the query kernel at the bench's workload, from
-    the committed ncu summary (profiles/infer_kernel_1080p.md), or None."""
+def load_profile_figure(key):
+    """A per-launch figure of the query kernel at the bench's workload from the
+    committed ncu summary (profiles/infer_kernel_1080p.md): `key: value`, or None."""
     path = os.path.join(ROOT, "profiles", "infer_kernel_1080p.md")
     try:
         for line in open(path):
-            if line.startswith("traffic_bytes_per_launch:"):
+            if line.startswith(key + ":"):
                 return float(line.split(":", 1)[1].strip())
     except OSError:
         pass
     return None
+
+
+def load_traffic():
+    """DRAM bytes (read + write) of one query launch, from the ncu summary."""
+    return load_profile_figure("traffic_bytes_per_launch")
+
+
+def issue_bound(inst, sms, clocks, launch_s):
+    """The CUDA-core issue-rate bound of the query kernel: its warp instructions
+    per launch (ncu) at 4 per cycle per SM on every SM at the SM clock seen
+    under load, against the measured launch time."""
+    if inst is None or not clocks or not clocks.get("sm_mhz"):
+        return None
+    bound_s = inst / (4.0 * sms * clocks["sm_mhz"] * 1e6)
+    return {"warp_instructions_per_launch": inst, "bound_us": bound_s * 1e6, "frac": bound_s / launch_s,
+            "what": "4 warp instructions per cycle per SM, all SMs, median SM clock of the timed region"}
 
 
 class ClockSampler:
@@ -877,6 +893,7 @@ def ours_arm(args, world, rank, local):
             "peak_source": f"bf16_tflops_sustained ({peak_kind})",
             "kernel_sms": sms, "timing": "query_alone_ms: CUDA events around each launch on its stream",
             "traffic": traffic,
+            "issue": issue_bound(load_profile_figure("inst_executed_per_launch"), sms, clocks, infer_s),
             "algorithmic_flop_per_launch": FLOP_PER_QUERY * Q,
             "algorithmic_bytes_per_launch": Q * (EVAL_BYTES + OUT_BYTES),
         },
