@@ -485,34 +485,35 @@ def batched_leg(evals, trains, steps=50):
 # ------------------------------------------------------------ precision leg --
 def precision_leg(evals, trains, eval_cnt, train_cnt, steps=500):
     """The same 1080p frame with a BF16 cache (bf16 weights, features,
-    activations and gradients; fp32 master weights and moments)."""
+    activations and gradients; fp32 master weights and moments): the
+    overlapped frame with its own tuned split, as the headline's, and the
+    query kernel timed alone."""
     import torch
 
     from vknrc_gb300 import Cache
 
     out = torch.empty((Q, 3), dtype=torch.float32, device="cuda")
     with Cache(seed=1234, learning_rate=1e-3, beta2=0.99, precision=1) as c:
+        plan, _ = c.autotune_frame(evals[0], eval_cnt, out, trains[0], train_cnt)
         for k in range(5):
-            c.frame(evals[k % len(evals)], eval_cnt, out, trains[k % len(trains)], train_cnt)
-        s, m, e = (torch.cuda.Event(enable_timing=True) for _ in range(3))
-        ms_inf = []
+            c.frame_overlapped(evals[k % len(evals)], eval_cnt, out, trains[k % len(trains)], train_cnt)
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         s.record()
         for k in range(steps):
-            a = torch.cuda.Event(enable_timing=True)
-            b = torch.cuda.Event(enable_timing=True)
-            a.record()
-            c.infer(evals[k % len(evals)], eval_cnt, out)
-            b.record()
-            c.train_batches(trains[k % len(trains)], train_cnt, write_use_last=True)
-            ms_inf.append((a, b))
+            c.frame_overlapped(evals[k % len(evals)], eval_cnt, out, trains[k % len(trains)], train_cnt)
         e.record()
         torch.cuda.synchronize()
+        frame_s = s.elapsed_time(e) / 1e3 / steps
+        s.record()
+        for k in range(100):
+            c.infer(evals[k % len(evals)], eval_cnt, out)
+        e.record()
+        torch.cuda.synchronize()
+        inf_s = s.elapsed_time(e) / 1e3 / 100
         if c.error() != 0:
             raise RuntimeError("device error in the bf16 leg")
-        frame_s = s.elapsed_time(e) / 1e3 / steps
-        inf_s = statistics.mean(a.elapsed_time(b) for a, b in ms_inf) / 1e3
     return {"ms_per_frame": frame_s * 1e3, "queries_per_s": Q / frame_s, "train_records_per_s": B * R / frame_s,
-            "infer_ms": inf_s * 1e3, "steps": steps,
+            "frame_plan": list(plan), "infer_ms": inf_s * 1e3, "steps": steps,
             "accuracy": "tests/test_gpu_precision.py: query error and 1000-step loss against the FP64 oracle"}
 
 
