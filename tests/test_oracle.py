@@ -146,3 +146,58 @@ def test_optimizer_step_semantics(oracle):
     before = opt.entries.copy()
     opt.adam(grad, 0)
     assert np.array_equal(before, opt.entries)
+
+
+def test_e4m3_conversion_follows_the_format(oracle):
+    """oracle_f32_to_e4m3 / oracle_e4m3_to_f32 (the FP8 query's conversions)
+    against the E4M3 definition: bias 7, 3 mantissa bits, subnormals at
+    2^-9, no infinities, max 448, NaN codes 0x7F/0xFF; round to nearest even,
+    saturated to +-448."""
+    codes = np.arange(256, dtype=np.uint8)
+    vals = oracle.e4m3_decode(codes)
+    finite = ~np.isnan(vals)
+    assert set(codes[~finite].tolist()) == {0x7F, 0xFF}
+    s, e, m = codes >> 7, (codes >> 3) & 15, (codes & 7).astype(np.float64)
+    mag = np.where(e == 0, m * 2.0 ** -9, (1.0 + m / 8.0) * 2.0 ** (e.astype(np.int64) - 7))
+    ref = np.where(s == 1, -mag, mag).astype(np.float32)
+    assert np.array_equal(vals[finite], ref[finite])
+    assert np.array_equal(oracle.e4m3(vals[finite]), codes[finite])  # every finite code round-trips
+    assert oracle.e4m3([448.0, 449.0, 1000.0, 1e30, -1e30]).tolist() == [0x7E, 0x7E, 0x7E, 0x7E, 0xFE]
+    assert oracle.e4m3([float("nan")]).tolist() == [0x7F]
+    # midpoints between neighbours (and between 0 and the smallest subnormal)
+    # go to the even code; a hair either side goes to the nearer neighbour
+    pos = np.concatenate([[0.0], np.sort(vals[finite & (vals > 0)]).astype(np.float64)])
+    lo, hi = pos[:-1], pos[1:]
+    mid = ((lo + hi) / 2).astype(np.float32)
+    c_lo, c_hi = oracle.e4m3(lo.astype(np.float32)), oracle.e4m3(hi.astype(np.float32))
+    want = np.where(c_lo % 2 == 0, c_lo, c_hi)
+    assert np.array_equal(oracle.e4m3(mid), want)
+    below = np.nextafter(mid, np.float32(0))
+    above = np.nextafter(mid, np.float32(np.inf))
+    assert np.array_equal(oracle.e4m3(below), c_lo)
+    assert np.array_equal(oracle.e4m3(above), c_hi)
+    assert np.array_equal(oracle.e4m3(-mid), want | 0x80)
+
+
+def test_fp8_quantize_scales_and_weights(oracle):
+    """oracle_fp8_quantize: per-layer weight scale max|W_l| / 448, its inverse,
+    and each weight e4m3(w * 448 / max|W_l|); with no observed activations the
+    input scales follow the bound max|x_l| <= max|x_{l-1}| * max row sum |W|
+    from max|x_0| = 1, and c[l] = s_w[l] s_x[l] / s_x[l+1]."""
+    rng = np.random.default_rng(5)
+    w = (rng.standard_normal(20672) * np.sqrt(2 / 64)).astype(np.float16)
+    w8, st = oracle.fp8_quantize(w.view(np.uint16))
+    s_w, s_x, c, inv_sx0, inv_w = st[0:6], st[6:12], st[12:18], st[18], st[19:25]
+    layer = np.minimum(np.arange(20672) // 4096, 5)
+    wf = w.astype(np.float32)
+    amax = np.array([np.abs(wf[layer == l]).max() for l in range(6)], np.float32)
+    assert np.array_equal(s_w, amax / np.float32(448))
+    assert np.array_equal(inv_w, np.float32(448) / amax)
+    assert np.array_equal(w8, oracle.e4m3(wf * inv_w[layer]))
+    rowsum = [np.abs(wf[layer == l].reshape(-1, 64)).sum(1).max() for l in range(6)]
+    ax = [1.0]
+    for l in range(1, 6):
+        ax.append(ax[-1] * rowsum[l - 1])
+    assert np.allclose(s_x, np.array(ax) / 448, rtol=1e-5)
+    assert np.allclose(c[:5], s_w[:5] * s_x[:5] / s_x[1:], rtol=1e-6)
+    assert np.isclose(c[5], s_w[5] * s_x[5], rtol=1e-6) and np.isclose(inv_sx0, 1 / s_x[0], rtol=1e-6)
