@@ -201,3 +201,18 @@ def test_fp8_quantize_scales_and_weights(oracle):
     assert np.allclose(s_x, np.array(ax) / 448, rtol=1e-5)
     assert np.allclose(c[:5], s_w[:5] * s_x[:5] / s_x[1:], rtol=1e-6)
     assert np.isclose(c[5], s_w[5] * s_x[5], rtol=1e-6) and np.isclose(inv_sx0, 1 / s_x[0], rtol=1e-6)
+
+
+def test_encode_f32_rounds_to_the_16_bit_encodings(oracle):
+    """oracle_encode_f32 (the FP8 query's unrounded features) rounded to fp16
+    (numpy's round to nearest even) and to bf16 (round to nearest even on the
+    bit pattern) gives oracle_encode's fp16 and bf16 features bit for bit."""
+    from vknrc_gb300 import synthetic as S
+
+    rec = S.inputs(S.rng_for(91), 4096)
+    rec[:7, 0] = [0.0, -0.0, 1e-30, 3.75, -2.5e6, 1e38, 0.5]  # edge positions (large, tiny, exact)
+    f = oracle.encode_f32(rec)
+    assert np.array_equal(f.astype(np.float16).view(np.uint16), oracle.encode(rec, 0))
+    u = f.view(np.uint32).astype(np.uint64)
+    bf = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16).astype(np.uint16)
+    assert np.array_equal(bf, oracle.encode(rec, 1))
