@@ -67,7 +67,7 @@ typedef struct nrc_train_record {
   nrc_input input;
 } nrc_train_record;
 
-/* Optimizer step state and per-parameter entry (src/VkNRCState.cpp:117-123). */
+/* Optimizer step state and per-parameter entry (src/VkNRCState.cpp:25-31). */
 typedef struct nrc_optimizer_state {
   uint32_t t;
   float beta1_t, beta2_t, alpha_t, alpha_t_1;
@@ -132,7 +132,7 @@ NRC_API const char* nrc_status_string(int status);
 NRC_API int nrc_default_config(nrc_config* cfg);
 
 /* Creates a cache on the current CUDA device and initialises it as
- * VkNRCState::ResetMLPBuffers does (src/VkNRCState.cpp:138-180): He-normal
+ * VkNRCState::ResetMLPBuffers does (src/VkNRCState.cpp:46-88): He-normal
  * weights N(0, sqrt(2/64)) from std::mt19937(seed) and
  * std::normal_distribution<float>, fp16 copies in weights and use_weights, zero
  * moments, state {0, 1, 1, 1, 0}. Synchronous. */
@@ -143,7 +143,7 @@ NRC_API int nrc_destroy(nrc_context* ctx);
 NRC_API int nrc_reset(nrc_context* ctx, uint64_t seed);
 
 /* The He initialisation of nrc_create on the host, without a device:
- * out_weights receives NRC_PARAM_COUNT fp32 values (src/VkNRCState.cpp:131-136). */
+ * out_weights receives NRC_PARAM_COUNT fp32 values (src/VkNRCState.cpp:39-44). */
 NRC_API int nrc_he_init_host(uint64_t seed, float* out_weights);
 
 /* Input encoding alone: NRCInputEncode (shader/src/NRCRecord.glsl:78-95) of
@@ -286,13 +286,38 @@ NRC_API int nrc_frame_scatter(nrc_context* ctx, const nrc_input* d_eval_inputs, 
                               const uint32_t* d_eval_count, uint32_t eval_capacity,
                               const nrc_scatter_targets* targets, uint32_t* const* d_train_counts, void* stream);
 
+/* The reference's prepare and optimizer passes on a weight-gradient sum the
+ * caller computed (NNTrain's prepare_pass and optimizer_pass,
+ * src/rg/NNTrain.hpp:95-118; nrc_train_prepare.comp:16-29 then
+ * nrc_optimize.comp:32-54): *d_count is clamped to cfg.train_batch_size and
+ * written back; if it is non-zero the step state advances and every parameter i
+ * is updated from d_grad_sum[i] / count / loss_scale (NaN and Inf scrubbed to
+ * 0), writing the fp32 entries, the 16-bit weights and, with
+ * write_use_weights, use_weights. d_grad_sum: NRC_PARAM_COUNT fp32, 16-byte
+ * aligned (nrc_gradient's output, undivided). The arithmetic is the fused
+ * trainer's optimizer phase. Stream-ordered, two launches. */
+NRC_API int nrc_optimize(nrc_context* ctx, const float* d_grad_sum, uint32_t* d_count, int write_use_weights,
+                         void* stream);
+
+/* The relative-L2 luminance loss gradient rows of min(*d_count, capacity)
+ * (prediction, target) pairs (NNLoadDA3_RelativeL2LuminanceLoss,
+ * shader/src/NN_nv.glsl:178-196): d_pred and d_target n x 3 fp32 (predictions
+ * unclamped, as nrc_gradient.comp:45-46 passes them); d_rows receives per pair
+ * the two 32-bit words (d0 | d1 << 16, d2 | 0 << 16) of the 16-bit row in the
+ * given precision (NRC_PRECISION_FP16: values past 65504 become inf, as the
+ * reference's packHalf2x16 makes them). The fused trainer computes its rows with
+ * the same code; this is its check path. */
+NRC_API int nrc_loss_gradient(const float* d_pred, const float* d_target, const uint32_t* d_count, uint32_t capacity,
+                              float loss_scale, uint32_t precision, uint32_t* d_rows, void* stream);
+
 /* One training step with nrc_train's semantics that allocates no device memory.
  * No counterpart in the reference: it serves callers that cannot call cudaMalloc,
  * such as a renderer that sub-allocates every device buffer from its own heaps or
  * a process held to a fixed device-memory budget. The caller owns the parameter
  * buffers in the layouts above (fp16 weights, optional fp16 use_weights, Adam
  * entries, step state) as well as the records and the count; `cfg` supplies the
- * hyper-parameters (seed, deterministic and track_loss are ignored).
+ * hyper-parameters (seed, deterministic, track_loss and fp8_inference are
+ * ignored: no FP8 copy of the weights is kept or refreshed).
  * Scratch: the per-CTA weight-gradient partials live in a fixed array compiled
  * into the library, 5,292,288 bytes held by every GPU that loads it until the
  * process exits; it bounds one call to 16,384 records: if min(capacity,
@@ -303,7 +328,10 @@ NRC_API int nrc_frame_scatter(nrc_context* ctx, const nrc_input* d_eval_inputs, 
  * Every call uses the same scratch: calls that may overlap on the GPU (other
  * streams, no ordering) race; order them. d_error (may be NULL) receives the
  * device-timeout flag; when NULL a word in the scratch is used, cleared on each
- * call. */
+ * call, which the caller cannot read: a step that hit a bounded-wait timeout
+ * then still returns NRC_OK, so pass d_error to observe timeouts. Pointers that
+ * are not aligned to their types (16 bytes for weights, entries and records;
+ * 4 for the state, count and error words) return NRC_ERROR_MISALIGNED. */
 NRC_API int nrc_train_noalloc(uint16_t* d_weights, uint16_t* d_use_weights, nrc_optimizer_entry* d_entries,
                               nrc_optimizer_state* d_state, const nrc_train_record* d_records, uint32_t* d_count,
                               uint32_t capacity, const nrc_config* cfg, uint32_t* d_error, void* stream);
@@ -597,7 +625,7 @@ NRC_API int nrc_path_trace(const nrc_scene* scene, const nrc_bvh* bvh, const nrc
  * (white point 3.2) and gamma 1/2.2; results to d_out_rgba8 (UNORM8, alpha 255)
  * and/or d_out_rgba (float, alpha 1), either may be NULL. The tone curve's small
  * negative values near black take pow() of 0. Replaces rg::ScreenPass
- * (src/rg/ScreenPass.cpp:62-71) minus the swapchain. */
+ * (src/rg/ScreenPass.cpp:60-68) minus the swapchain. */
 NRC_API int nrc_screen(const float* d_color, float* d_accumulate, uint32_t width, uint32_t height, int accumulate,
                        uint32_t accumulate_count, uint8_t* d_out_rgba8, float* d_out_rgba, void* stream);
 

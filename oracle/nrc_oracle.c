@@ -298,6 +298,18 @@ static inline void loss_grad_f32(const float p[3], const float t[3], float s, fl
   for (int c = 0; c < 3; ++c) d[c] = (s2 * (p[c] - t[c])) / den;
 }
 
+/* The relative-L2 gradient rows as the reference stores them (NN_nv.glsl:185-186):
+ * per record the words (d0 | d1 << 16, d2 | 0 << 16) of the 16-bit row, in
+ * format fmt (0 fp16, 1 bf16); values beyond the format's range become inf. */
+void oracle_loss_rows(const float* pred, const float* target, int64_t n, float loss_scale, int fmt, uint32_t* rows) {
+  for (int64_t i = 0; i < n; ++i) {
+    float d[3];
+    loss_grad_f32(pred + 3 * i, target + 3 * i, loss_scale, d);
+    rows[2 * i] = (uint32_t)to16(d[0], fmt) | ((uint32_t)to16(d[1], fmt) << 16);
+    rows[2 * i + 1] = (uint32_t)to16(d[2], fmt);
+  }
+}
+
 static inline double loss_value(const double p[3], const float t[3]) {
   const double px = p[0] > 0 ? p[0] : 0, py = p[1] > 0 ? p[1] : 0, pz = p[2] > 0 ? p[2] : 0;
   const double lum = 0.299 * px + 0.587 * py + 0.114 * pz;

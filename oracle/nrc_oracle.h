@@ -63,7 +63,12 @@ void oracle_train_grad(const uint16_t* w, const uint16_t* enc, const float* targ
 void oracle_train_grad_w64(const double* w, const uint16_t* enc, const float* target, int64_t n,
                            float loss_scale, double* grad, double* loss_sum, int nthreads);
 
-/* Optimizer state and entries (src/VkNRCState.cpp:117-123). */
+/* The relative-L2 luminance loss gradient rows (NN_nv.glsl:178-196) for n
+ * (prediction, target) pairs, each as the two 32-bit words (d0 | d1 << 16,
+ * d2 | 0 << 16) of the reference's 16-bit row; fmt 0 fp16, 1 bf16. */
+void oracle_loss_rows(const float* pred, const float* target, int64_t n, float loss_scale, int fmt, uint32_t* rows);
+
+/* Optimizer state and entries (src/VkNRCState.cpp:25-31). */
 typedef struct oracle_opt_state {
   uint32_t t;
   float beta1_t, beta2_t, alpha_t, alpha_t_1;

@@ -57,6 +57,7 @@ def lib() -> ctypes.CDLL:
         _lib.oracle_encode_f32.argtypes = [vp, i64, vp]
         _lib.oracle_fp8_quantize.argtypes = [vp, i32, vp, vp, vp]
         _lib.oracle_forward_fp8.argtypes = [vp, vp, f32, vp, i64, vp, i32]
+        _lib.oracle_loss_rows.argtypes = [vp, vp, i64, f32, i32, vp]
         _lib.oracle_expf.argtypes = [f32]
         _lib.oracle_expf.restype = f32
     return _lib
@@ -72,6 +73,11 @@ def ref_lib():
         _ref.ref_sph_encode.argtypes = [vp, i64, vp]
         _ref.ref_evaluate.argtypes = [vp, vp, i64, vp]
         _ref.ref_train.argtypes = [vp, vp, vp, i64, vp]
+        if hasattr(_ref, "ref_prepare"):
+            _ref.ref_prepare.argtypes = [ctypes.c_uint32, vp, vp]
+            _ref.ref_prepare.restype = ctypes.c_uint32
+            _ref.ref_optimize.argtypes = [vp, vp, i64, ctypes.c_uint32, vp, ctypes.c_uint32, vp, vp]
+            _ref.ref_loss_rows.argtypes = [vp, vp, i64, ctypes.c_float, vp]
     return _ref
 
 
@@ -330,6 +336,41 @@ class Optimizer:
         lib().oracle_adam_fmt(_p(self.entries), _p(g), count, ctypes.byref(self.state), ctypes.byref(self.hp),
                               _p(w16), _p(use16) if use16 is not None else None, int(use_ema), fmt)
         return w16, use16
+
+
+def loss_rows(pred: np.ndarray, target: np.ndarray, loss_scale: float = 1.0, fmt: int = 0) -> np.ndarray:
+    """(n, 2) uint32: the relative-L2 gradient row words of each (prediction, target) pair."""
+    p = _c(pred, np.float32).reshape(-1, 3)
+    t = _c(target, np.float32).reshape(-1, 3)
+    out = np.empty((p.shape[0], 2), np.uint32)
+    lib().oracle_loss_rows(_p(p), _p(t), p.shape[0], float(loss_scale), fmt, _p(out))
+    return out
+
+
+def ref_prepare(count: int, state: OptState):
+    """nrc_train_prepare.comp compiled from the reference: (clamped count, work groups); advances state."""
+    r = ref_lib()
+    groups = ctypes.c_uint32(0)
+    n = r.ref_prepare(count, ctypes.byref(state), ctypes.byref(groups))
+    return n, groups.value
+
+
+def ref_optimize(entries: np.ndarray, grad: np.ndarray, count: int, state: OptState, use_ema: bool,
+                 w16: np.ndarray, use16: np.ndarray) -> None:
+    """nrc_optimize.comp compiled from the reference, in place on entries / w16 / use16."""
+    assert entries.dtype == np.float32 and entries.flags.c_contiguous and entries.shape == (P, 4)
+    assert w16.dtype == np.uint16 and use16.dtype == np.uint16
+    g = _c(grad, np.float32)
+    ref_lib().ref_optimize(_p(entries), _p(g), P, count, ctypes.byref(state), int(use_ema), _p(w16), _p(use16))
+
+
+def ref_loss_rows(pred: np.ndarray, target: np.ndarray, loss_scale: float = 1.0) -> np.ndarray:
+    """NNLoadDA3_RelativeL2LuminanceLoss compiled from the reference: (n, 2) uint32 row words."""
+    p = _c(pred, np.float32).reshape(-1, 3)
+    t = _c(target, np.float32).reshape(-1, 3)
+    out = np.empty((p.shape[0], 2), np.uint32)
+    ref_lib().ref_loss_rows(_p(p), _p(t), p.shape[0], float(loss_scale), _p(out))
+    return out
 
 
 def ref_encode(records: np.ndarray):

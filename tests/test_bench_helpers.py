@@ -18,12 +18,23 @@ def _bench():
 
 def test_profile_figures_parse():
     b = _bench()
-    traffic = b.load_traffic()
     inst = b.load_profile_figure("inst_executed_per_launch")
-    assert traffic is not None and inst is not None
-    # DRAM bytes of one 1080p launch: at least the 116 MB of records read once
-    assert b.Q * b.EVAL_BYTES <= traffic < b.Q * (b.EVAL_BYTES + b.OUT_BYTES) * 1.1
+    raw = b.load_profile_figure("traffic_bytes_per_launch")
+    assert raw is not None and inst is not None
+    # DRAM bytes of one 1080p launch: at least the records read once
+    assert b.Q * 20 <= raw < b.Q * (b.EVAL_BYTES + b.OUT_BYTES) * 1.1
     assert inst > 0 and b.load_profile_figure("no_such_figure") is None
+
+
+def test_traffic_reported_only_for_the_profiled_sources():
+    b = _bench()
+    traffic, src = b.load_traffic()
+    with open(os.path.join(ROOT, "profiles", "infer_kernel_1080p.md")) as fh:
+        recorded = [ln.split(":", 1)[1].strip() for ln in fh if ln.startswith("kernel_source_sha256_16:")]
+    if recorded and recorded[0] == b.kernel_source_hash():
+        assert traffic == b.load_profile_figure("traffic_bytes_per_launch") and "ncu" in src
+    else:
+        assert traffic is None and "changed" in src
 
 
 def test_issue_bound_arithmetic():

@@ -98,7 +98,7 @@ int configure_kernels() {
 }
 
 void he_init(uint64_t seed, float* w) {
-  // src/VkNRCState.cpp:131-136: std::normal_distribution<float>{0, sqrt(2/64)}
+  // src/VkNRCState.cpp:39-44: std::normal_distribution<float>{0, sqrt(2/64)}
   // over std::mt19937, one draw per parameter in index order.
   std::mt19937 rng(static_cast<std::mt19937::result_type>(seed));
   std::normal_distribution<float> norm{0.0f, std::sqrt(2.0f / float(NRC_WIDTH))};
@@ -460,6 +460,32 @@ int nrc_gradient(nrc_context* c, const nrc_train_record* rec, const uint32_t* d_
   p.batch[0] = nrc::TrainBatch{rec, const_cast<uint32_t*>(d_count), capacity, 0};
   p.grad_out = d_grad;
   return from_cuda(nrc::launch_train(p, &c->map_w16, c->num_sms, static_cast<cudaStream_t>(stream)));
+}
+
+int nrc_optimize(nrc_context* c, const float* d_grad_sum, uint32_t* d_count, int write_use_weights, void* stream) {
+  int s = check_ctx(c);
+  if (s != NRC_OK) return s;
+  if (d_grad_sum == nullptr || d_count == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  if (!aligned16(d_grad_sum) || (reinterpret_cast<uintptr_t>(d_count) & 3u)) return NRC_ERROR_MISALIGNED;
+  const nrc::TrainParams p = train_params(c, 1, nrc::kTrainStep);
+  s = from_cuda(nrc::launch_optimize(p, d_grad_sum, d_count, write_use_weights != 0, static_cast<cudaStream_t>(stream)));
+  return s == NRC_OK ? fp8_refresh(c, 0, static_cast<cudaStream_t>(stream)) : s;
+}
+
+int nrc_loss_gradient(const float* d_pred, const float* d_target, const uint32_t* d_count, uint32_t capacity,
+                      float loss_scale, uint32_t precision, uint32_t* d_rows, void* stream) {
+  if (d_count == nullptr || (capacity > 0 && (d_pred == nullptr || d_target == nullptr || d_rows == nullptr)) ||
+      (precision != NRC_PRECISION_FP16 && precision != NRC_PRECISION_BF16))
+    return NRC_ERROR_INVALID_ARGUMENT;
+  if ((reinterpret_cast<uintptr_t>(d_pred) | reinterpret_cast<uintptr_t>(d_target) |
+       reinterpret_cast<uintptr_t>(d_rows) | reinterpret_cast<uintptr_t>(d_count)) & 3u)
+    return NRC_ERROR_MISALIGNED;
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return NRC_ERROR_NO_DEVICE;
+  return from_cuda(nrc::launch_loss_rows(d_pred, d_target, d_count, capacity, loss_scale,
+                                         precision == NRC_PRECISION_BF16, d_rows, sms,
+                                         static_cast<cudaStream_t>(stream)));
 }
 
 int nrc_train_batches(nrc_context* c, const nrc_train_record* const* recs, uint32_t* const* counts, uint32_t capacity,

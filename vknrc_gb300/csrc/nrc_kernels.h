@@ -202,6 +202,14 @@ struct TrainLaunch {
 
 constexpr int kMaxTrainJobs = 32;  // caches per batched training launch
 
+// The reference's prepare + optimizer passes over a given gradient sum
+// (p supplies the hyper-parameters and the cache's buffers), and the relative-L2
+// gradient rows of given predictions (nrc_optimize.cu).
+cudaError_t launch_optimize(const TrainParams& p, const float* grad_sum, uint32_t* d_count, bool write_use,
+                            cudaStream_t stream);
+cudaError_t launch_loss_rows(const float* pred, const float* target, const uint32_t* d_count, uint32_t capacity,
+                             float loss_scale, bool bf16, uint32_t* rows, int num_sms, cudaStream_t stream);
+
 uint32_t train_smem_bytes();
 uint32_t train_grid(const TrainParams& p, int max_ctas);
 // The grid barrier counter p.sync[0] and exit counter p.sync[1] must be zero

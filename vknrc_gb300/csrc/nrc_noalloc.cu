@@ -14,10 +14,14 @@
 
 namespace {
 
-// One gradient partial per CTA; a CTA handles at most two 128-record tiles, so
-// the array bounds one call at kNoAllocSlots * 256 = 16,384 records.
+// One gradient partial per CTA, for at most kNoAllocSlots CTAs; a CTA sums any
+// number of record tiles into its partial, so the slots do not bound the record
+// count. The 16,384-record limit is this entry point's documented policy: one
+// call is one training batch of the reference's size (NRC_TRAIN_BATCH_SIZE),
+// which keeps a call's duration, and so the window in which a second call on
+// another stream would race on the shared array, within one step's length.
 constexpr int kNoAllocSlots = 64;
-constexpr uint32_t kNoAllocMaxRecords = kNoAllocSlots * 2 * nrc::kTile;
+constexpr uint32_t kNoAllocMaxRecords = 16384;
 constexpr size_t kScratchFloats = size_t(kNoAllocSlots) * nrc::kParams + 64;  // + error word, barrier counter
 
 // Held by every GPU that loads the library until the process exits:
@@ -72,6 +76,7 @@ int setup_current_device(DeviceSetup** out) {
 }
 
 bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+bool aligned4(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 3u) == 0; }
 
 }  // namespace
 
@@ -84,7 +89,8 @@ extern "C" NRC_API int nrc_train_noalloc(uint16_t* d_weights, uint16_t* d_use_we
       (cfg->precision != NRC_PRECISION_FP16 && cfg->precision != NRC_PRECISION_BF16))
     return NRC_ERROR_INVALID_ARGUMENT;
   if (!aligned16(d_weights) || !aligned16(d_entries) || (d_records && !aligned16(d_records)) ||
-      (d_use_weights && (reinterpret_cast<uintptr_t>(d_use_weights) & 1u)))
+      (d_use_weights && (reinterpret_cast<uintptr_t>(d_use_weights) & 1u)) || !aligned4(d_state) ||
+      !aligned4(d_count) || (d_error && !aligned4(d_error)))
     return NRC_ERROR_MISALIGNED;
   const uint32_t records = capacity < cfg->train_batch_size ? capacity : cfg->train_batch_size;
   if (records > kNoAllocMaxRecords) return NRC_ERROR_TOO_LARGE;

@@ -39,6 +39,7 @@
 
 #include "nrc_common.cuh"
 #include "nrc_kernels.h"
+#include "nrc_train_math.cuh"
 
 namespace nrc {
 
@@ -152,10 +153,6 @@ __device__ __forceinline__ uint32_t relu_mask2(uint32_t g, uint32_t a) {
   return kBF16 ? relu_mask_bf16x2(g, a) : relu_mask_f16x2(g, a);
 }
 
-template <bool kBF16>
-__device__ __forceinline__ uint16_t to16(float x) {
-  return kBF16 ? __bfloat16_as_ushort(__float2bfloat16_rn(x)) : __half_as_ushort(__float2half_rn(x));
-}
 
 // Write half h (32 inputs) of one layer's final weight gradient from TMEM to the
 // CTA's partial slot. M=64 accumulator layout: output row 16q+t lives in TMEM
@@ -218,38 +215,6 @@ __device__ __forceinline__ bool grid_sync(uint32_t* counter, uint32_t target, ui
   }
   __syncthreads();
   return *reinterpret_cast<volatile uint32_t*>(sync_ok) != 0;
-}
-
-// One optimizer update (nrc_optimize.comp:32-54) of parameter i from its
-// gradient sum; exactly the CPU oracle's operation order. `e` is the CTA's
-// shared-memory copy of the entry; the entry is also written back to memory.
-struct AdamHyper {
-  float lr, beta1, beta2, eps, ema_alpha, loss_scale;
-  int use_ema;
-};
-
-template <bool kBF16>
-__device__ __forceinline__ void adam_one(int i, float gsum, uint32_t n, const nrc_optimizer_state& st,
-                                         const AdamHyper& hp, nrc_optimizer_entry& e,
-                                         nrc_optimizer_entry* __restrict__ entries, uint16_t* __restrict__ w16,
-                                         uint16_t* __restrict__ use16) {
-  float g = __fdiv_rn(__fdiv_rn(gsum, static_cast<float>(n)), hp.loss_scale);
-  if (isnan(g) || isinf(g)) g = 0.0f;
-  const float m = __fmaf_rn(hp.beta1, e.m, __fmul_rn(__fsub_rn(1.0f, hp.beta1), g));
-  const float v = __fmaf_rn(hp.beta2, e.v, __fmul_rn(__fsub_rn(1.0f, hp.beta2), __fmul_rn(g, g)));
-  const float hm = __fdiv_rn(m, __fsub_rn(1.0f, st.beta1_t));
-  const float hv = __fdiv_rn(v, __fsub_rn(1.0f, st.beta2_t));
-  const float w = __fsub_rn(e.weight, __fdiv_rn(__fmul_rn(hp.lr, hm), __fadd_rn(__fsqrt_rn(hv), hp.eps)));
-  const float eta_t = __fsub_rn(1.0f, st.alpha_t), eta_t1 = __fsub_rn(1.0f, st.alpha_t_1);
-  const float ea = __fdiv_rn(__fsub_rn(1.0f, hp.ema_alpha), eta_t), eb = __fmul_rn(hp.ema_alpha, eta_t1);
-  const float ema = __fmaf_rn(ea, w, __fmul_rn(eb, e.ema_weight));
-  e.m = m;
-  e.v = v;
-  e.weight = w;
-  e.ema_weight = ema;
-  entries[i] = e;
-  w16[i] = to16<kBF16>(w);
-  if (use16 != nullptr) use16[i] = to16<kBF16>(hp.use_ema ? ema : w);
 }
 
 // One launch trains up to N caches: CTAs [group_start[j], group_start[j+1])
@@ -579,16 +544,10 @@ __global__ void __launch_bounds__(kTrainThreads, 1) train_steps_kernel(const __g
             uint32_t o4[4];
             tmem_ld4(lane_base + kDCol, o4);
             const float p0 = __uint_as_float(o4[0]), p1 = __uint_as_float(o4[1]), p2 = __uint_as_float(o4[2]);
-            const float lum = __fmaf_rn(0.114f, fmaxf(p2, 0.0f),
-                                        __fmaf_rn(0.587f, fmaxf(p1, 0.0f), __fmul_rn(0.299f, fmaxf(p0, 0.0f))));
-            const float den = __fmaf_rn(lum, lum, 0.01f);
-            const float s2 = __fmul_rn(2.0f, P.loss_scale);
-            const float d0 = __fdiv_rn(__fmul_rn(s2, __fsub_rn(p0, target[0])), den);
-            const float d1 = __fdiv_rn(__fmul_rn(s2, __fsub_rn(p1, target[1])), den);
-            const float d2 = __fdiv_rn(__fmul_rn(s2, __fsub_rn(p2, target[2])), den);
+            float d[3];
+            const float den = rel_l2_grad(p0, p1, p2, target, P.loss_scale, d);
             if (valid) {
-              gw[0] = pack2<kBF16>(d0, d1);
-              gw[1] = pack2<kBF16>(d2, 0.0f);
+              loss_row<kBF16>(d, gw);
               if (P.loss_acc != nullptr) {
                 const double dd = static_cast<double>(den);
                 const double e0 = static_cast<double>(p0) - target[0], e1 = static_cast<double>(p1) - target[1],

@@ -36,7 +36,7 @@ EXPORTS = [
     "nrc_server_get_stats", "nrc_screen", "nrc_checkpoint_bytes", "nrc_save_checkpoint", "nrc_load_checkpoint",
     "nrc_unpack_eval", "nrc_unpack_train", "nrc_infer_fp8", "nrc_fp8_refresh", "nrc_get_fp8",
     "nrc_frame_overlapped", "nrc_autotune_frame", "nrc_bvh_build", "nrc_bvh_destroy", "nrc_bvh_info",
-    "nrc_path_trace",
+    "nrc_path_trace", "nrc_optimize", "nrc_loss_gradient",
 ]
 
 
@@ -182,6 +182,8 @@ def lib(build_if_missing: bool = True) -> ctypes.CDLL:
     L.nrc_infer_encoded.argtypes = [vp, vp, vp, u32, vp, i32, vp]
     L.nrc_train.argtypes = [vp, vp, vp, u32, i32, vp]
     L.nrc_gradient.argtypes = [vp, vp, vp, u32, vp, vp]
+    L.nrc_optimize.argtypes = [vp, vp, vp, i32, vp]
+    L.nrc_loss_gradient.argtypes = [vp, vp, vp, u32, ctypes.c_float, u32, vp, vp]
     L.nrc_train_batches.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), u32, i32, i32, vp]
     L.nrc_frame.argtypes = [vp, vp, vp, u32, vp, ctypes.POINTER(vp), ctypes.POINTER(vp), u32, vp]
     L.nrc_get_weights.argtypes = [vp, i32, vp]
@@ -328,6 +330,10 @@ class Cache:
         cap = records.shape[0] if capacity is None else capacity
         check(lib().nrc_gradient(self.h, _ptr(records), _ptr(count), cap, _ptr(grad), _stream(stream)),
               "nrc_gradient")
+
+    def optimize(self, grad_sum, count, write_use=True, stream=None):
+        """nrc_optimize: the prepare + optimizer passes on a given gradient sum."""
+        check(lib().nrc_optimize(self.h, _ptr(grad_sum), _ptr(count), int(write_use), _stream(stream)), "nrc_optimize")
 
     def train_batches(self, records: Sequence, counts: Sequence, capacity=None, write_use_last=True, stream=None):
         cap = records[0].shape[0] if capacity is None else capacity
@@ -597,6 +603,13 @@ class Server:
         st = ServerStats()
         check(lib().nrc_server_get_stats(self.h, ctypes.byref(st), int(reset)), "nrc_server_get_stats")
         return {k: getattr(st, k) for k, _ in ServerStats._fields_}
+
+
+def loss_gradient(pred, target, count, rows, loss_scale=1.0, precision=0, capacity=None, stream=None) -> None:
+    """nrc_loss_gradient: the relative-L2 gradient row words (n x 2 uint32) of n (prediction, target) pairs."""
+    cap = pred.shape[0] if capacity is None else capacity
+    check(lib().nrc_loss_gradient(_ptr(pred), _ptr(target), _ptr(count), cap, float(loss_scale), int(precision),
+                                  _ptr(rows), _stream(stream)), "nrc_loss_gradient")
 
 
 def screen(color, accumulate=None, accumulate_count=0, out_rgba8=None, out_rgba=None, stream=None) -> None:

@@ -258,3 +258,42 @@ def terrain_scene(rng: np.random.Generator, n: int = 256, texture: int = 64) -> 
                       rng.integers(0, 256, (texture // 2, texture, 4), dtype=np.uint8)]
     sc["instance_ranges"] = np.array([[0, p], [0, floor_t.shape[0] // 8]], np.uint32)
     return sc
+
+
+def train_records_device(gen, n: int, target: str = "field", sigma: float = 1.0, device: str = "cuda"):
+    """The distributions of train_records, drawn on the device with a seeded
+    torch.Generator (for runs of many frames, where host generation would
+    dominate): an (n, 20) float32 tensor of nrc_train_record rows. The stream
+    differs from the host generator's; the distributions are the same."""
+    import torch
+
+    def unif(*shape):
+        return torch.rand(*shape, generator=gen, device=device, dtype=torch.float32)
+
+    def sph(d):
+        d = d.double()
+        d = d / d.norm(dim=1, keepdim=True).clamp_min(1e-30)
+        u = 0.5 + torch.atan2(d[:, 1], d[:, 0]) / (2 * np.pi)
+        u = torch.where((d[:, 0] == 0) & (d[:, 1] == 0), torch.full_like(u, 0.5), u)
+        v = torch.arccos(d[:, 2].clamp(-1, 1)) / np.pi
+        return torch.stack([u, v], 1).float()
+
+    rec = torch.empty((n, TRAIN_FLOATS), dtype=torch.float32, device=device)
+    x = rec[:, 6:20]
+    x[:, 0:3] = unif(n, 3)
+    x[:, 3:5] = torch.round(sph(torch.randn(n, 3, generator=gen, device=device)) * 65535.0) / 65535.0
+    x[:, 5:7] = sph(torch.randn(n, 3, generator=gen, device=device))
+    x[:, 7] = unif(n)
+    x[:, 8:14] = unif(n, 6)
+    noise = torch.exp(sigma * torch.randn(n, 3, generator=gen, device=device))
+    if target == "lognormal":
+        rec[:, 0:3] = noise
+    elif target == "field":
+        p, d, nrm, rough = x[:, 0:3], x[:, 3:5], x[:, 5:7], x[:, 7]
+        shade = 0.6 + 0.4 * torch.sin(2 * np.pi * (p[:, 0] + 0.3 * p[:, 2])) * torch.cos(np.pi * nrm[:, 1])
+        gloss = torch.exp(-4.0 * rough) * (0.5 + 0.5 * torch.cos(2 * np.pi * (p[:, 1] + d[:, 0])))
+        rec[:, 0:3] = (x[:, 8:11] * shade[:, None] + x[:, 11:14] * gloss[:, None] + 0.05) * noise
+    else:
+        raise ValueError(target)
+    rec[:, 3:6] = 1.0
+    return rec
