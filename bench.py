@@ -318,8 +318,11 @@ def plain_fp16_leg(evals, trains, eval_cnt, train_cnt, frames=50, loss_frames=20
     steps of 16,384 records, each nrc_encode + the same fp16 forward under torch
     autograd + the relative-L2 luminance loss (denominator held constant, as the
     fused kernel does) + backward + torch's fused Adam on fp32 master weights.
-    Reports its frames/s beside the fused frame, and the held-out relative-L2 loss
-    that both reach from the same initial weights after the same frames."""
+    Each frame is one CUDA graph replay (one graph per combination of the rotated
+    record frames, captured once): no host launch overhead, the fp16 weight
+    copies made once per step inside the graph. Reports its frames/s beside the
+    fused frame, and the held-out relative-L2 loss that both reach from the same
+    initial weights after the same frames."""
     import numpy as np
     import torch
 
@@ -332,7 +335,7 @@ def plain_fp16_leg(evals, trains, eval_cnt, train_cnt, frames=50, loss_frames=20
     shapes = [(64, 64)] * 5 + [(3, 64)]
     offs = [0, 4096, 8192, 12288, 16384, 20480, 20672]
     masters = [torch.nn.Parameter(w0[offs[l]:offs[l + 1]].view(*shapes[l]).clone()) for l in range(6)]
-    opt = torch.optim.Adam(masters, lr=1e-3, betas=(0.9, 0.99), eps=1e-8, fused=True)
+    opt = torch.optim.Adam(masters, lr=1e-3, betas=(0.9, 0.99), eps=1e-8, fused=True, capturable=True)
     lum_w = torch.tensor([0.299, 0.587, 0.114], device="cuda")
     enc_q = torch.empty((Q, 64), dtype=torch.float16, device="cuda")
     enc_t = torch.empty((R, 64), dtype=torch.float16, device="cuda")
@@ -349,7 +352,8 @@ def plain_fp16_leg(evals, trains, eval_cnt, train_cnt, frames=50, loss_frames=20
     def query(k):
         c.encode(evals[k % len(evals)], eval_cnt, enc_q)
         with torch.no_grad():
-            out.copy_(torch.clamp_min(mlp(enc_q, [w.half() for w in masters]), 0))
+            w16 = [w.half() for w in masters]  # the rendering weights of this frame, once
+            out.copy_(torch.clamp_min(mlp(enc_q, w16), 0))
 
     def train_step(k, b):
         c.encode(t_in[k % len(t_in)][b], train_cnt[b], enc_t)
@@ -358,7 +362,7 @@ def plain_fp16_leg(evals, trains, eval_cnt, train_cnt, frames=50, loss_frames=20
             lum = torch.clamp_min(p, 0) @ lum_w
             den = lum * lum + 0.01
         loss = (((p - t_tg[k % len(t_tg)][b]) ** 2).sum(1) / den).mean()
-        opt.zero_grad(set_to_none=True)
+        opt.zero_grad(set_to_none=False)
         loss.backward()
         opt.step()
 
@@ -367,8 +371,39 @@ def plain_fp16_leg(evals, trains, eval_cnt, train_cnt, frames=50, loss_frames=20
         for b in range(B):
             train_step(k, b)
 
+    # warm-up on a side stream (allocates the gradients and Adam state), then one
+    # graph per record-frame combination, sharing one memory pool
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        for k in range(3):
+            frame(k)
+    torch.cuda.current_stream().wait_stream(side)
+    torch.cuda.synchronize()
+    state0 = [p_.detach().clone() for p_ in masters]
+    n_graphs = int(np.lcm(len(evals), len(trains)))
+    pool = torch.cuda.graph_pool_handle()
+    graphs = []
+    for k in range(n_graphs):
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, pool=pool):
+            frame(k)
+        graphs.append(g)
+    torch.cuda.synchronize()
+
+    def restart():
+        """The weights back to their initial values and Adam restarted (the capture ran steps)."""
+        with torch.no_grad():
+            for p_, w in zip(masters, state0):
+                p_.copy_(w)
+            for st in opt.state.values():
+                st["exp_avg"].zero_()
+                st["exp_avg_sq"].zero_()
+                st["step"].zero_()
+
+    restart()
     for k in range(3):
-        frame(k)
+        graphs[k % n_graphs].replay()
     torch.cuda.synchronize()
     s, m, e = (torch.cuda.Event(enable_timing=True) for _ in range(3))
     s.record()
@@ -376,7 +411,7 @@ def plain_fp16_leg(evals, trains, eval_cnt, train_cnt, frames=50, loss_frames=20
         query(k)
     m.record()
     for k in range(frames):
-        frame(k)
+        graphs[k % n_graphs].replay()
     e.record()
     torch.cuda.synchronize()
     infer_s = s.elapsed_time(m) / 1e3 / frames
@@ -384,14 +419,11 @@ def plain_fp16_leg(evals, trains, eval_cnt, train_cnt, frames=50, loss_frames=20
 
     # equal-error check: both paths from the same initial weights through the same
     # `loss_frames` frames of records, then the mean relative-L2 loss on held-out records
-    for p_, w in zip(masters, [w0[offs[l]:offs[l + 1]].view(*shapes[l]) for l in range(6)]):
-        with torch.no_grad():
-            p_.copy_(w)
-    opt = torch.optim.Adam(masters, lr=1e-3, betas=(0.9, 0.99), eps=1e-8, fused=True)
+    restart()
     fused = Cache(seed=777, **hyper)
     fout = torch.empty((Q, 3), dtype=torch.float32, device="cuda")
     for k in range(loss_frames):
-        frame(k)
+        graphs[k % n_graphs].replay()
         fused.frame(evals[k % len(evals)], eval_cnt, fout, trains[k % len(trains)], train_cnt)
     held = torch.from_numpy(S.train_records(S.rng_for(3000), R, target="field", sigma=1.0)).cuda()
     h_in, h_tg = held[:, 6:20].contiguous(), held[:, 0:3].contiguous()
@@ -407,17 +439,19 @@ def plain_fp16_leg(evals, trains, eval_cnt, train_cnt, frames=50, loss_frames=20
             lum = torch.clamp_min(p, 0) @ lum_w
             return float(((((p - h_tg) ** 2).sum(1)) / (lum * lum + 0.01)).mean())
 
+    torch.cuda.synchronize()
     wf = torch.from_numpy(fused.get_weights(0).view(np.float16).astype(np.float32)).cuda()
     loss_plain = rel_l2([p_.detach().half().float() for p_ in masters])
     loss_fused = rel_l2([wf[offs[l]:offs[l + 1]].view(*shapes[l]) for l in range(6)])
     if fused.error() != 0 or c.error() != 0:
         raise RuntimeError("device error status during the plain-path leg")
+    del graphs
     fused.close()
     c.close()
     return {
-        "what": "per frame: nrc_encode + 6 torch fp16 GEMMs (cuBLAS) for the 1080p query, then 4 training steps "
-                "(nrc_encode + fp16 GEMM forward/backward under autograd + relative-L2 loss + torch fused Adam, "
-                "fp32 masters)",
+        "what": "per frame, one CUDA graph replay: nrc_encode + 6 torch fp16 GEMMs (cuBLAS) for the 1080p query, "
+                "then 4 training steps (nrc_encode + fp16 GEMM forward/backward under autograd + relative-L2 loss + "
+                "torch fused capturable Adam, fp32 masters)",
         "frames": frames, "ms_per_frame": frame_s * 1e3, "frames_per_s": 1.0 / frame_s,
         "queries_per_s": Q / frame_s, "train_records_per_s": B * R / frame_s,
         "infer_only_queries_per_s": Q / infer_s,
@@ -766,6 +800,129 @@ def serving_leg(evals, trains, seconds=2.0, sessions=32, rate=2000.0, budget=40 
     }
 
 
+PACKED_EVAL_BYTES = 20   # nrc_eval_record
+PACKED_TRAIN_BYTES = 40  # nrc_packed_train_record
+
+
+def packed_leg(cache, stream, E, world, frames=4):
+    """The frame on the reference's record formats (nrc_frame_packed): packed
+    eval records (20 B) and packed train records (40 B) of a 522,254-triangle
+    scene resident on the device, unpacked inside the query kernel and by one
+    launch before the training. Times (1) the frame with its inputs resident
+    (`frames` distinct record frames rotated, 176 MB: cold in L2), (2) the
+    packed-record query alone, and (3) end to end through the C ABI with host
+    buffers: each frame's packed records copied from pinned memory and its rgb
+    results copied back, pipelined over two buffer sets as the unpacked e2e."""
+    import numpy as np
+    import torch
+
+    from vknrc_gb300 import nrc, synthetic as S
+
+    sc = S.terrain_scene(S.rng_for(3), n=512)
+    ds = nrc.DeviceScene(sc)
+    ev_h = [torch.from_numpy(S.eval_records(S.rng_for(4000, f), sc, Q).view(np.int32)) for f in range(frames)]
+    tr_h = [[torch.from_numpy(S.packed_train_records(S.rng_for(5000, f, b), sc, R).view(np.int32)) for b in range(B)]
+            for f in range(frames)]
+    ev_d = [t.cuda() for t in ev_h]
+    tr_d = [[t.cuda() for t in f] for f in tr_h]
+    eval_cnt = torch.tensor([Q], dtype=torch.int32, device="cuda")
+    train_cnt = [torch.tensor([R], dtype=torch.int32, device="cuda") for _ in range(B)]
+    out = torch.empty((Q, 3), dtype=torch.float32, device="cuda")
+
+    def frame(k, ev=None, tr=None, o=None):
+        cache.frame_packed(ds, ev if ev is not None else ev_d[k % frames], eval_cnt, o if o is not None else out,
+                           tr if tr is not None else tr_d[k % frames], train_cnt)
+
+    for k in range(5):
+        frame(k)
+    torch.cuda.synchronize()
+    K = 200
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record(stream)
+    for k in range(K):
+        frame(k)
+    e.record(stream)
+    torch.cuda.synchronize()
+    frame_s = s.elapsed_time(e) / 1e3 / K
+    # the packed-record query alone, each launch timed
+    for k in range(3):
+        cache.infer_packed(ds, ev_d[k % frames], eval_cnt, out)
+    QA = 100
+    ev_q = [torch.cuda.Event(enable_timing=True) for _ in range(QA + 1)]
+    torch.cuda.synchronize()
+    ev_q[0].record(stream)
+    for k in range(QA):
+        cache.infer_packed(ds, ev_d[k % frames], eval_cnt, out)
+        ev_q[k + 1].record(stream)
+    torch.cuda.synchronize()
+    q_ms = [ev_q[k].elapsed_time(ev_q[k + 1]) for k in range(QA)]
+
+    # end to end with host buffers
+    h_ev = [t.pin_memory() for t in ev_h[:2]]
+    h_tr = [[t.pin_memory() for t in f] for f in tr_h[:2]]
+    d_ev = [torch.empty_like(ev_d[0]) for _ in range(2)]
+    d_tr = [[torch.empty_like(tr_d[0][0]) for _ in range(B)] for _ in range(2)]
+    d_out = [out, torch.empty_like(out)]
+    h_out = [torch.empty((Q, 3), dtype=torch.float32).pin_memory() for _ in range(2)]
+    h2d = Q * PACKED_EVAL_BYTES + B * R * PACKED_TRAIN_BYTES
+    d2h = Q * OUT_BYTES
+    up_s, down_s = torch.cuda.Stream(), torch.cuda.Stream()
+    ev_up = [torch.cuda.Event() for _ in range(2)]
+    ev_done = [torch.cuda.Event() for _ in range(2)]
+    ev_back = [torch.cuda.Event() for _ in range(2)]
+
+    def e2e_frame(k):
+        j = k % 2
+        with torch.cuda.stream(up_s):
+            up_s.wait_event(ev_done[j])
+            d_ev[j].copy_(h_ev[k % 2], non_blocking=True)
+            for b in range(B):
+                d_tr[j][b].copy_(h_tr[k % 2][b], non_blocking=True)
+            ev_up[j].record(up_s)
+        stream.wait_event(ev_up[j])
+        stream.wait_event(ev_back[j])
+        frame(k, d_ev[j], d_tr[j], d_out[j])
+        ev_done[j].record(stream)
+        with torch.cuda.stream(down_s):
+            down_s.wait_event(ev_done[j])
+            h_out[j].copy_(d_out[j], non_blocking=True)
+            ev_back[j].record(down_s)
+
+    for j in range(2):
+        ev_done[j].record(stream)
+        ev_back[j].record(stream)
+    for k in range(3):
+        e2e_frame(k)
+    torch.cuda.synchronize()
+    barrier(world)
+    s.record(stream)
+    up_s.wait_stream(stream)
+    down_s.wait_stream(stream)
+    for k in range(E):
+        e2e_frame(k)
+    stream.wait_stream(down_s)
+    e.record(stream)
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(s.elapsed_time(e) / 1e3, world)
+    if cache.error() != 0:
+        raise RuntimeError("device error status during the packed-record leg")
+    return {
+        "e2e": {"value": world * Q * E / e2e_s, "unit": "queries/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "steps": E, "call": "nrc_frame_packed",
+                "schedule": "the reference's record formats (20-byte eval records, 40-byte train records) of a "
+                            "522,254-triangle scene resident on the device; pinned host buffers, frame k's H2D "
+                            "overlapping frame k-1's compute and frame k-2's D2H"},
+        "frame_packed": {"ms_per_frame": frame_s * 1e3, "queries_per_s": Q / frame_s,
+                         "train_records_per_s": B * R / frame_s, "frames": K,
+                         "what": "nrc_frame_packed with resident inputs (4 record frames rotated, L2-cold): "
+                                 "train-record unpack launch, then the training and the packed-record query "
+                                 "overlapped"},
+        "query_packed_alone_ms": {"mean": statistics.mean(q_ms), "p50": statistics.median(q_ms), "launches": QA,
+                                  "what": "nrc_infer_packed of 2,073,600 packed records (scene unpack fused into the "
+                                          "query kernel) on all SMs, timed alone"},
+    }
+
+
 def ours_arm(args, world, rank, local):
     import numpy as np
     import torch
@@ -870,6 +1027,8 @@ def ours_arm(args, world, rank, local):
     torch.cuda.synchronize()
     e2e_s = max_over_ranks(s.elapsed_time(e) / 1e3, world)
 
+    packed = packed_leg(cache, stream, E, world)
+
     # the query kernel alone on every SM (the roofline's kernel; in the frame it
     # shares the SMs with the training): the same rotated, L2-cold record frames
     for k in range(3):
@@ -945,11 +1104,15 @@ def ours_arm(args, world, rank, local):
             "algorithmic_flop_per_launch": FLOP_PER_QUERY * Q,
             "algorithmic_bytes_per_launch": Q * (EVAL_BYTES + OUT_BYTES),
         },
-        "e2e": {"value": world * Q * E / e2e_s, "unit": "queries/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "steps": E,
-                "schedule": "pinned host buffers; frame k's H2D overlaps frame k-1's compute and frame k-2's D2H "
-                            "(bounded by the host-to-device link: 121 MB per frame at the ~210 GB/s that both the copy engine "
-                            "and SM loads from mapped pinned memory reach)"},
+        "e2e": packed["e2e"],
+        "e2e_unpacked_records": {"value": world * Q * E / e2e_s, "unit": "queries/s", "h2d_bytes_per_step": h2d,
+                                 "d2h_bytes_per_step": d2h, "steps": E, "call": "nrc_frame_overlapped",
+                                 "schedule": "56-byte unpacked records (nrc_input) and 80-byte train records; pinned "
+                                             "host buffers, frame k's H2D overlapping frame k-1's compute and frame "
+                                             "k-2's D2H (bounded by the host-to-device link: 121 MB per frame at "
+                                             "about 210 GB/s)"},
+        "frame_packed": packed["frame_packed"],
+        "query_packed_alone_ms": packed["query_packed_alone_ms"],
         "clocks": clocks,
     }
     if plain is not None:

@@ -520,6 +520,56 @@ typedef struct nrc_packed_train_record {
   nrc_packed_input input;
 } nrc_packed_train_record;
 
+/* The reference's inference pass on its own record format: queries over
+ * min(*d_count, capacity) packed eval records (nrc_eval_record, 20 bytes,
+ * d_records 16-byte aligned) of `scene`, each unpacked inside the query kernel
+ * (UnpackNRCInput, NRCRecord.glsl:97-125, as nrc_inference.comp:33-36 does)
+ * before the encode and the MLP. nrc_infer_packed writes the clamped
+ * predictions to d_out_rgb (3 floats per record; the destination words are not
+ * used). nrc_infer_scatter_packed runs the destination epilogue
+ * (nrc_inference.comp:50-73) with each record's own destination word: screen
+ * pixels as nrc_infer_scatter, and train-target completion in packed train
+ * records (nrc_packed_train_record, targets->train_records); d_out_rgb may be
+ * NULL. Replaces rg::NNInference (src/rg/NNInference.hpp:18-37) with the
+ * scene's buffers as device pointers. */
+typedef struct nrc_packed_scatter_targets {
+  float* bias_factor_r;
+  const float* factor_gb;
+  uint32_t width, height;
+  nrc_packed_train_record* train_records[NRC_TRAIN_BATCH_COUNT];
+  uint32_t train_capacity[NRC_TRAIN_BATCH_COUNT];
+} nrc_packed_scatter_targets;
+
+NRC_API int nrc_infer_packed(nrc_context* ctx, const nrc_scene* scene, const nrc_eval_record* d_records,
+                             const uint32_t* d_count, uint32_t capacity, float* d_out_rgb, int weight_set,
+                             void* stream);
+NRC_API int nrc_infer_scatter_packed(nrc_context* ctx, const nrc_scene* scene, const nrc_eval_record* d_records,
+                                     const uint32_t* d_count, uint32_t capacity,
+                                     const nrc_packed_scatter_targets* targets, float* d_out_rgb, int weight_set,
+                                     void* stream);
+
+/* One frame on the reference's record formats: the packed train batches are
+ * unpacked (one launch, into a workspace the context keeps: the first call
+ * with a larger train_capacity allocates it, so make that call before any
+ * stream capture), then the frame runs as nrc_frame_overlapped with the
+ * packed-record query (results to d_out_rgb as nrc_infer_packed) beside the
+ * four training steps. */
+NRC_API int nrc_frame_packed(nrc_context* ctx, const nrc_scene* scene, const nrc_eval_record* d_eval_records,
+                             const uint32_t* d_eval_count, uint32_t eval_capacity, float* d_out_rgb,
+                             const nrc_packed_train_record* const* d_train_records, uint32_t* const* d_train_counts,
+                             uint32_t train_capacity, void* stream);
+
+/* The reference's frame schedule on its record formats
+ * (src/rg/NRCRenderGraph.cpp:46-80): nrc_infer_scatter_packed with the
+ * rendering weights (screen pixels, and the self-training targets completed in
+ * targets->train_records), then those packed train batches unpacked (workspace
+ * as nrc_frame_packed) and trained in NRC_TRAIN_BATCH_COUNT chained steps, the
+ * last writing use_weights. */
+NRC_API int nrc_frame_scatter_packed(nrc_context* ctx, const nrc_scene* scene, const nrc_eval_record* d_eval_records,
+                                     const uint32_t* d_eval_count, uint32_t eval_capacity,
+                                     const nrc_packed_scatter_targets* targets, uint32_t* const* d_train_counts,
+                                     void* stream);
+
 /* Unpacks min(*d_count, capacity) eval records into d_inputs (and their
  * destination words into d_dst, may be NULL), ready for nrc_infer_scatter. */
 NRC_API int nrc_unpack_eval(const nrc_scene* scene, const nrc_eval_record* d_records, const uint32_t* d_count,

@@ -126,7 +126,8 @@ def test_gpu_unpack_train_then_query_with_destinations(cuda, oracle):
     gb = S.rng_for(25).uniform(0, 1, (H, W, 2)).astype(np.float32)
     with Cache(seed=26) as c:
         img = dev(img0)
-        c.infer_scatter(inputs, dst, count(n), nrc.scatter_targets(img, dev(gb)))
+        gb_d = dev(gb)  # held: the kernel reads it after the call returns
+        c.infer_scatter(inputs, dst, count(n), nrc.scatter_targets(img, gb_d))
         got_img = host(img)
         pred_t = torch.empty((n, 3), dtype=torch.float32, device="cuda")
         c.infer(inputs, count(n), pred_t)  # the kernel's own predictions, for the oracle's epilogue

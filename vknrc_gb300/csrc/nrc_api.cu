@@ -38,6 +38,10 @@ struct nrc_context {
   __half* use_next = nullptr;   // the overlapped frame's training writes use_weights here first
   nrc_frame_plan plan = {0u, 0u};  // the overlapped frame's split, once tuned
   bool plan_tuned = false;         // nrc_autotune_frame has set `plan` (which may be sequential)
+  // packed-record frames: the unpacked train records of the frame's batches
+  // (NRC_TRAIN_BATCH_COUNT x train_ws_cap), allocated by the first such call
+  nrc_train_record* train_ws = nullptr;
+  uint32_t train_ws_cap = 0;
 };
 
 namespace nrc {
@@ -292,6 +296,7 @@ int nrc_destroy(nrc_context* c) {
   if (dev != c->device) cudaSetDevice(c->device);
   cudaDeviceSynchronize();
   cudaFree(c->block);
+  if (c->train_ws != nullptr) cudaFree(c->train_ws);
   if (dev >= 0 && dev != c->device) cudaSetDevice(dev);
   delete c;
   return NRC_OK;
@@ -368,9 +373,10 @@ static int scatter_out(const nrc_scatter_targets* t, nrc::QueryOut* q) {
   for (int b = 0; b < NRC_TRAIN_BATCH_COUNT; ++b) {
     if (t->train_records[b] != nullptr && (reinterpret_cast<uintptr_t>(t->train_records[b]) & 3u))
       return NRC_ERROR_MISALIGNED;
-    q->train[b] = t->train_records[b];
+    q->train[b] = reinterpret_cast<float*>(t->train_records[b]);
     q->train_cap[b] = t->train_records[b] != nullptr ? t->train_capacity[b] : 0u;
   }
+  q->train_stride = sizeof(nrc_train_record) / 4;
   return NRC_OK;
 }
 
@@ -516,9 +522,47 @@ int nrc_frame(nrc_context* c, const nrc_input* eval_in, const uint32_t* d_eval_c
   return nrc_train_batches(c, train_rec, train_counts, train_capacity, NRC_TRAIN_BATCH_COUNT, 1, stream);
 }
 
-int nrc_frame_overlapped(nrc_context* c, const nrc_input* eval_in, const uint32_t* d_eval_count, uint32_t eval_capacity,
-                         float* out, const nrc_train_record* const* train_rec, uint32_t* const* train_counts,
-                         uint32_t train_capacity, const nrc_frame_plan* plan_in, void* query_event, void* stream) {
+}  // extern "C"
+
+static int scene_check_impl(const nrc_scene* sc) {
+  if (sc == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  const bool geometry = sc->primitive_count > 0 && sc->instance_count > 0;
+  if (geometry && (sc->vertices == nullptr || sc->vertex_indices == nullptr || sc->texcoords == nullptr ||
+                   sc->texcoord_indices == nullptr || sc->materials == nullptr || sc->material_ids == nullptr ||
+                   sc->transforms == nullptr))
+    return NRC_ERROR_INVALID_ARGUMENT;
+  if (sc->texture_count > 0 && sc->textures == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  if ((reinterpret_cast<uintptr_t>(sc->materials) & 15u) || (reinterpret_cast<uintptr_t>(sc->textures) & 7u))
+    return NRC_ERROR_MISALIGNED;
+  return NRC_OK;
+}
+
+namespace {
+
+// What a frame's query reads: unpacked records (nrc_input), or the reference's
+// packed eval records over a scene (unpacked inside the query kernel).
+struct FrameQuery {
+  const nrc_input* in = nullptr;
+  const nrc_eval_record* packed = nullptr;
+  const nrc_scene* scene = nullptr;
+};
+
+cudaError_t launch_frame_query(nrc_context* c, const FrameQuery& fq, const uint32_t* d_count, uint32_t capacity,
+                               const nrc::QueryOut& q, bool overlapped, const nrc::FrameJoin& join, cudaStream_t st) {
+  const uint32_t grid = nrc::infer_grid(capacity, c->num_sms);
+  if (fq.packed != nullptr)
+    return nrc::launch_infer_packed(fq.packed, *fq.scene, d_count, capacity, &c->map_use16, q, c->err,
+                                    overlapped ? c->tiles : nullptr, join, grid, st, c->bf16);
+  if (overlapped)
+    return nrc::launch_infer_frame(fq.in, d_count, capacity, &c->map_use16, q, c->err, c->tiles, join, grid, st,
+                                   c->bf16);
+  return nrc::launch_infer(fq.in, false, d_count, capacity, &c->map_use16, q, c->err, c->num_sms, st, c->bf16);
+}
+
+// The body of nrc_frame_overlapped for either form of query input.
+int frame_overlapped(nrc_context* c, const FrameQuery& fq, const uint32_t* d_eval_count, uint32_t eval_capacity,
+                     float* out, const nrc_train_record* const* train_rec, uint32_t* const* train_counts,
+                     uint32_t train_capacity, const nrc_frame_plan* plan_in, void* query_event, void* stream) {
   int s = check_ctx(c);
   if (s != NRC_OK) return s;
   if (train_rec == nullptr || train_counts == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
@@ -527,8 +571,9 @@ int nrc_frame_overlapped(nrc_context* c, const nrc_input* eval_in, const uint32_
     if (train_rec[b] != nullptr && !aligned16(train_rec[b])) return NRC_ERROR_MISALIGNED;
   }
   if (eval_capacity > 0) {
-    if (eval_in == nullptr || d_eval_count == nullptr || out == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
-    if (!aligned16(eval_in) || (reinterpret_cast<uintptr_t>(out) & 3u)) return NRC_ERROR_MISALIGNED;
+    const void* in = fq.packed != nullptr ? static_cast<const void*>(fq.packed) : static_cast<const void*>(fq.in);
+    if (in == nullptr || d_eval_count == nullptr || out == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+    if (!aligned16(in) || (reinterpret_cast<uintptr_t>(out) & 3u)) return NRC_ERROR_MISALIGNED;
   }
   nrc_frame_plan plan = plan_in ? *plan_in : c->plan;
   if (plan_in == nullptr && !c->plan_tuned) {
@@ -550,8 +595,7 @@ int nrc_frame_overlapped(nrc_context* c, const nrc_input* eval_in, const uint32_
   if (sequential) {
     // the query with the current rendering weights, then the training, which writes them
     if (eval_capacity > 0) {
-      e = nrc::launch_infer(eval_in, false, d_eval_count, eval_capacity, &c->map_use16, q, c->err, c->num_sms, st,
-                            c->bf16);
+      e = launch_frame_query(c, fq, d_eval_count, eval_capacity, q, false, nrc::FrameJoin{}, st);
       if (e != cudaSuccess) return from_cuda(e);
     }
     if (query_event != nullptr && (e = cudaEventRecord(static_cast<cudaEvent_t>(query_event), st)) != cudaSuccess)
@@ -580,13 +624,146 @@ int nrc_frame_overlapped(nrc_context* c, const nrc_input* eval_in, const uint32_
   e = nrc::launch_train(p, &c->map_w16, static_cast<int>(plan.train_ctas), st);
   if (e != cudaSuccess) return from_cuda(e);
   if (eval_capacity > 0) {
-    e = nrc::launch_infer_frame(eval_in, d_eval_count, eval_capacity, &c->map_use16, q, c->err, c->tiles, join,
-                                nrc::infer_grid(eval_capacity, c->num_sms), st, c->bf16);
+    e = launch_frame_query(c, fq, d_eval_count, eval_capacity, q, true, join, st);
     if (e != cudaSuccess) return from_cuda(e);
   }
   if (query_event != nullptr && (e = cudaEventRecord(static_cast<cudaEvent_t>(query_event), st)) != cudaSuccess)
     return from_cuda(e);
   return fp8_refresh(c, 0, st);
+}
+
+// Grows the context's unpacked-train-record workspace to `capacity` records
+// per batch (an allocation: not inside a stream capture).
+int ensure_train_ws(nrc_context* c, uint32_t capacity) {
+  if (capacity <= c->train_ws_cap) return NRC_OK;
+  cudaError_t e = cudaSuccess;
+  if (c->train_ws != nullptr) {
+    if ((e = cudaDeviceSynchronize()) != cudaSuccess) return from_cuda(e);
+    cudaFree(c->train_ws);
+    c->train_ws = nullptr;
+    c->train_ws_cap = 0;
+  }
+  void* p = nullptr;
+  e = cudaMalloc(&p, size_t(NRC_TRAIN_BATCH_COUNT) * capacity * sizeof(nrc_train_record));
+  if (e != cudaSuccess) return e == cudaErrorMemoryAllocation ? NRC_ERROR_OUT_OF_MEMORY : from_cuda(e);
+  c->train_ws = static_cast<nrc_train_record*>(p);
+  c->train_ws_cap = capacity;
+  return NRC_OK;
+}
+
+// Unpacks the frame's packed train batches into the workspace; ws[b] receives
+// batch b's array.
+int unpack_train_ws(nrc_context* c, const nrc_scene* scene, const nrc_packed_train_record* const* rec,
+                    uint32_t* const* counts, uint32_t capacity, const nrc_train_record** ws, cudaStream_t st) {
+  for (int b = 0; b < NRC_TRAIN_BATCH_COUNT; ++b) {
+    if (counts[b] == nullptr || (capacity > 0 && rec[b] == nullptr)) return NRC_ERROR_INVALID_ARGUMENT;
+    if (rec[b] != nullptr && (reinterpret_cast<uintptr_t>(rec[b]) & 3u)) return NRC_ERROR_MISALIGNED;
+  }
+  int s = ensure_train_ws(c, capacity > 0 ? capacity : 1);
+  if (s != NRC_OK) return s;
+  nrc_train_record* out[NRC_TRAIN_BATCH_COUNT];
+  for (int b = 0; b < NRC_TRAIN_BATCH_COUNT; ++b) {
+    out[b] = c->train_ws + size_t(b) * c->train_ws_cap;
+    ws[b] = out[b];
+  }
+  if (capacity == 0) return NRC_OK;
+  return from_cuda(nrc::launch_unpack_train_batches(*scene, rec, counts, capacity, out, NRC_TRAIN_BATCH_COUNT,
+                                                    c->num_sms, st));
+}
+
+}  // namespace
+
+extern "C" {
+
+int nrc_frame_overlapped(nrc_context* c, const nrc_input* eval_in, const uint32_t* d_eval_count, uint32_t eval_capacity,
+                         float* out, const nrc_train_record* const* train_rec, uint32_t* const* train_counts,
+                         uint32_t train_capacity, const nrc_frame_plan* plan_in, void* query_event, void* stream) {
+  FrameQuery fq;
+  fq.in = eval_in;
+  return frame_overlapped(c, fq, d_eval_count, eval_capacity, out, train_rec, train_counts, train_capacity, plan_in,
+                          query_event, stream);
+}
+
+int nrc_infer_packed(nrc_context* c, const nrc_scene* scene, const nrc_eval_record* rec, const uint32_t* d_count,
+                     uint32_t capacity, float* out, int weight_set, void* stream) {
+  int s = check_ctx(c);
+  if (s != NRC_OK) return s;
+  if ((s = scene_check_impl(scene)) != NRC_OK) return s;
+  if (weight_set != NRC_WEIGHTS_USE && weight_set != NRC_WEIGHTS_TRAIN) return NRC_ERROR_INVALID_ARGUMENT;
+  if (capacity == 0) return NRC_OK;
+  if (rec == nullptr || d_count == nullptr || out == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  if (!aligned16(rec) || (reinterpret_cast<uintptr_t>(out) & 3u)) return NRC_ERROR_MISALIGNED;
+  nrc::QueryOut q = {};
+  q.out = out;
+  q.clamp = 1;
+  return from_cuda(nrc::launch_infer_packed(rec, *scene, d_count, capacity, weight_map_of(c, weight_set), q, c->err,
+                                            nullptr, nrc::FrameJoin{}, nrc::infer_grid(capacity, c->num_sms),
+                                            static_cast<cudaStream_t>(stream), c->bf16));
+}
+
+int nrc_infer_scatter_packed(nrc_context* c, const nrc_scene* scene, const nrc_eval_record* rec,
+                             const uint32_t* d_count, uint32_t capacity, const nrc_packed_scatter_targets* targets,
+                             float* out, int weight_set, void* stream) {
+  int s = check_ctx(c);
+  if (s != NRC_OK) return s;
+  if ((s = scene_check_impl(scene)) != NRC_OK) return s;
+  if (weight_set != NRC_WEIGHTS_USE && weight_set != NRC_WEIGHTS_TRAIN) return NRC_ERROR_INVALID_ARGUMENT;
+  nrc::QueryOut q = {};
+  // the packed targets differ from nrc_scatter_targets only in the train records' type
+  static_assert(sizeof(nrc_packed_scatter_targets) == sizeof(nrc_scatter_targets), "target layouts");
+  if ((s = scatter_out(reinterpret_cast<const nrc_scatter_targets*>(targets), &q)) != NRC_OK) return s;
+  q.train_stride = sizeof(nrc_packed_train_record) / 4;
+  if (capacity == 0) return NRC_OK;
+  if (rec == nullptr || d_count == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  if (!aligned16(rec) || (reinterpret_cast<uintptr_t>(out) & 3u)) return NRC_ERROR_MISALIGNED;
+  q.out = out;
+  q.clamp = 1;
+  q.scatter = 1;
+  return from_cuda(nrc::launch_infer_packed(rec, *scene, d_count, capacity, weight_map_of(c, weight_set), q, c->err,
+                                            nullptr, nrc::FrameJoin{}, nrc::infer_grid(capacity, c->num_sms),
+                                            static_cast<cudaStream_t>(stream), c->bf16));
+}
+
+int nrc_frame_scatter_packed(nrc_context* c, const nrc_scene* scene, const nrc_eval_record* eval_rec,
+                             const uint32_t* d_eval_count, uint32_t eval_capacity,
+                             const nrc_packed_scatter_targets* targets, uint32_t* const* train_counts, void* stream) {
+  int s = check_ctx(c);
+  if (s != NRC_OK) return s;
+  if (targets == nullptr || train_counts == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  uint32_t cap = 0;
+  for (int b = 0; b < NRC_TRAIN_BATCH_COUNT; ++b) {
+    if (targets->train_records[b] == nullptr || train_counts[b] == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+    if (b > 0 && targets->train_capacity[b] != cap) return NRC_ERROR_INVALID_ARGUMENT;  // one capacity, as nrc_frame
+    cap = targets->train_capacity[b];
+  }
+  s = nrc_infer_scatter_packed(c, scene, eval_rec, d_eval_count, eval_capacity, targets, nullptr, NRC_WEIGHTS_USE,
+                               stream);
+  if (s != NRC_OK) return s;
+  const nrc_packed_train_record* prec[NRC_TRAIN_BATCH_COUNT];
+  for (int b = 0; b < NRC_TRAIN_BATCH_COUNT; ++b) prec[b] = targets->train_records[b];
+  const nrc_train_record* ws[NRC_TRAIN_BATCH_COUNT];
+  if ((s = unpack_train_ws(c, scene, prec, train_counts, cap, ws, static_cast<cudaStream_t>(stream))) != NRC_OK)
+    return s;
+  return nrc_train_batches(c, ws, train_counts, cap, NRC_TRAIN_BATCH_COUNT, 1, stream);
+}
+
+int nrc_frame_packed(nrc_context* c, const nrc_scene* scene, const nrc_eval_record* eval_rec,
+                     const uint32_t* d_eval_count, uint32_t eval_capacity, float* out,
+                     const nrc_packed_train_record* const* train_rec, uint32_t* const* train_counts,
+                     uint32_t train_capacity, void* stream) {
+  int s = check_ctx(c);
+  if (s != NRC_OK) return s;
+  if ((s = scene_check_impl(scene)) != NRC_OK) return s;
+  if (train_rec == nullptr || train_counts == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  const nrc_train_record* ws[NRC_TRAIN_BATCH_COUNT];
+  if ((s = unpack_train_ws(c, scene, train_rec, train_counts, train_capacity, ws, static_cast<cudaStream_t>(stream))) !=
+      NRC_OK)
+    return s;
+  FrameQuery fq;
+  fq.packed = eval_rec;
+  fq.scene = scene;
+  return frame_overlapped(c, fq, d_eval_count, eval_capacity, out, ws, train_counts, train_capacity, nullptr, nullptr,
+                          stream);
 }
 
 int nrc_autotune_frame(nrc_context* c, const nrc_input* eval_in, const uint32_t* d_eval_count, uint32_t eval_capacity,
@@ -954,22 +1131,10 @@ int nrc_get_fp8(nrc_context* c, uint8_t* host_w8, float* host_scales) {
 }
 
 // ---------------------------------------------------------------- unpack --
-static int scene_check(const nrc_scene* sc) {
-  if (sc == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
-  const bool geometry = sc->primitive_count > 0 && sc->instance_count > 0;
-  if (geometry && (sc->vertices == nullptr || sc->vertex_indices == nullptr || sc->texcoords == nullptr ||
-                   sc->texcoord_indices == nullptr || sc->materials == nullptr || sc->material_ids == nullptr ||
-                   sc->transforms == nullptr))
-    return NRC_ERROR_INVALID_ARGUMENT;
-  if (sc->texture_count > 0 && sc->textures == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
-  if ((reinterpret_cast<uintptr_t>(sc->materials) & 15u) || (reinterpret_cast<uintptr_t>(sc->textures) & 7u))
-    return NRC_ERROR_MISALIGNED;
-  return NRC_OK;
-}
 
 int nrc_unpack_eval(const nrc_scene* sc, const nrc_eval_record* rec, const uint32_t* d_count, uint32_t capacity,
                     nrc_input* out, uint32_t* out_dst, void* stream) {
-  int s = scene_check(sc);
+  int s = scene_check_impl(sc);
   if (s != NRC_OK) return s;
   if (capacity == 0) return NRC_OK;
   if (rec == nullptr || d_count == nullptr || out == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
@@ -982,7 +1147,7 @@ int nrc_unpack_eval(const nrc_scene* sc, const nrc_eval_record* rec, const uint3
 
 int nrc_unpack_train(const nrc_scene* sc, const nrc_packed_train_record* rec, const uint32_t* d_count,
                      uint32_t capacity, nrc_train_record* out, void* stream) {
-  int s = scene_check(sc);
+  int s = scene_check_impl(sc);
   if (s != NRC_OK) return s;
   if (capacity == 0) return NRC_OK;
   if (rec == nullptr || d_count == nullptr || out == nullptr) return NRC_ERROR_INVALID_ARGUMENT;

@@ -201,35 +201,50 @@ __device__ __forceinline__ void encode_input(const float (&r)[kInFloats], uint32
 
 // The same features in E4M3 for the FP8 query: feature k, multiplied by inv_s
 // (448 / the features' absmax scale), rounded to nearest even and saturated,
-// in byte k % 4 of word k / 4 (words 0..15 of e).
+// in byte k % 4 of word k / 4. Split like the 16-bit encode at feature 32:
+// half 0 gives words 0..7 (features 0..31), half 1 words 8..15.
+__device__ __forceinline__ uint32_t e4m3_q4(float a, float b, float c, float d, float inv_s) {
+  return pack4_e4m3(__fmul_rn(a, inv_s), __fmul_rn(b, inv_s), __fmul_rn(c, inv_s), __fmul_rn(d, inv_s));
+}
+// triangle-wave frequency k of coordinate p (the two forms agree; see enc_tri_h)
+__device__ __forceinline__ float enc_tri_k(float p, int k) {
+  return fabsf(p) < 0x1p100f ? enc_tri_h(p, 0.5f * static_cast<float>(1 << k)) : enc_tri(p, static_cast<float>(1 << k));
+}
+// four triangle-wave features of coordinate p, frequencies 4w..4w+3
+__device__ __forceinline__ uint32_t enc_tri4_e4m3(float p, int w, float inv_s) {
+  return e4m3_q4(enc_tri_k(p, 4 * w), enc_tri_k(p, 4 * w + 1), enc_tri_k(p, 4 * w + 2), enc_tri_k(p, 4 * w + 3), inv_s);
+}
+__device__ __forceinline__ uint32_t enc_blob_e4m3(float x, float inv_s) {
+  float f0, f1, f2, f3;
+  enc_qcdf_x2(0.0f, 1.0f, x, f0, f1);
+  enc_qcdf_x2(2.0f, 3.0f, x, f2, f3);
+  const float f4 = enc_qcdf(4.0f, x);
+  return e4m3_q4(__fsub_rn(f1, f0), __fsub_rn(f2, f1), __fsub_rn(f3, f2), __fsub_rn(f4, f3), inv_s);
+}
+
+__device__ __forceinline__ void encode_e4m3_half0(const float (&r)[kInFloats], float inv_s, uint32_t* e) {
+#pragma unroll
+  for (int c = 0; c < 2; ++c)
+#pragma unroll
+    for (int w = 0; w < 3; ++w) e[3 * c + w] = enc_tri4_e4m3(r[c], w, inv_s);
+  e[6] = enc_tri4_e4m3(r[2], 0, inv_s);
+  e[7] = enc_tri4_e4m3(r[2], 1, inv_s);
+}
+
+__device__ __forceinline__ void encode_e4m3_half1(const float (&r)[kInFloats], float inv_s, uint32_t* e) {
+  e[0] = enc_tri4_e4m3(r[2], 2, inv_s);
+  e[1] = enc_blob_e4m3(r[3], inv_s);
+  e[2] = enc_blob_e4m3(r[4], inv_s);
+  e[3] = enc_blob_e4m3(r[5], inv_s);
+  e[4] = enc_blob_e4m3(r[6], inv_s);
+  e[5] = enc_blob_e4m3(__fsub_rn(1.0f, enc_expf(-r[7])), inv_s);
+  e[6] = e4m3_q4(r[8], r[9], r[10], r[11], inv_s);
+  e[7] = e4m3_q4(r[12], r[13], 1.0f, 1.0f, inv_s);
+}
+
 __device__ __forceinline__ void encode_input_e4m3(const float (&r)[kInFloats], float inv_s, uint32_t (&e)[32]) {
-  auto q4 = [&](float a, float b, float c, float d) {
-    return pack4_e4m3(__fmul_rn(a, inv_s), __fmul_rn(b, inv_s), __fmul_rn(c, inv_s), __fmul_rn(d, inv_s));
-  };
-  // triangle-wave frequency k of coordinate p (the two forms agree; see enc_tri_h)
-  auto tri = [](float p, int k) {
-    return fabsf(p) < 0x1p100f ? enc_tri_h(p, 0.5f * static_cast<float>(1 << k))
-                               : enc_tri(p, static_cast<float>(1 << k));
-  };
-#pragma unroll
-  for (int c = 0; c < 3; ++c)
-#pragma unroll
-    for (int w = 0; w < 3; ++w)
-      e[3 * c + w] = q4(tri(r[c], 4 * w), tri(r[c], 4 * w + 1), tri(r[c], 4 * w + 2), tri(r[c], 4 * w + 3));
-  auto blob = [&](float x) {
-    float f0, f1, f2, f3;
-    enc_qcdf_x2(0.0f, 1.0f, x, f0, f1);
-    enc_qcdf_x2(2.0f, 3.0f, x, f2, f3);
-    const float f4 = enc_qcdf(4.0f, x);
-    return q4(__fsub_rn(f1, f0), __fsub_rn(f2, f1), __fsub_rn(f3, f2), __fsub_rn(f4, f3));
-  };
-  e[9] = blob(r[3]);
-  e[10] = blob(r[4]);
-  e[11] = blob(r[5]);
-  e[12] = blob(r[6]);
-  e[13] = blob(__fsub_rn(1.0f, enc_expf(-r[7])));
-  e[14] = q4(r[8], r[9], r[10], r[11]);
-  e[15] = q4(r[12], r[13], 1.0f, 1.0f);
+  encode_e4m3_half0(r, inv_s, e);
+  encode_e4m3_half1(r, inv_s, e + 8);
 }
 
 // Device-side error word bits (read back by nrc_get_error).

@@ -19,6 +19,7 @@
 
 #include "nrc_common.cuh"
 #include "nrc_kernels.h"
+#include "nrc_unpack.cuh"
 
 namespace nrc {
 
@@ -31,10 +32,17 @@ constexpr uint32_t kRecBytes = sizeof(nrc_input);      // 56
 constexpr uint32_t kRecTileBytes = kTile * kRecBytes;  // 7168
 constexpr uint32_t kRecSmemOff = kWeightSmemBytes;     // 43008, 1024-aligned
 constexpr uint32_t kBarOff = kRecSmemOff + kSlots * 2 * kRecTileBytes;
-constexpr uint32_t kSmemBytes = kBarOff + 512 + 1024;  // + alignment slack
+constexpr uint32_t kLutOff = kBarOff + 512;            // packed records: the sRGB decode table
+constexpr uint32_t kSmemBytes = kLutOff + 1024 + 1024;  // + alignment slack
+constexpr uint32_t kPackedBytes = sizeof(nrc_eval_record);  // 20: packed eval records (scene unpack fused)
+static_assert(kPackedBytes == 20, "nrc_eval_record layout");
 static_assert(kWeightSmemBytes % 1024 == 0, "weight tiles 1024-aligned");
 static_assert(kSlots * kSlotCols <= 512, "TMEM columns");
 static_assert(kJoinChunks * 16 == kParams * 2, "join copy covers the weights");
+
+// sRGB -> linear table of the packed-record query (srgb_lut(), written by
+// configure_infer_kernels on each device).
+__device__ float g_srgb[256];
 
 struct SlotBars {
   uint64_t rec_full[2];   // bulk copy of a record tile landed (tx bytes)
@@ -49,16 +57,17 @@ __device__ __forceinline__ uint8_t* align1024(uint8_t* p) {
   return reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(p) + 1023) & ~uintptr_t(1023));
 }
 
-// Issue the bulk copy of record tile `tile` into `dst`. Full tiles move 7168
-// bytes; the last, partial tile moves the largest 16-byte multiple of its bytes
-// and its trailing record (if cut) is read directly from global memory.
-__device__ __forceinline__ void issue_record_tile(const nrc_input* __restrict__ in, uint32_t tile, uint32_t n,
-                                                  uint8_t* dst, uint64_t* full) {
+// Issue the bulk copy of record tile `tile` (records of rec_bytes each) into
+// `dst`. Full tiles move 128 records; the last, partial tile moves the largest
+// 16-byte multiple of its bytes and its trailing record (if cut) is read
+// directly from global memory.
+__device__ __forceinline__ void issue_record_tile(const void* __restrict__ in, uint32_t rec_bytes, uint32_t tile,
+                                                  uint32_t n, uint8_t* dst, uint64_t* full) {
   const uint32_t rows = min(static_cast<uint32_t>(kTile), n - tile * kTile);
-  const uint32_t bytes = rows == kTile ? kRecTileBytes : ((rows * kRecBytes) & ~15u);
+  const uint32_t bytes = (rows * rec_bytes) & ~15u;  // full tiles: 7168 or 2560, multiples of 16
   if (bytes > 0) {
     mbar_arrive_expect_tx(full, bytes);
-    bulk_g2s(dst, reinterpret_cast<const uint8_t*>(in) + static_cast<size_t>(tile) * kRecTileBytes, bytes, full);
+    bulk_g2s(dst, static_cast<const uint8_t*>(in) + static_cast<size_t>(tile) * kTile * rec_bytes, bytes, full);
   } else {
     mbar_arrive(full);
   }
@@ -98,11 +107,11 @@ __device__ __forceinline__ void scatter_query(const QueryOut& Q, uint32_t dst, f
     *bf = make_float4(__fmaf_rn(v.w, p0, v.x), __fmaf_rn(gb.x, p1, v.y), __fmaf_rn(gb.y, p2, v.z), 0.0f);
   } else {  // train records l..r of batch b: bias += factor * p
     const uint32_t b = e & 3u, l = (e >> 2) & 0x3FFFu, r = e >> 16;
-    float* rec = reinterpret_cast<float*>(Q.train[b]);
+    float* rec = Q.train[b];
     if (rec == nullptr) return;
     const uint32_t end = min(r + 1, Q.train_cap[b]);
     for (uint32_t i = l; i < end; ++i) {
-      float* t = rec + static_cast<size_t>(i) * (sizeof(nrc_train_record) / 4);
+      float* t = rec + static_cast<size_t>(i) * Q.train_stride;
       t[0] = __fmaf_rn(t[3], p0, t[0]);
       t[1] = __fmaf_rn(t[4], p1, t[1]);
       t[2] = __fmaf_rn(t[5], p2, t[2]);
@@ -119,7 +128,11 @@ __device__ __forceinline__ void scatter_query(const QueryOut& Q, uint32_t dst, f
 // layer's fp32 sum multiplied by its scale constant before the ReLU and the
 // conversion; the weights keep the 128-byte rows of the 16-bit layout, K bytes
 // 64..127 being zero and never read).
-template <bool kEncoded, bool kScatter, int N, int kFmt>
+// kPacked: the input is the reference's 20-byte eval records (nrc_eval_record)
+// over the job's scene: each thread unpacks its record (UnpackNRCInput, the
+// gathers of nrc_unpack.cuh) before the encode, and the destination word is the
+// record's own.
+template <bool kEncoded, bool kScatter, int N, int kFmt, bool kPacked = false>
 __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_constant__ InferLaunch<N> L) {
 
   constexpr bool kBF16 = kFmt == 1, kF8 = kFmt == 2;
@@ -140,6 +153,11 @@ __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_co
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(w_full + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  constexpr uint32_t rec_bytes = kPacked ? kPackedBytes : kRecBytes;
+  float* lut = reinterpret_cast<float*>(smem + kLutOff);
+  if (kPacked) {
+    for (uint32_t i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = g_srgb[i];
+  }
 
   // dynamic tiles (single-cache record queries with a tile counter)
   const bool dyn = N == 1 && !kEncoded && J.tiles != nullptr;
@@ -183,7 +201,7 @@ __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_co
   const uint64_t wdesc = sdesc_sw128(smem_u32(smem_w), 16, 1024);  // layer l: + l * 512
   const uint32_t id64 = idesc_16_f32(128, 64, 0, 0, kBF16), id16 = idesc_16_f32(128, 16, 0, 0, kBF16);
   uint8_t* stage0 = smem_rec + (s * 2 + 0) * kRecTileBytes;
-  const nrc_input* rec_in = static_cast<const nrc_input*>(input);
+  const uint8_t* rec_in = static_cast<const uint8_t*>(input);
   auto tile_of = [&](uint32_t it) { return (it * G + rank) * kSlots + s; };
 
   // The copy of the slot's tile into record stage b; with dynamic tiles the
@@ -194,11 +212,11 @@ __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_co
       const uint32_t t = atomicAdd(J.tiles, 1u);
       B.tile[b] = t;
       if (t < num_tiles)
-        issue_record_tile(rec_in, t, n, stage0 + b * kRecTileBytes, &B.rec_full[b]);
+        issue_record_tile(rec_in, rec_bytes, t, n, stage0 + b * kRecTileBytes, &B.rec_full[b]);
       else
         mbar_arrive(&B.rec_full[b]);
     } else if (static_tile < num_tiles) {
-      issue_record_tile(rec_in, static_tile, n, stage0 + b * kRecTileBytes, &B.rec_full[b]);
+      issue_record_tile(rec_in, rec_bytes, static_tile, n, stage0 + b * kRecTileBytes, &B.rec_full[b]);
     }
   };
   if (!kEncoded && leader)
@@ -225,12 +243,20 @@ __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_co
         ok = warp_all(mbar_wait(&B.rec_full[b], (it >> 1) & 1, kWaitLimitNs));
         if (!ok) break;
       }
-      const uint32_t bulk = rows_valid == kTile ? kRecTileBytes : ((rows_valid * kRecBytes) & ~15u);
+      const uint32_t bulk = (rows_valid * rec_bytes) & ~15u;
       float r[kInFloats];
-      if (row < static_cast<int>(rows_valid)) {
-        const float2* src = (static_cast<uint32_t>(row + 1) * kRecBytes <= bulk)
-                                ? reinterpret_cast<const float2*>(stage + row * kRecBytes)
-                                : reinterpret_cast<const float2*>(rec_in + grow);
+      if (kPacked && row < static_cast<int>(rows_valid)) {
+        // the 20-byte record (4-byte aligned in the stage and in memory)
+        const uint32_t* src = (static_cast<uint32_t>(row + 1) * rec_bytes <= bulk)
+                                  ? reinterpret_cast<const uint32_t*>(stage + row * rec_bytes)
+                                  : reinterpret_cast<const uint32_t*>(rec_in + grow * rec_bytes);
+        const nrc_packed_input pin{src[1], src[2], src[3], src[4]};
+        qdst = src[0];
+        unpack_one(J.scene, pin, lut, r);
+      } else if (row < static_cast<int>(rows_valid)) {
+        const float2* src = (static_cast<uint32_t>(row + 1) * rec_bytes <= bulk)
+                                ? reinterpret_cast<const float2*>(stage + row * rec_bytes)
+                                : reinterpret_cast<const float2*>(rec_in + grow * rec_bytes);
 #pragma unroll
         for (int k = 0; k < 7; ++k) {
           const float2 v = src[k];
@@ -301,7 +327,7 @@ __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_co
         }
       }
       // load the destination word while the output layer's MMAs run
-      if (kScatter && l == 5 && row < static_cast<int>(rows_valid)) qdst = __ldg(Q.dst + grow);
+      if (kScatter && !kPacked && l == 5 && row < static_cast<int>(rows_valid)) qdst = __ldg(Q.dst + grow);
       const float cl = kF8 ? J.fp8->c[l] : 1.0f;  // the layer's scale constant (FP8 query)
       ok = ok && warp_all(mbar_wait(&B.d_ready, ph_d, kWaitLimitNs));
       if (!ok) break;
@@ -386,7 +412,7 @@ __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_co
   }
 }
 
-template <bool kEncoded, bool kScatter, int N, int kFmt>
+template <bool kEncoded, bool kScatter, int N, int kFmt, bool kPacked = false>
 cudaError_t launch(const InferLaunch<N>& L, uint32_t grid, cudaStream_t stream) {
   cudaLaunchAttribute attr;
   attr.id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -398,13 +424,19 @@ cudaError_t launch(const InferLaunch<N>& L, uint32_t grid, cudaStream_t stream) 
   cfg.stream = stream;
   cfg.attrs = &attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, infer_kernel<kEncoded, kScatter, N, kFmt>, L);
+  return cudaLaunchKernelEx(&cfg, infer_kernel<kEncoded, kScatter, N, kFmt, kPacked>, L);
 }
 
-template <bool kEncoded, bool kScatter, int N, int kFmt>
+// The shared-memory limit, and the largest carveout: the query and the trainer
+// (206 KB) then run in the same SM configuration, so an SM passing from one to
+// the other between kernels needs no reconfiguration.
+template <bool kEncoded, bool kScatter, int N, int kFmt, bool kPacked = false>
 cudaError_t set_smem() {
-  return cudaFuncSetAttribute(infer_kernel<kEncoded, kScatter, N, kFmt>,
-                              cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+  cudaError_t e = cudaFuncSetAttribute(infer_kernel<kEncoded, kScatter, N, kFmt, kPacked>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(infer_kernel<kEncoded, kScatter, N, kFmt, kPacked>,
+                              cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
 }
 
 }  // namespace
@@ -418,6 +450,12 @@ cudaError_t configure_infer_kernels() {
   if (e == cudaSuccess) e = set_smem<false, true, 1, 1>();
   if (e == cudaSuccess) e = set_smem<false, false, kMaxInferJobs, 1>();
   if (e == cudaSuccess) e = set_smem<false, false, 1, 2>();
+  if (e == cudaSuccess) e = set_smem<false, false, 1, 0, true>();
+  if (e == cudaSuccess) e = set_smem<false, true, 1, 0, true>();
+  if (e == cudaSuccess) e = set_smem<false, false, 1, 1, true>();
+  if (e == cudaSuccess) e = set_smem<false, true, 1, 1, true>();
+  // the sRGB decode table the packed-record query stages into shared memory
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_srgb, srgb_lut().v, sizeof(g_srgb));
   return e;
 }
 
@@ -474,6 +512,32 @@ cudaError_t launch_infer_frame(const nrc_input* input, const uint32_t* d_count, 
   if (q.dst != nullptr)
     return bf16 ? launch<false, true, 1, 1>(L, grid, stream) : launch<false, true, 1, 0>(L, grid, stream);
   return bf16 ? launch<false, false, 1, 1>(L, grid, stream) : launch<false, false, 1, 0>(L, grid, stream);
+}
+
+cudaError_t launch_infer_packed(const nrc_eval_record* input, const nrc_scene& scene, const uint32_t* d_count,
+                                uint32_t capacity, const CUtensorMap* wmap, const QueryOut& q, uint32_t* err,
+                                uint32_t* tiles, const FrameJoin& join, uint32_t grid, cudaStream_t stream, bool bf16) {
+  if (grid == 0) return cudaSuccess;
+  InferLaunch<1> L;
+  L.job[0] = InferJob{};
+  L.job[0].wmap = *wmap;
+  L.job[0].input = input;
+  L.job[0].d_count = d_count;
+  L.job[0].capacity = capacity;
+  L.job[0].err = err;
+  L.job[0].q = q;
+  L.job[0].scene = scene;
+  if (tiles != nullptr) {  // the overlapped frame's query: dynamic tiles, started beside the training
+    L.job[0].tiles = tiles;
+    L.job[0].no_wait = 1;
+    L.job[0].join = join;
+  }
+  L.group_start[0] = 0;
+  L.group_start[1] = grid;
+  L.njobs = 1;
+  if (q.scatter)
+    return bf16 ? launch<false, true, 1, 1, true>(L, grid, stream) : launch<false, true, 1, 0, true>(L, grid, stream);
+  return bf16 ? launch<false, false, 1, 1, true>(L, grid, stream) : launch<false, false, 1, 0, true>(L, grid, stream);
 }
 
 cudaError_t launch_infer_fp8(const nrc_input* input, const uint32_t* d_count, uint32_t capacity,

@@ -41,12 +41,14 @@ int infer_tiles_per_cta();
 struct QueryOut {
   float* out;
   int clamp;
+  int scatter;  // packed-record queries: run the destination epilogue on the records' own words
   const uint32_t* dst;
   float* bias_factor_r;
   const float* factor_gb;
   uint32_t width, height;
-  nrc_train_record* train[NRC_TRAIN_BATCH_COUNT];
+  float* train[NRC_TRAIN_BATCH_COUNT];  // train records whose targets the queries complete
   uint32_t train_cap[NRC_TRAIN_BATCH_COUNT];
+  uint32_t train_stride;  // floats per train record: 20 (nrc_train_record) or 10 (nrc_packed_train_record)
 };
 
 // bf16: the weights and the operands are bf16 (the bf16 precision form); the
@@ -110,6 +112,7 @@ struct InferJob {
   // reads nothing that training writes).
   uint32_t no_wait;
   FrameJoin join;  // dynamic tiles only: joined by the last CTA out
+  nrc_scene scene;  // packed eval records: the scene their records unpack from
 };
 
 // Kernel parameters of a query launch over up to N caches; CTAs
@@ -144,6 +147,14 @@ uint32_t infer_grid(uint32_t capacity, int num_sms);
 cudaError_t launch_infer_frame(const nrc_input* input, const uint32_t* d_count, uint32_t capacity,
                                const CUtensorMap* wmap, const QueryOut& q, uint32_t* err, uint32_t* tiles,
                                const FrameJoin& join, uint32_t grid, cudaStream_t stream, bool bf16);
+// The query over the reference's packed eval records (nrc_eval_record, 20 B)
+// of `scene`: each record is unpacked in the kernel (UnpackNRCInput) before the
+// encode. q.scatter: the destination epilogue with each record's own
+// destination word (q.dst unused); tiles non-null: the overlapped frame's
+// dynamic-tile form of launch_infer_frame.
+cudaError_t launch_infer_packed(const nrc_eval_record* input, const nrc_scene& scene, const uint32_t* d_count,
+                                uint32_t capacity, const CUtensorMap* wmap, const QueryOut& q, uint32_t* err,
+                                uint32_t* tiles, const FrameJoin& join, uint32_t grid, cudaStream_t stream, bool bf16);
 // One launch answering njobs caches' record queries (dense rgb output, no
 // destination words), group_size[j] >= 1 CTAs for job j, sum <= SMs.
 cudaError_t launch_infer_many(const InferJob* jobs, int njobs, const uint32_t* group_size, cudaStream_t stream,
@@ -229,6 +240,11 @@ cudaError_t launch_encode(const nrc_input* in, const uint32_t* d_count, uint32_t
                           int num_sms, cudaStream_t stream);
 cudaError_t launch_sph_encode(const float* dirs, const uint32_t* d_count, uint32_t capacity, float* out,
                               int num_sms, cudaStream_t stream);
+// The train records of nbatches batches (min(*counts[b], capacity) each) in one
+// launch, into unpacked arrays out[b].
+cudaError_t launch_unpack_train_batches(const nrc_scene& scene, const nrc_packed_train_record* const* in,
+                                       uint32_t* const* counts, uint32_t capacity, nrc_train_record* const* out,
+                                       int nbatches, int num_sms, cudaStream_t stream);
 cudaError_t launch_unpack(const nrc_scene& scene, bool train, const void* in, const uint32_t* d_count,
                           uint32_t capacity, void* out, uint32_t* out_dst, int num_sms, cudaStream_t stream);
 cudaError_t launch_screen(const float* color, float* accum, uint32_t width, uint32_t height, int acc_on,

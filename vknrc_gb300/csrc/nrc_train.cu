@@ -755,7 +755,8 @@ cudaError_t configure_train_kernels() {
                       reinterpret_cast<const void*>(train_steps_kernel<kMaxTrainJobs, true>)};
   cudaError_t e = cudaSuccess;
   for (int i = 0; i < 4 && e == cudaSuccess; ++i)
-    e = cudaFuncSetAttribute(k[i], cudaFuncAttributeMaxDynamicSharedMemorySize, kTrainSmemBytes);
+    if ((e = cudaFuncSetAttribute(k[i], cudaFuncAttributeMaxDynamicSharedMemorySize, kTrainSmemBytes)) == cudaSuccess)
+      e = cudaFuncSetAttribute(k[i], cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
   return e;
 }
 

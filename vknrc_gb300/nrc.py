@@ -36,7 +36,8 @@ EXPORTS = [
     "nrc_server_get_stats", "nrc_screen", "nrc_checkpoint_bytes", "nrc_save_checkpoint", "nrc_load_checkpoint",
     "nrc_unpack_eval", "nrc_unpack_train", "nrc_infer_fp8", "nrc_fp8_refresh", "nrc_get_fp8",
     "nrc_frame_overlapped", "nrc_autotune_frame", "nrc_bvh_build", "nrc_bvh_destroy", "nrc_bvh_info",
-    "nrc_path_trace", "nrc_optimize", "nrc_loss_gradient",
+    "nrc_path_trace", "nrc_optimize", "nrc_loss_gradient", "nrc_infer_packed", "nrc_infer_scatter_packed",
+    "nrc_frame_packed", "nrc_frame_scatter_packed",
 ]
 
 
@@ -72,8 +73,9 @@ class ScatterTargets(ctypes.Structure):
 
 def scatter_targets(bias_factor_r=None, factor_gb=None, train_records: Sequence = ()) -> ScatterTargets:
     """Build the targets from CUDA tensors: bias_factor_r (H, W, 4) and
-    factor_gb (H, W, 2) float32 images, up to four (cap, 20) train record arrays
-    (None entries are skipped)."""
+    factor_gb (H, W, 2) float32 images, up to four train record arrays: (cap, 20)
+    nrc_train_record rows, or (cap, 10) nrc_packed_train_record rows for the
+    packed-record calls (None entries are skipped)."""
     t = ScatterTargets()
     if bias_factor_r is not None:
         t.bias_factor_r = _ptr(bias_factor_r)
@@ -224,6 +226,13 @@ def lib(build_if_missing: bool = True) -> ctypes.CDLL:
     L.nrc_path_trace.argtypes = [ctypes.POINTER(SceneStruct), vp, ctypes.POINTER(TraceParams),
                                  ctypes.POINTER(TraceTargets), vp]
     L.nrc_unpack_eval.argtypes = [ctypes.POINTER(SceneStruct), vp, vp, u32, vp, vp, vp]
+    L.nrc_infer_packed.argtypes = [vp, ctypes.POINTER(SceneStruct), vp, vp, u32, vp, i32, vp]
+    L.nrc_infer_scatter_packed.argtypes = [vp, ctypes.POINTER(SceneStruct), vp, vp, u32,
+                                           ctypes.POINTER(ScatterTargets), vp, i32, vp]
+    L.nrc_frame_packed.argtypes = [vp, ctypes.POINTER(SceneStruct), vp, vp, u32, vp, ctypes.POINTER(vp),
+                                   ctypes.POINTER(vp), u32, vp]
+    L.nrc_frame_scatter_packed.argtypes = [vp, ctypes.POINTER(SceneStruct), vp, vp, u32,
+                                           ctypes.POINTER(ScatterTargets), ctypes.POINTER(vp), vp]
     L.nrc_unpack_train.argtypes = [ctypes.POINTER(SceneStruct), vp, vp, u32, vp, vp]
     L.nrc_checkpoint_bytes.restype = ctypes.c_size_t
     L.nrc_checkpoint_bytes.argtypes = []
@@ -321,6 +330,41 @@ class Cache:
         cnts = (ctypes.c_void_p * TRAIN_BATCH_COUNT)(*[_ptr(c) for c in train_counts])
         check(lib().nrc_frame_scatter(self.h, _ptr(eval_inputs), _ptr(eval_dst), _ptr(eval_count), ecap,
                                       ctypes.byref(targets), cnts, _stream(stream)), "nrc_frame_scatter")
+
+    # ------------------------------------------- the reference's record formats --
+    def infer_packed(self, scene: "DeviceScene", records, count, out, capacity=None, weight_set=WEIGHTS_USE,
+                     stream=None):
+        """nrc_infer_packed: (n, 5) packed eval records of `scene` -> (n, 3) clamped rgb."""
+        cap = records.shape[0] if capacity is None else capacity
+        check(lib().nrc_infer_packed(self.h, ctypes.byref(scene.s), _ptr(records), _ptr(count), cap, _ptr(out),
+                                     weight_set, _stream(stream)), "nrc_infer_packed")
+
+    def infer_scatter_packed(self, scene: "DeviceScene", records, count, targets: ScatterTargets, out=None,
+                             capacity=None, weight_set=WEIGHTS_USE, stream=None):
+        """nrc_infer_scatter_packed: targets from scatter_targets() with (cap, 10) packed train records."""
+        cap = records.shape[0] if capacity is None else capacity
+        check(lib().nrc_infer_scatter_packed(self.h, ctypes.byref(scene.s), _ptr(records), _ptr(count), cap,
+                                             ctypes.byref(targets), _ptr(out), weight_set, _stream(stream)),
+              "nrc_infer_scatter_packed")
+
+    def frame_packed(self, scene: "DeviceScene", eval_records, eval_count, out, train_records: Sequence,
+                     train_counts: Sequence, eval_capacity=None, train_capacity=None, stream=None):
+        """nrc_frame_packed: packed eval records (n, 5) and four packed train batches (cap, 10)."""
+        ecap = eval_records.shape[0] if eval_capacity is None else eval_capacity
+        tcap = train_records[0].shape[0] if train_capacity is None else train_capacity
+        recs = (ctypes.c_void_p * TRAIN_BATCH_COUNT)(*[_ptr(r) for r in train_records])
+        cnts = (ctypes.c_void_p * TRAIN_BATCH_COUNT)(*[_ptr(c) for c in train_counts])
+        check(lib().nrc_frame_packed(self.h, ctypes.byref(scene.s), _ptr(eval_records), _ptr(eval_count), ecap,
+                                     _ptr(out), recs, cnts, tcap, _stream(stream)), "nrc_frame_packed")
+
+    def frame_scatter_packed(self, scene: "DeviceScene", eval_records, eval_count, targets: ScatterTargets,
+                             train_counts: Sequence, eval_capacity=None, stream=None):
+        """nrc_frame_scatter_packed: the reference's frame on its record formats."""
+        ecap = eval_records.shape[0] if eval_capacity is None else eval_capacity
+        cnts = (ctypes.c_void_p * TRAIN_BATCH_COUNT)(*[_ptr(c) for c in train_counts])
+        check(lib().nrc_frame_scatter_packed(self.h, ctypes.byref(scene.s), _ptr(eval_records), _ptr(eval_count),
+                                             ecap, ctypes.byref(targets), cnts, _stream(stream)),
+              "nrc_frame_scatter_packed")
 
     def train(self, records, count, capacity=None, write_use=False, stream=None):
         cap = records.shape[0] if capacity is None else capacity
