@@ -502,26 +502,33 @@ def batched_leg(evals, trains, steps=50):
     tc = [[torch.tensor([r], dtype=torch.int32, device="cuda") for _ in range(B)] for r in BATCHED_TRAIN]
     qjobs = [nrc.query_job(c, q, k, o) for c, q, k, o in zip(caches, qs, qc, outs)]
     tjobs = [nrc.train_job(c, rr, t) for c, rr, t in zip(caches, recs, tc)]
-    plan_q, plan_t = nrc.plan_query_ctas(qjobs), nrc.plan_train_ctas(tjobs)
+    prop_q, prop_t = nrc.plan_query_ctas(qjobs), nrc.plan_train_ctas(tjobs)
+    # the library's autotuner times candidate splits (training on scratch copies of the caches)
+    plan_q, plan_t, tuned_q_ms, tuned_t_ms = nrc.autotune_many(qjobs, tjobs)
     stream = torch.cuda.Stream()
     stream.wait_stream(torch.cuda.current_stream())
-    with torch.cuda.stream(stream):
-        for _ in range(3):
-            nrc.infer_many(qjobs, stream=stream)
-            nrc.train_many(tjobs, stream=stream)
-        g = torch.cuda.CUDAGraph()
-        with torch.cuda.graph(g, stream=stream):
-            nrc.infer_many(qjobs, stream=stream)
-            nrc.train_many(tjobs, stream=stream)
-        for _ in range(3):
-            g.replay()
-        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        s.record(stream)
-        for _ in range(steps):
-            g.replay()
-        e.record(stream)
-    stream.synchronize()
-    batched_s = s.elapsed_time(e) / 1e3 / steps
+
+    def graph_frame_s(gq, gt):
+        with torch.cuda.stream(stream):
+            for _ in range(3):
+                nrc.infer_many(qjobs, ctas=gq, stream=stream)
+                nrc.train_many(tjobs, ctas=gt, stream=stream)
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, stream=stream):
+                nrc.infer_many(qjobs, ctas=gq, stream=stream)
+                nrc.train_many(tjobs, ctas=gt, stream=stream)
+            for _ in range(3):
+                g.replay()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            for _ in range(steps):
+                g.replay()
+            e.record(stream)
+        stream.synchronize()
+        return s.elapsed_time(e) / 1e3 / steps
+
+    proportional_s = graph_frame_s(prop_q, prop_t)
+    batched_s = graph_frame_s(plan_q, plan_t)
     # the same work, cache after cache, through nrc_frame
     cur = torch.cuda.current_stream()
 
@@ -553,7 +560,11 @@ def batched_leg(evals, trains, steps=50):
         "one_by_one": {"ms_per_frame": solo_s * 1e3, "cache_frames_per_s": n / solo_s,
                        "what": "nrc_frame per cache, cache after cache (query kernel + training launch each)"},
         "speedup_vs_one_by_one": solo_s / batched_s,
-        "ctas": {"query": plan_q, "train": plan_t, "chosen_by": "proportional split of the SMs by tiles"},
+        "ctas": {"query": plan_q, "train": plan_t,
+                 "chosen_by": "nrc_autotune_many (proportional split and the just-enough split for each tiles-per-"
+                              "CTA count, each launch timed; training on scratch copies)",
+                 "tuned_launch_ms": {"query": tuned_q_ms, "train": tuned_t_ms},
+                 "proportional": {"query": prop_q, "train": prop_t, "ms_per_frame": proportional_s * 1e3}},
     }
 
 
@@ -750,6 +761,14 @@ def serving_leg(evals, trains, seconds=2.0, sessions=32, rate=2000.0, budget=40 
         who = rng.integers(0, sessions, n)
         wall = run(list(zip(times.tolist(), who.tolist())))
         st_poisson = srv.stats(reset=True)
+        # a heavier Poisson stream, near the saturation throughput: requests queue and
+        # the worker batches several sessions per launch
+        rate_hi = 3.0 * rate
+        n_hi = int(rate_hi * seconds)
+        times_hi = np.cumsum(rng.exponential(1.0 / rate_hi, n_hi))
+        who_hi = rng.integers(0, sessions, n_hi)
+        wall_hi = run(list(zip(times_hi.tolist(), who_hi.tolist())))
+        st_hi = srv.stats(reset=True)
         # saturation: every request submitted at once (closed batch of work)
         m = 8 * sessions
         wall_sat = run([(0.0, k % sessions) for k in range(m)])
@@ -789,6 +808,10 @@ def serving_leg(evals, trains, seconds=2.0, sessions=32, rate=2000.0, budget=40 
         "latency_ms": {"p50": st_poisson["latency_p50_ms"], "p99": st_poisson["latency_p99_ms"],
                        "max": st_poisson["latency_max_ms"]},
         "mean_batch_sessions": st_poisson["mean_batch_sessions"],
+        "high_load": {"offered_req_per_s": rate_hi, "requests": n_hi, "frames_per_s": n_hi / wall_hi,
+                      "latency_ms": {"p50": st_hi["latency_p50_ms"], "p99": st_hi["latency_p99_ms"],
+                                     "max": st_hi["latency_max_ms"]},
+                      "mean_batch_sessions": st_hi["mean_batch_sessions"]},
         "saturation": {"requests": m, "frames_per_s": sat_fps, "queries_per_s": sat_q / wall_sat,
                        "latency_p50_ms": st_sat["latency_p50_ms"],
                        "latency_p99_ms": st_sat["latency_p99_ms"],

@@ -380,6 +380,20 @@ NRC_API int nrc_train_many(const nrc_train_job* jobs, uint32_t njobs, const uint
 NRC_API int nrc_plan_query_ctas(const nrc_query_job* jobs, uint32_t njobs, uint32_t* out_ctas);
 NRC_API int nrc_plan_train_ctas(const nrc_train_job* jobs, uint32_t njobs, uint32_t* out_ctas);
 
+/* The batched launches' autotuner (no counterpart in the reference, which runs
+ * one cache): times candidate CTA splits of one nrc_infer_many launch (nq <= 32
+ * jobs, one precision, capacities > 0) and of one nrc_train_many launch
+ * (nt <= 32 jobs, one precision) and writes the fastest to q_ctas / t_ctas (nq /
+ * nt entries), their mean launch times to q_ms / t_ms (may be NULL). The
+ * candidates are the proportional default and, for each number of tiles per
+ * CTA, the split that gives every job just the CTAs that number needs. Query
+ * candidates run on the jobs themselves (they write the jobs' outputs);
+ * training candidates run on scratch copies of the caches, so the caller's
+ * caches are not trained (their count buffers are clamped as by a call).
+ * Synchronous; allocates the scratch caches for its duration. */
+NRC_API int nrc_autotune_many(const nrc_query_job* qjobs, uint32_t nq, const nrc_train_job* tjobs, uint32_t nt,
+                              uint32_t* q_ctas, uint32_t* t_ctas, float* q_ms, float* t_ms);
+
 /* ---------------------------------------------------------------------------
  * Serving: a device-resident loop over many render sessions. No counterpart in
  * the reference, which serves one renderer (src/main.cpp:84-91); each session
@@ -522,9 +536,11 @@ typedef struct nrc_packed_train_record {
 
 /* The reference's inference pass on its own record format: queries over
  * min(*d_count, capacity) packed eval records (nrc_eval_record, 20 bytes,
- * d_records 16-byte aligned) of `scene`, each unpacked inside the query kernel
- * (UnpackNRCInput, NRCRecord.glsl:97-125, as nrc_inference.comp:33-36 does)
- * before the encode and the MLP. nrc_infer_packed writes the clamped
+ * d_records 4-byte aligned) of `scene`, unpacked (UnpackNRCInput,
+ * NRCRecord.glsl:97-125, as nrc_inference.comp:33-36 does) by one launch into a
+ * workspace the context keeps, then queried. The first call with a larger
+ * capacity allocates the workspace (56 + 4 bytes per record), so make it before
+ * any stream capture. nrc_infer_packed writes the clamped
  * predictions to d_out_rgb (3 floats per record; the destination words are not
  * used). nrc_infer_scatter_packed runs the destination epilogue
  * (nrc_inference.comp:50-73) with each record's own destination word: screen
@@ -548,12 +564,11 @@ NRC_API int nrc_infer_scatter_packed(nrc_context* ctx, const nrc_scene* scene, c
                                      const nrc_packed_scatter_targets* targets, float* d_out_rgb, int weight_set,
                                      void* stream);
 
-/* One frame on the reference's record formats: the packed train batches are
- * unpacked (one launch, into a workspace the context keeps: the first call
- * with a larger train_capacity allocates it, so make that call before any
- * stream capture), then the frame runs as nrc_frame_overlapped with the
- * packed-record query (results to d_out_rgb as nrc_infer_packed) beside the
- * four training steps. */
+/* One frame on the reference's record formats: the packed train batches and
+ * the packed eval records are unpacked (two launches, into workspaces the
+ * context keeps: the first call with a larger capacity allocates them, so make
+ * that call before any stream capture), then the frame runs as
+ * nrc_frame_overlapped (results to d_out_rgb as nrc_infer_packed). */
 NRC_API int nrc_frame_packed(nrc_context* ctx, const nrc_scene* scene, const nrc_eval_record* d_eval_records,
                              const uint32_t* d_eval_count, uint32_t eval_capacity, float* d_out_rgb,
                              const nrc_packed_train_record* const* d_train_records, uint32_t* const* d_train_counts,

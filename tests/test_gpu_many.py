@@ -179,3 +179,44 @@ def test_batched_frame_graph_capture_replays(cuda):
     finally:
         for c in eager + graphed:
             c.close()
+
+
+def test_autotune_many_valid_split_and_caches_untouched(cuda):
+    """nrc_autotune_many returns a split that fits on the SMs with at least one
+    CTA per job, leaves the caches' training state as it was (the training
+    candidates run on scratch copies), and the batched launches run with it."""
+    import torch
+
+    from vknrc_gb300 import Cache, nrc, synthetic as S
+
+    qn = [256 * 256, 4097, 1280 * 720]
+    tn = [4096, 16384, 30000]
+    caches = [Cache(seed=700 + j, train_batch_size=tn[j]) for j in range(3)]
+    try:
+        qs = [dev(_queries(710 + j, n)) for j, n in enumerate(qn)]
+        qc = [count(n) for n in qn]
+        outs = [torch.empty((n, 3), dtype=torch.float32, device="cuda") for n in qn]
+        recs = [[dev(S.train_records(S.rng_for(720 + j, b), n, sigma=0.5)) for b in range(4)] for j, n in enumerate(tn)]
+        tc = [[count(n) for _ in range(4)] for n in tn]
+        qjobs = [nrc.query_job(c, q, k, o) for c, q, k, o in zip(caches, qs, qc, outs)]
+        tjobs = [nrc.train_job(c, r, t) for c, r, t in zip(caches, recs, tc)]
+        before = [c.get_optimizer() for c in caches]
+        w_before = [c.get_weights(1) for c in caches]
+        gq, gt, qms, tms = nrc.autotune_many(qjobs, tjobs)
+        sms = torch.cuda.get_device_properties(0).multi_processor_count
+        assert len(gq) == 3 and len(gt) == 3 and min(gq) >= 1 and min(gt) >= 1
+        assert sum(gq) <= sms and sum(gt) <= sms
+        assert qms > 0 and tms > 0
+        for c, (st, ent), w in zip(caches, before, w_before):
+            st2, ent2 = c.get_optimizer()
+            assert st2 == st
+            np.testing.assert_array_equal(ent2, ent)
+            np.testing.assert_array_equal(c.get_weights(1), w)
+        nrc.infer_many(qjobs, ctas=gq)
+        nrc.train_many(tjobs, ctas=gt)
+        torch.cuda.synchronize()
+        assert all(c.get_optimizer()[0][0] == 4 for c in caches)
+        assert all(c.error() == 0 for c in caches)
+    finally:
+        for c in caches:
+            c.close()

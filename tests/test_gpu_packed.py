@@ -1,12 +1,12 @@
 """The query and the frame on the reference's record formats: packed eval
 records (nrc_eval_record, 20 B) and packed train records
-(nrc_packed_train_record, 40 B) over a scene, unpacked inside the query kernel
-(UnpackNRCInput, shader/src/NRCRecord.glsl:97-125, as nrc_inference.comp:33-36
-does) and by one unpack launch before the training.
+(nrc_packed_train_record, 40 B) over a scene, unpacked (UnpackNRCInput,
+shader/src/NRCRecord.glsl:97-125, as nrc_inference.comp:33-36 does) into the
+context's workspaces by the unpack kernel, then queried and trained.
 
 Each packed call is checked bit for bit against the same work done in two
 steps on the GPU (nrc_unpack_eval / nrc_unpack_train, then the unpacked-record
-call: the kernels run the same unpack and encode arithmetic), and against the
+call), and against the
 oracle: oracle_unpack + the oracle's forward within the query tolerance, and
 the destination epilogue (oracle_scatter) bit for bit on the GPU's own
 predictions."""

@@ -38,8 +38,12 @@ struct nrc_context {
   __half* use_next = nullptr;   // the overlapped frame's training writes use_weights here first
   nrc_frame_plan plan = {0u, 0u};  // the overlapped frame's split, once tuned
   bool plan_tuned = false;         // nrc_autotune_frame has set `plan` (which may be sequential)
-  // packed-record frames: the unpacked train records of the frame's batches
-  // (NRC_TRAIN_BATCH_COUNT x train_ws_cap), allocated by the first such call
+  // packed-record calls: the unpacked eval records and their destination words
+  // (eval_ws_cap each), and the unpacked train records of a frame's batches
+  // (NRC_TRAIN_BATCH_COUNT x train_ws_cap), allocated by the first call that needs them
+  nrc_input* eval_ws = nullptr;
+  uint32_t* eval_dst_ws = nullptr;
+  uint32_t eval_ws_cap = 0;
   nrc_train_record* train_ws = nullptr;
   uint32_t train_ws_cap = 0;
 };
@@ -297,6 +301,7 @@ int nrc_destroy(nrc_context* c) {
   cudaDeviceSynchronize();
   cudaFree(c->block);
   if (c->train_ws != nullptr) cudaFree(c->train_ws);
+  if (c->eval_ws != nullptr) cudaFree(c->eval_ws);
   if (dev >= 0 && dev != c->device) cudaSetDevice(dev);
   delete c;
   return NRC_OK;
@@ -539,28 +544,16 @@ static int scene_check_impl(const nrc_scene* sc) {
 
 namespace {
 
-// What a frame's query reads: unpacked records (nrc_input), or the reference's
-// packed eval records over a scene (unpacked inside the query kernel).
-struct FrameQuery {
-  const nrc_input* in = nullptr;
-  const nrc_eval_record* packed = nullptr;
-  const nrc_scene* scene = nullptr;
-};
-
-cudaError_t launch_frame_query(nrc_context* c, const FrameQuery& fq, const uint32_t* d_count, uint32_t capacity,
+cudaError_t launch_frame_query(nrc_context* c, const nrc_input* in, const uint32_t* d_count, uint32_t capacity,
                                const nrc::QueryOut& q, bool overlapped, const nrc::FrameJoin& join, cudaStream_t st) {
-  const uint32_t grid = nrc::infer_grid(capacity, c->num_sms);
-  if (fq.packed != nullptr)
-    return nrc::launch_infer_packed(fq.packed, *fq.scene, d_count, capacity, &c->map_use16, q, c->err,
-                                    overlapped ? c->tiles : nullptr, join, grid, st, c->bf16);
   if (overlapped)
-    return nrc::launch_infer_frame(fq.in, d_count, capacity, &c->map_use16, q, c->err, c->tiles, join, grid, st,
-                                   c->bf16);
-  return nrc::launch_infer(fq.in, false, d_count, capacity, &c->map_use16, q, c->err, c->num_sms, st, c->bf16);
+    return nrc::launch_infer_frame(in, d_count, capacity, &c->map_use16, q, c->err, c->tiles, join,
+                                   nrc::infer_grid(capacity, c->num_sms), st, c->bf16);
+  return nrc::launch_infer(in, false, d_count, capacity, &c->map_use16, q, c->err, c->num_sms, st, c->bf16);
 }
 
-// The body of nrc_frame_overlapped for either form of query input.
-int frame_overlapped(nrc_context* c, const FrameQuery& fq, const uint32_t* d_eval_count, uint32_t eval_capacity,
+// The body of nrc_frame_overlapped.
+int frame_overlapped(nrc_context* c, const nrc_input* eval_in, const uint32_t* d_eval_count, uint32_t eval_capacity,
                      float* out, const nrc_train_record* const* train_rec, uint32_t* const* train_counts,
                      uint32_t train_capacity, const nrc_frame_plan* plan_in, void* query_event, void* stream) {
   int s = check_ctx(c);
@@ -571,9 +564,8 @@ int frame_overlapped(nrc_context* c, const FrameQuery& fq, const uint32_t* d_eva
     if (train_rec[b] != nullptr && !aligned16(train_rec[b])) return NRC_ERROR_MISALIGNED;
   }
   if (eval_capacity > 0) {
-    const void* in = fq.packed != nullptr ? static_cast<const void*>(fq.packed) : static_cast<const void*>(fq.in);
-    if (in == nullptr || d_eval_count == nullptr || out == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
-    if (!aligned16(in) || (reinterpret_cast<uintptr_t>(out) & 3u)) return NRC_ERROR_MISALIGNED;
+    if (eval_in == nullptr || d_eval_count == nullptr || out == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+    if (!aligned16(eval_in) || (reinterpret_cast<uintptr_t>(out) & 3u)) return NRC_ERROR_MISALIGNED;
   }
   nrc_frame_plan plan = plan_in ? *plan_in : c->plan;
   if (plan_in == nullptr && !c->plan_tuned) {
@@ -595,7 +587,7 @@ int frame_overlapped(nrc_context* c, const FrameQuery& fq, const uint32_t* d_eva
   if (sequential) {
     // the query with the current rendering weights, then the training, which writes them
     if (eval_capacity > 0) {
-      e = launch_frame_query(c, fq, d_eval_count, eval_capacity, q, false, nrc::FrameJoin{}, st);
+      e = launch_frame_query(c, eval_in, d_eval_count, eval_capacity, q, false, nrc::FrameJoin{}, st);
       if (e != cudaSuccess) return from_cuda(e);
     }
     if (query_event != nullptr && (e = cudaEventRecord(static_cast<cudaEvent_t>(query_event), st)) != cudaSuccess)
@@ -624,12 +616,46 @@ int frame_overlapped(nrc_context* c, const FrameQuery& fq, const uint32_t* d_eva
   e = nrc::launch_train(p, &c->map_w16, static_cast<int>(plan.train_ctas), st);
   if (e != cudaSuccess) return from_cuda(e);
   if (eval_capacity > 0) {
-    e = launch_frame_query(c, fq, d_eval_count, eval_capacity, q, true, join, st);
+    e = launch_frame_query(c, eval_in, d_eval_count, eval_capacity, q, true, join, st);
     if (e != cudaSuccess) return from_cuda(e);
   }
   if (query_event != nullptr && (e = cudaEventRecord(static_cast<cudaEvent_t>(query_event), st)) != cudaSuccess)
     return from_cuda(e);
   return fp8_refresh(c, 0, st);
+}
+
+// Grows the context's unpacked-eval-record workspace to `capacity` records
+// (an allocation: not inside a stream capture).
+int ensure_eval_ws(nrc_context* c, uint32_t capacity) {
+  if (capacity <= c->eval_ws_cap) return NRC_OK;
+  cudaError_t e = cudaSuccess;
+  if (c->eval_ws != nullptr) {
+    if ((e = cudaDeviceSynchronize()) != cudaSuccess) return from_cuda(e);
+    cudaFree(c->eval_ws);
+    c->eval_ws = nullptr;
+    c->eval_dst_ws = nullptr;
+    c->eval_ws_cap = 0;
+  }
+  const size_t in_bytes = up256(size_t(capacity) * sizeof(nrc_input));
+  void* p = nullptr;
+  e = cudaMalloc(&p, in_bytes + size_t(capacity) * sizeof(uint32_t));
+  if (e != cudaSuccess) return e == cudaErrorMemoryAllocation ? NRC_ERROR_OUT_OF_MEMORY : from_cuda(e);
+  c->eval_ws = static_cast<nrc_input*>(p);
+  c->eval_dst_ws = reinterpret_cast<uint32_t*>(static_cast<uint8_t*>(p) + in_bytes);
+  c->eval_ws_cap = capacity;
+  return NRC_OK;
+}
+
+// Unpacks min(*d_count, capacity) packed eval records (and, with dst, their
+// destination words) into the context's workspace.
+int unpack_eval_ws(nrc_context* c, const nrc_scene* scene, const nrc_eval_record* rec, const uint32_t* d_count,
+                   uint32_t capacity, bool dst, cudaStream_t st) {
+  if (rec == nullptr || d_count == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  if (reinterpret_cast<uintptr_t>(rec) & 3u) return NRC_ERROR_MISALIGNED;
+  int s = ensure_eval_ws(c, capacity);
+  if (s != NRC_OK) return s;
+  return from_cuda(nrc::launch_unpack(*scene, false, rec, d_count, capacity, c->eval_ws,
+                                      dst ? c->eval_dst_ws : nullptr, c->num_sms, st));
 }
 
 // Grows the context's unpacked-train-record workspace to `capacity` records
@@ -678,9 +704,7 @@ extern "C" {
 int nrc_frame_overlapped(nrc_context* c, const nrc_input* eval_in, const uint32_t* d_eval_count, uint32_t eval_capacity,
                          float* out, const nrc_train_record* const* train_rec, uint32_t* const* train_counts,
                          uint32_t train_capacity, const nrc_frame_plan* plan_in, void* query_event, void* stream) {
-  FrameQuery fq;
-  fq.in = eval_in;
-  return frame_overlapped(c, fq, d_eval_count, eval_capacity, out, train_rec, train_counts, train_capacity, plan_in,
+  return frame_overlapped(c, eval_in, d_eval_count, eval_capacity, out, train_rec, train_counts, train_capacity, plan_in,
                           query_event, stream);
 }
 
@@ -691,14 +715,15 @@ int nrc_infer_packed(nrc_context* c, const nrc_scene* scene, const nrc_eval_reco
   if ((s = scene_check_impl(scene)) != NRC_OK) return s;
   if (weight_set != NRC_WEIGHTS_USE && weight_set != NRC_WEIGHTS_TRAIN) return NRC_ERROR_INVALID_ARGUMENT;
   if (capacity == 0) return NRC_OK;
-  if (rec == nullptr || d_count == nullptr || out == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
-  if (!aligned16(rec) || (reinterpret_cast<uintptr_t>(out) & 3u)) return NRC_ERROR_MISALIGNED;
+  if (out == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  if (reinterpret_cast<uintptr_t>(out) & 3u) return NRC_ERROR_MISALIGNED;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if ((s = unpack_eval_ws(c, scene, rec, d_count, capacity, false, st)) != NRC_OK) return s;
   nrc::QueryOut q = {};
   q.out = out;
   q.clamp = 1;
-  return from_cuda(nrc::launch_infer_packed(rec, *scene, d_count, capacity, weight_map_of(c, weight_set), q, c->err,
-                                            nullptr, nrc::FrameJoin{}, nrc::infer_grid(capacity, c->num_sms),
-                                            static_cast<cudaStream_t>(stream), c->bf16));
+  return from_cuda(nrc::launch_infer(c->eval_ws, false, d_count, capacity, weight_map_of(c, weight_set), q, c->err,
+                                     c->num_sms, st, c->bf16));
 }
 
 int nrc_infer_scatter_packed(nrc_context* c, const nrc_scene* scene, const nrc_eval_record* rec,
@@ -714,14 +739,14 @@ int nrc_infer_scatter_packed(nrc_context* c, const nrc_scene* scene, const nrc_e
   if ((s = scatter_out(reinterpret_cast<const nrc_scatter_targets*>(targets), &q)) != NRC_OK) return s;
   q.train_stride = sizeof(nrc_packed_train_record) / 4;
   if (capacity == 0) return NRC_OK;
-  if (rec == nullptr || d_count == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
-  if (!aligned16(rec) || (reinterpret_cast<uintptr_t>(out) & 3u)) return NRC_ERROR_MISALIGNED;
+  if (reinterpret_cast<uintptr_t>(out) & 3u) return NRC_ERROR_MISALIGNED;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if ((s = unpack_eval_ws(c, scene, rec, d_count, capacity, true, st)) != NRC_OK) return s;
   q.out = out;
   q.clamp = 1;
-  q.scatter = 1;
-  return from_cuda(nrc::launch_infer_packed(rec, *scene, d_count, capacity, weight_map_of(c, weight_set), q, c->err,
-                                            nullptr, nrc::FrameJoin{}, nrc::infer_grid(capacity, c->num_sms),
-                                            static_cast<cudaStream_t>(stream), c->bf16));
+  q.dst = c->eval_dst_ws;
+  return from_cuda(nrc::launch_infer(c->eval_ws, false, d_count, capacity, weight_map_of(c, weight_set), q, c->err,
+                                     c->num_sms, st, c->bf16));
 }
 
 int nrc_frame_scatter_packed(nrc_context* c, const nrc_scene* scene, const nrc_eval_record* eval_rec,
@@ -759,10 +784,11 @@ int nrc_frame_packed(nrc_context* c, const nrc_scene* scene, const nrc_eval_reco
   if ((s = unpack_train_ws(c, scene, train_rec, train_counts, train_capacity, ws, static_cast<cudaStream_t>(stream))) !=
       NRC_OK)
     return s;
-  FrameQuery fq;
-  fq.packed = eval_rec;
-  fq.scene = scene;
-  return frame_overlapped(c, fq, d_eval_count, eval_capacity, out, ws, train_counts, train_capacity, nullptr, nullptr,
+  if (eval_capacity > 0 &&
+      (s = unpack_eval_ws(c, scene, eval_rec, d_eval_count, eval_capacity, false, static_cast<cudaStream_t>(stream))) !=
+          NRC_OK)
+    return s;
+  return frame_overlapped(c, c->eval_ws, d_eval_count, eval_capacity, out, ws, train_counts, train_capacity, nullptr, nullptr,
                           stream);
 }
 
@@ -1087,6 +1113,148 @@ int nrc_train_many(const nrc_train_job* jobs, uint32_t n, const uint32_t* ctas, 
       if ((s = fp8_refresh(kept[j].ctx, 0, static_cast<cudaStream_t>(stream))) != NRC_OK) return s;
   }
   return NRC_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Candidate CTA splits of one batched launch: the proportional default first,
+// then for every count k of tiles per CTA (per pass of the query's slots, per
+// step of the training) the split that gives each job just enough CTAs to take
+// its tiles in k rounds, when those fit on the SMs. A launch lasts as long as
+// its busiest group, so a job gains nothing from CTAs beyond those that cut its
+// rounds; the largest k that fits wastes the fewest.
+std::vector<std::vector<uint32_t>> split_candidates(const std::vector<uint64_t>& tiles, uint32_t per_round,
+                                                    uint32_t group_cap, uint32_t sms,
+                                                    const std::vector<uint32_t>& proportional) {
+  std::vector<std::vector<uint32_t>> cand = {proportional};
+  uint64_t most = 1;
+  for (uint64_t t : tiles) most = std::max(most, t);
+  for (uint64_t k = 1; k <= (most + per_round - 1) / per_round; ++k) {
+    std::vector<uint32_t> g(tiles.size());
+    uint64_t sum = 0;
+    bool ok = true;
+    for (size_t j = 0; j < tiles.size(); ++j) {
+      const uint64_t want = std::max<uint64_t>(1, (tiles[j] + k * per_round - 1) / (k * per_round));
+      if (want > group_cap) ok = false;
+      g[j] = static_cast<uint32_t>(std::min<uint64_t>(want, group_cap));
+      sum += g[j];
+    }
+    if (!ok || sum > sms) continue;
+    if (std::find(cand.begin(), cand.end(), g) == cand.end()) cand.push_back(g);
+    if (cand.size() >= 12) break;
+  }
+  return cand;
+}
+
+// Mean duration in ms of `reps` launches of fn on `st`, after two untimed ones.
+template <typename F>
+int time_launches(F fn, cudaStream_t st, cudaEvent_t a, cudaEvent_t b, int reps, float* ms) {
+  int s = NRC_OK;
+  for (int k = 0; k < 2 && s == NRC_OK; ++k) s = fn();
+  if (s != NRC_OK) return s;
+  cudaEventRecord(a, st);
+  for (int k = 0; k < reps && s == NRC_OK; ++k) s = fn();
+  cudaEventRecord(b, st);
+  if (s != NRC_OK) return s;
+  const cudaError_t e = cudaEventSynchronize(b);
+  if (e != cudaSuccess) return from_cuda(e);
+  cudaEventElapsedTime(ms, a, b);
+  *ms /= static_cast<float>(reps);
+  return NRC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int nrc_autotune_many(const nrc_query_job* qjobs, uint32_t nq, const nrc_train_job* tjobs, uint32_t nt,
+                      uint32_t* q_ctas, uint32_t* t_ctas, float* q_ms, float* t_ms) {
+  if (nq > kMaxJobsPerLaunch || nt > kMaxJobsPerLaunch || (nq > 0 && q_ctas == nullptr) ||
+      (nt > 0 && t_ctas == nullptr))
+    return NRC_ERROR_INVALID_ARGUMENT;
+  int s = check_jobs(qjobs, nq, query_job_check);
+  if (s == NRC_OK) s = check_jobs(tjobs, nt, train_job_check);
+  if (s != NRC_OK) return s;
+  for (uint32_t j = 0; j < nq; ++j)
+    if (qjobs[j].capacity == 0 || qjobs[j].ctx->bf16 != qjobs[0].ctx->bf16) return NRC_ERROR_INVALID_ARGUMENT;
+  for (uint32_t j = 0; j < nt; ++j)
+    if (tjobs[j].ctx->bf16 != tjobs[0].ctx->bf16) return NRC_ERROR_INVALID_ARGUMENT;
+  const uint32_t sms = static_cast<uint32_t>(device_sms());
+  cudaStream_t st = nullptr;
+  cudaEvent_t a = nullptr, b = nullptr;
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreate(&a);
+  if (e == cudaSuccess) e = cudaEventCreate(&b);
+  if (e != cudaSuccess) s = from_cuda(e);
+  // queries: timed on the jobs themselves (a query writes only its outputs)
+  if (s == NRC_OK && nq > 0) {
+    std::vector<uint64_t> tiles(nq);
+    for (uint32_t j = 0; j < nq; ++j) tiles[j] = (uint64_t(qjobs[j].capacity) + nrc::kTile - 1) / nrc::kTile;
+    std::vector<uint32_t> prop(nq);
+    plan_query(qjobs, nq, static_cast<int>(sms), prop.data());
+    const auto cand = split_candidates(tiles, static_cast<uint32_t>(nrc::infer_tiles_per_cta()), sms, sms, prop);
+    float best = 1e30f;
+    for (const auto& g : cand) {
+      float ms = 0.0f;
+      s = time_launches([&] { return nrc_infer_many(qjobs, nq, g.data(), st); }, st, a, b, 5, &ms);
+      if (s != NRC_OK) break;
+      if (ms < best) {
+        best = ms;
+        std::copy(g.begin(), g.end(), q_ctas);
+      }
+    }
+    if (s == NRC_OK && q_ms) *q_ms = best;
+  }
+  // training: timed on scratch copies of the caches (tuning trains them, not the caller's)
+  std::vector<nrc_context*> scratch;
+  if (s == NRC_OK && nt > 0) {
+    std::vector<nrc_train_job> sj(tjobs, tjobs + nt);
+    for (uint32_t j = 0; j < nt && s == NRC_OK; ++j) {
+      nrc_context* t = nullptr;
+      if ((s = nrc_create(&tjobs[j].ctx->cfg, &t)) != NRC_OK) break;
+      scratch.push_back(t);
+      const nrc_context* c = tjobs[j].ctx;
+      e = cudaMemcpy(t->w16, c->w16, kParams * 2, cudaMemcpyDeviceToDevice);
+      if (e == cudaSuccess) e = cudaMemcpy(t->use16, c->use16, kParams * 2, cudaMemcpyDeviceToDevice);
+      if (e == cudaSuccess)
+        e = cudaMemcpy(t->entries, c->entries, kParams * sizeof(nrc_optimizer_entry), cudaMemcpyDeviceToDevice);
+      if (e == cudaSuccess) e = cudaMemcpy(t->state, c->state, sizeof(nrc_optimizer_state), cudaMemcpyDeviceToDevice);
+      if (e != cudaSuccess) s = from_cuda(e);
+      sj[j].ctx = t;
+    }
+    if (s == NRC_OK) {
+      std::vector<uint64_t> tiles(nt);
+      for (uint32_t j = 0; j < nt; ++j) {
+        const uint32_t rec = std::min(sj[j].capacity, sj[j].ctx->cfg.train_batch_size);
+        tiles[j] = std::max<uint64_t>(1, (uint64_t(rec) + nrc::kTile - 1) / nrc::kTile);
+      }
+      std::vector<uint32_t> prop(nt);
+      plan_train(sj.data(), nt, static_cast<int>(sms), prop.data());
+      const auto cand = split_candidates(tiles, 1u, nrc::train_grid(nrc::TrainParams{}, static_cast<int>(sms)), sms,
+                                         prop);
+      float best = 1e30f;
+      for (const auto& g : cand) {
+        float ms = 0.0f;
+        s = time_launches([&] { return nrc_train_many(sj.data(), nt, g.data(), st); }, st, a, b, 5, &ms);
+        if (s != NRC_OK) break;
+        if (ms < best) {
+          best = ms;
+          std::copy(g.begin(), g.end(), t_ctas);
+        }
+      }
+      if (s == NRC_OK && t_ms) *t_ms = best;
+    }
+    for (nrc_context* t : scratch)
+      if (s == NRC_OK && nrc_get_error(t) != NRC_OK) s = NRC_ERROR_DEVICE_TIMEOUT;
+  }
+  for (nrc_context* t : scratch) nrc_destroy(t);
+  if (a) cudaEventDestroy(a);
+  if (b) cudaEventDestroy(b);
+  if (st) cudaStreamDestroy(st);
+  return s;
 }
 
 // ------------------------------------------------------------------- fp8 --

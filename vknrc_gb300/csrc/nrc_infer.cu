@@ -19,7 +19,6 @@
 
 #include "nrc_common.cuh"
 #include "nrc_kernels.h"
-#include "nrc_unpack.cuh"
 
 namespace nrc {
 
@@ -32,17 +31,11 @@ constexpr uint32_t kRecBytes = sizeof(nrc_input);      // 56
 constexpr uint32_t kRecTileBytes = kTile * kRecBytes;  // 7168
 constexpr uint32_t kRecSmemOff = kWeightSmemBytes;     // 43008, 1024-aligned
 constexpr uint32_t kBarOff = kRecSmemOff + kSlots * 2 * kRecTileBytes;
-constexpr uint32_t kLutOff = kBarOff + 512;            // packed records: the sRGB decode table
-constexpr uint32_t kSmemBytes = kLutOff + 1024 + 1024;  // + alignment slack
-constexpr uint32_t kPackedBytes = sizeof(nrc_eval_record);  // 20: packed eval records (scene unpack fused)
-static_assert(kPackedBytes == 20, "nrc_eval_record layout");
+constexpr uint32_t kSmemBytes = kBarOff + 512 + 1024;  // + alignment slack
 static_assert(kWeightSmemBytes % 1024 == 0, "weight tiles 1024-aligned");
 static_assert(kSlots * kSlotCols <= 512, "TMEM columns");
 static_assert(kJoinChunks * 16 == kParams * 2, "join copy covers the weights");
 
-// sRGB -> linear table of the packed-record query (srgb_lut(), written by
-// configure_infer_kernels on each device).
-__device__ float g_srgb[256];
 
 struct SlotBars {
   uint64_t rec_full[2];   // bulk copy of a record tile landed (tx bytes)
@@ -128,11 +121,7 @@ __device__ __forceinline__ void scatter_query(const QueryOut& Q, uint32_t dst, f
 // layer's fp32 sum multiplied by its scale constant before the ReLU and the
 // conversion; the weights keep the 128-byte rows of the 16-bit layout, K bytes
 // 64..127 being zero and never read).
-// kPacked: the input is the reference's 20-byte eval records (nrc_eval_record)
-// over the job's scene: each thread unpacks its record (UnpackNRCInput, the
-// gathers of nrc_unpack.cuh) before the encode, and the destination word is the
-// record's own.
-template <bool kEncoded, bool kScatter, int N, int kFmt, bool kPacked = false>
+template <bool kEncoded, bool kScatter, int N, int kFmt>
 __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_constant__ InferLaunch<N> L) {
 
   constexpr bool kBF16 = kFmt == 1, kF8 = kFmt == 2;
@@ -153,11 +142,7 @@ __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_co
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(w_full + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  constexpr uint32_t rec_bytes = kPacked ? kPackedBytes : kRecBytes;
-  float* lut = reinterpret_cast<float*>(smem + kLutOff);
-  if (kPacked) {
-    for (uint32_t i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = g_srgb[i];
-  }
+  constexpr uint32_t rec_bytes = kRecBytes;
 
   // dynamic tiles (single-cache record queries with a tile counter)
   const bool dyn = N == 1 && !kEncoded && J.tiles != nullptr;
@@ -245,15 +230,7 @@ __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_co
       }
       const uint32_t bulk = (rows_valid * rec_bytes) & ~15u;
       float r[kInFloats];
-      if (kPacked && row < static_cast<int>(rows_valid)) {
-        // the 20-byte record (4-byte aligned in the stage and in memory)
-        const uint32_t* src = (static_cast<uint32_t>(row + 1) * rec_bytes <= bulk)
-                                  ? reinterpret_cast<const uint32_t*>(stage + row * rec_bytes)
-                                  : reinterpret_cast<const uint32_t*>(rec_in + grow * rec_bytes);
-        const nrc_packed_input pin{src[1], src[2], src[3], src[4]};
-        qdst = src[0];
-        unpack_one(J.scene, pin, lut, r);
-      } else if (row < static_cast<int>(rows_valid)) {
+      if (row < static_cast<int>(rows_valid)) {
         const float2* src = (static_cast<uint32_t>(row + 1) * rec_bytes <= bulk)
                                 ? reinterpret_cast<const float2*>(stage + row * rec_bytes)
                                 : reinterpret_cast<const float2*>(rec_in + grow * rec_bytes);
@@ -327,7 +304,7 @@ __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_co
         }
       }
       // load the destination word while the output layer's MMAs run
-      if (kScatter && !kPacked && l == 5 && row < static_cast<int>(rows_valid)) qdst = __ldg(Q.dst + grow);
+      if (kScatter && l == 5 && row < static_cast<int>(rows_valid)) qdst = __ldg(Q.dst + grow);
       const float cl = kF8 ? J.fp8->c[l] : 1.0f;  // the layer's scale constant (FP8 query)
       ok = ok && warp_all(mbar_wait(&B.d_ready, ph_d, kWaitLimitNs));
       if (!ok) break;
@@ -412,7 +389,7 @@ __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_co
   }
 }
 
-template <bool kEncoded, bool kScatter, int N, int kFmt, bool kPacked = false>
+template <bool kEncoded, bool kScatter, int N, int kFmt>
 cudaError_t launch(const InferLaunch<N>& L, uint32_t grid, cudaStream_t stream) {
   cudaLaunchAttribute attr;
   attr.id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -424,18 +401,18 @@ cudaError_t launch(const InferLaunch<N>& L, uint32_t grid, cudaStream_t stream) 
   cfg.stream = stream;
   cfg.attrs = &attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, infer_kernel<kEncoded, kScatter, N, kFmt, kPacked>, L);
+  return cudaLaunchKernelEx(&cfg, infer_kernel<kEncoded, kScatter, N, kFmt>, L);
 }
 
 // The shared-memory limit, and the largest carveout: the query and the trainer
 // (206 KB) then run in the same SM configuration, so an SM passing from one to
 // the other between kernels needs no reconfiguration.
-template <bool kEncoded, bool kScatter, int N, int kFmt, bool kPacked = false>
+template <bool kEncoded, bool kScatter, int N, int kFmt>
 cudaError_t set_smem() {
-  cudaError_t e = cudaFuncSetAttribute(infer_kernel<kEncoded, kScatter, N, kFmt, kPacked>,
+  cudaError_t e = cudaFuncSetAttribute(infer_kernel<kEncoded, kScatter, N, kFmt>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(infer_kernel<kEncoded, kScatter, N, kFmt, kPacked>,
+  return cudaFuncSetAttribute(infer_kernel<kEncoded, kScatter, N, kFmt>,
                               cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
 }
 
@@ -450,12 +427,6 @@ cudaError_t configure_infer_kernels() {
   if (e == cudaSuccess) e = set_smem<false, true, 1, 1>();
   if (e == cudaSuccess) e = set_smem<false, false, kMaxInferJobs, 1>();
   if (e == cudaSuccess) e = set_smem<false, false, 1, 2>();
-  if (e == cudaSuccess) e = set_smem<false, false, 1, 0, true>();
-  if (e == cudaSuccess) e = set_smem<false, true, 1, 0, true>();
-  if (e == cudaSuccess) e = set_smem<false, false, 1, 1, true>();
-  if (e == cudaSuccess) e = set_smem<false, true, 1, 1, true>();
-  // the sRGB decode table the packed-record query stages into shared memory
-  if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_srgb, srgb_lut().v, sizeof(g_srgb));
   return e;
 }
 
@@ -512,32 +483,6 @@ cudaError_t launch_infer_frame(const nrc_input* input, const uint32_t* d_count, 
   if (q.dst != nullptr)
     return bf16 ? launch<false, true, 1, 1>(L, grid, stream) : launch<false, true, 1, 0>(L, grid, stream);
   return bf16 ? launch<false, false, 1, 1>(L, grid, stream) : launch<false, false, 1, 0>(L, grid, stream);
-}
-
-cudaError_t launch_infer_packed(const nrc_eval_record* input, const nrc_scene& scene, const uint32_t* d_count,
-                                uint32_t capacity, const CUtensorMap* wmap, const QueryOut& q, uint32_t* err,
-                                uint32_t* tiles, const FrameJoin& join, uint32_t grid, cudaStream_t stream, bool bf16) {
-  if (grid == 0) return cudaSuccess;
-  InferLaunch<1> L;
-  L.job[0] = InferJob{};
-  L.job[0].wmap = *wmap;
-  L.job[0].input = input;
-  L.job[0].d_count = d_count;
-  L.job[0].capacity = capacity;
-  L.job[0].err = err;
-  L.job[0].q = q;
-  L.job[0].scene = scene;
-  if (tiles != nullptr) {  // the overlapped frame's query: dynamic tiles, started beside the training
-    L.job[0].tiles = tiles;
-    L.job[0].no_wait = 1;
-    L.job[0].join = join;
-  }
-  L.group_start[0] = 0;
-  L.group_start[1] = grid;
-  L.njobs = 1;
-  if (q.scatter)
-    return bf16 ? launch<false, true, 1, 1, true>(L, grid, stream) : launch<false, true, 1, 0, true>(L, grid, stream);
-  return bf16 ? launch<false, false, 1, 1, true>(L, grid, stream) : launch<false, false, 1, 0, true>(L, grid, stream);
 }
 
 cudaError_t launch_infer_fp8(const nrc_input* input, const uint32_t* d_count, uint32_t capacity,

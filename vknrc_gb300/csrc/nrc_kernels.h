@@ -41,7 +41,6 @@ int infer_tiles_per_cta();
 struct QueryOut {
   float* out;
   int clamp;
-  int scatter;  // packed-record queries: run the destination epilogue on the records' own words
   const uint32_t* dst;
   float* bias_factor_r;
   const float* factor_gb;
@@ -112,7 +111,6 @@ struct InferJob {
   // reads nothing that training writes).
   uint32_t no_wait;
   FrameJoin join;  // dynamic tiles only: joined by the last CTA out
-  nrc_scene scene;  // packed eval records: the scene their records unpack from
 };
 
 // Kernel parameters of a query launch over up to N caches; CTAs
@@ -147,14 +145,6 @@ uint32_t infer_grid(uint32_t capacity, int num_sms);
 cudaError_t launch_infer_frame(const nrc_input* input, const uint32_t* d_count, uint32_t capacity,
                                const CUtensorMap* wmap, const QueryOut& q, uint32_t* err, uint32_t* tiles,
                                const FrameJoin& join, uint32_t grid, cudaStream_t stream, bool bf16);
-// The query over the reference's packed eval records (nrc_eval_record, 20 B)
-// of `scene`: each record is unpacked in the kernel (UnpackNRCInput) before the
-// encode. q.scatter: the destination epilogue with each record's own
-// destination word (q.dst unused); tiles non-null: the overlapped frame's
-// dynamic-tile form of launch_infer_frame.
-cudaError_t launch_infer_packed(const nrc_eval_record* input, const nrc_scene& scene, const uint32_t* d_count,
-                                uint32_t capacity, const CUtensorMap* wmap, const QueryOut& q, uint32_t* err,
-                                uint32_t* tiles, const FrameJoin& join, uint32_t grid, cudaStream_t stream, bool bf16);
 // One launch answering njobs caches' record queries (dense rgb output, no
 // destination words), group_size[j] >= 1 CTAs for job j, sum <= SMs.
 cudaError_t launch_infer_many(const InferJob* jobs, int njobs, const uint32_t* group_size, cudaStream_t stream,

@@ -35,43 +35,64 @@ __device__ __forceinline__ void write_train(nrc_train_record* dst, const nrc_pac
   o[4] = make_float4(r[10], r[11], r[12], r[13]);
 }
 
-__global__ void __launch_bounds__(256) unpack_batches_kernel(const __grid_constant__ UnpackParams P,
+__global__ void __launch_bounds__(256, 4) unpack_batches_kernel(const __grid_constant__ UnpackParams P,
                                                               const __grid_constant__ UnpackBatches U,
                                                               uint32_t capacity) {
   __shared__ float lut[256];
   lut[threadIdx.x] = P.lut.v[threadIdx.x];
   __syncthreads();
-  const uint32_t b = blockIdx.y;
-  const uint32_t n = min(*U.count[b], capacity);
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const nrc_packed_train_record rec = U.in[b][i];
-    float r[kInFloats];
-    unpack_one(P.scene, rec.input, lut, r);
-    write_train(U.out[b] + i, rec, r);
+  const uint32_t bt = blockIdx.y;
+  const uint32_t n = min(*U.count[bt], capacity);
+  const size_t stride = static_cast<size_t>(gridDim.x) * blockDim.x;
+  for (size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += 2 * stride) {
+    const size_t j = i + stride;
+    const bool two = j < n;
+    const nrc_packed_train_record a = U.in[bt][i], b = U.in[bt][two ? j : i];
+    float ra[kInFloats], rb[kInFloats];
+    unpack_one(P.scene, a.input, lut, ra);
+    unpack_one(P.scene, b.input, lut, rb);
+    write_train(U.out[bt] + i, a, ra);
+    if (two) write_train(U.out[bt] + j, b, rb);
   }
 }
 
+// One thread per two records (i and i + stride of the grid-stride loop), so
+// that the dependent gathers of two records are in flight at once.
 template <bool kTrain>
-__global__ void __launch_bounds__(256) unpack_kernel(const __grid_constant__ UnpackParams P, const void* __restrict__ in,
+__global__ void __launch_bounds__(256, 4) unpack_kernel(const __grid_constant__ UnpackParams P, const void* __restrict__ in,
                                                       const uint32_t* __restrict__ d_count, uint32_t capacity,
                                                       void* __restrict__ out, uint32_t* __restrict__ out_dst) {
   __shared__ float lut[256];
   lut[threadIdx.x] = P.lut.v[threadIdx.x];
   __syncthreads();
   const uint32_t n = min(*d_count, capacity);
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    float r[kInFloats];
+  const size_t stride = static_cast<size_t>(gridDim.x) * blockDim.x;
+  for (size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += 2 * stride) {
+    const size_t j = i + stride;
+    const bool two = j < n;
+    float ra[kInFloats], rb[kInFloats];
     if (kTrain) {
-      const nrc_packed_train_record rec = static_cast<const nrc_packed_train_record*>(in)[i];
-      unpack_one(P.scene, rec.input, lut, r);
-      write_train(static_cast<nrc_train_record*>(out) + i, rec, r);
+      const nrc_packed_train_record* rec = static_cast<const nrc_packed_train_record*>(in);
+      const nrc_packed_train_record a = rec[i], b = rec[two ? j : i];
+      unpack_one(P.scene, a.input, lut, ra);
+      unpack_one(P.scene, b.input, lut, rb);
+      write_train(static_cast<nrc_train_record*>(out) + i, a, ra);
+      if (two) write_train(static_cast<nrc_train_record*>(out) + j, b, rb);
     } else {
-      const nrc_eval_record rec = static_cast<const nrc_eval_record*>(in)[i];
-      unpack_one(P.scene, rec.input, lut, r);
-      float2* o = reinterpret_cast<float2*>(static_cast<nrc_input*>(out) + i);
+      const nrc_eval_record* rec = static_cast<const nrc_eval_record*>(in);
+      const nrc_eval_record a = rec[i], b = rec[two ? j : i];
+      unpack_one(P.scene, a.input, lut, ra);
+      unpack_one(P.scene, b.input, lut, rb);
+      float2* oa = reinterpret_cast<float2*>(static_cast<nrc_input*>(out) + i);
 #pragma unroll
-      for (int k = 0; k < 7; ++k) o[k] = make_float2(r[2 * k], r[2 * k + 1]);
-      if (out_dst != nullptr) out_dst[i] = rec.dst;
+      for (int k = 0; k < 7; ++k) oa[k] = make_float2(ra[2 * k], ra[2 * k + 1]);
+      if (out_dst != nullptr) out_dst[i] = a.dst;
+      if (two) {
+        float2* ob = reinterpret_cast<float2*>(static_cast<nrc_input*>(out) + j);
+#pragma unroll
+        for (int k = 0; k < 7; ++k) ob[k] = make_float2(rb[2 * k], rb[2 * k + 1]);
+        if (out_dst != nullptr) out_dst[j] = b.dst;
+      }
     }
   }
 }
@@ -95,7 +116,7 @@ const SrgbLut& srgb_lut() {
 cudaError_t launch_unpack(const nrc_scene& scene, bool train, const void* in, const uint32_t* d_count,
                           uint32_t capacity, void* out, uint32_t* out_dst, int num_sms, cudaStream_t stream) {
   const uint32_t want = (capacity + 255) / 256;
-  const uint32_t cap = static_cast<uint32_t>(num_sms) * 8;
+  const uint32_t cap = static_cast<uint32_t>(num_sms) * 4;  // the resident blocks (4 per SM)
   const uint32_t grid = want < cap ? want : cap;
   if (grid == 0) return cudaSuccess;
   UnpackParams p;

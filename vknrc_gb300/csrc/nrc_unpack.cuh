@@ -84,23 +84,38 @@ __device__ inline F3 sample_texture(const nrc_texture& t, float tu, float tv, co
 
 // UnpackNRCInput into 14 floats (nrc_input); false (and zeros) for a record
 // whose indices fall outside the scene. `lut` is the sRGB decode table
-// (srgb_lut()) in shared memory.
+// (srgb_lut()) in shared memory. The loads take no early exit: an out-of-range
+// index is replaced by 0 (in range once the scene's counts are non-zero, checked
+// first) and the record's outputs are zeroed at the end, so a thread can have
+// the loads of several records in flight.
 __device__ __forceinline__ bool unpack_one(const nrc_scene& S, const nrc_packed_input& in, const float* lut, float (&r)[kInFloats]) {
+  if (S.primitive_count == 0 || S.instance_count == 0 || S.vertex_count == 0 || S.texcoord_count == 0 ||
+      S.material_count == 0) {
 #pragma unroll
-  for (int k = 0; k < kInFloats; ++k) r[k] = 0.0f;
+    for (int k = 0; k < kInFloats; ++k) r[k] = 0.0f;
+    return false;
+  }
   const uint32_t prim = in.primitive_id, inst = in.flip_bit_instance_id & 0x7FFFFFFFu;
   const bool flip = (in.flip_bit_instance_id >> 31) != 0;
-  if (prim >= S.primitive_count || inst >= S.instance_count) return false;
+  bool ok = prim < S.primitive_count && inst < S.instance_count;
+  const uint32_t pr = ok ? prim : 0u, in_id = ok ? inst : 0u;
   uint32_t vi[3], ti[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    vi[k] = S.vertex_indices[size_t(prim) * 3 + k];
-    ti[k] = S.texcoord_indices[size_t(prim) * 3 + k];
-    if (vi[k] >= S.vertex_count || ti[k] >= S.texcoord_count) return false;
+    vi[k] = S.vertex_indices[size_t(pr) * 3 + k];
+    ti[k] = S.texcoord_indices[size_t(pr) * 3 + k];
   }
-  const uint32_t mid = S.material_ids[prim];
-  if (mid >= S.material_count) return false;
-  const float* T = S.transforms + size_t(inst) * 12;
+  uint32_t mid = S.material_ids[pr];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) ok = ok && vi[k] < S.vertex_count && ti[k] < S.texcoord_count;
+  ok = ok && mid < S.material_count;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    vi[k] = ok ? vi[k] : 0u;
+    ti[k] = ok ? ti[k] : 0u;
+  }
+  mid = ok ? mid : 0u;
+  const float* T = S.transforms + size_t(in_id) * 12;
   F3 v[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
@@ -139,12 +154,16 @@ __device__ __forceinline__ bool unpack_one(const nrc_scene& S, const nrc_packed_
 #pragma unroll
   for (int c = 0; c < 2; ++c) {
     F3 col{konst[c][0], konst[c][1], konst[c][2]};
-    if (ids[c] != 0xFFFFFFFFu && ids[c] < S.texture_count) col = sample_texture(S.textures[ids[c]], tu, tv, lut);
+    if (ok && ids[c] != 0xFFFFFFFFu && ids[c] < S.texture_count) col = sample_texture(S.textures[ids[c]], tu, tv, lut);
     r[8 + 3 * c] = col.x;
     r[9 + 3 * c] = col.y;
     r[10 + 3 * c] = col.z;
   }
-  return true;
+  if (!ok) {
+#pragma unroll
+    for (int k = 0; k < kInFloats; ++k) r[k] = 0.0f;
+  }
+  return ok;
 }
 
 // sRGB -> linear of the 256 byte values, in double, rounded once (host).

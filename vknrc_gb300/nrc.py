@@ -37,7 +37,7 @@ EXPORTS = [
     "nrc_unpack_eval", "nrc_unpack_train", "nrc_infer_fp8", "nrc_fp8_refresh", "nrc_get_fp8",
     "nrc_frame_overlapped", "nrc_autotune_frame", "nrc_bvh_build", "nrc_bvh_destroy", "nrc_bvh_info",
     "nrc_path_trace", "nrc_optimize", "nrc_loss_gradient", "nrc_infer_packed", "nrc_infer_scatter_packed",
-    "nrc_frame_packed", "nrc_frame_scatter_packed",
+    "nrc_frame_packed", "nrc_frame_scatter_packed", "nrc_autotune_many",
 ]
 
 
@@ -203,6 +203,8 @@ def lib(build_if_missing: bool = True) -> ctypes.CDLL:
     L.nrc_train_many.argtypes = [ctypes.POINTER(TrainJob), u32, vp, vp]
     L.nrc_plan_query_ctas.argtypes = [ctypes.POINTER(QueryJob), u32, vp]
     L.nrc_plan_train_ctas.argtypes = [ctypes.POINTER(TrainJob), u32, vp]
+    L.nrc_autotune_many.argtypes = [ctypes.POINTER(QueryJob), u32, ctypes.POINTER(TrainJob), u32, vp, vp,
+                                    ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]
     L.nrc_server_create.argtypes = [ctypes.POINTER(ServerConfig), ctypes.POINTER(vp)]
     L.nrc_server_destroy.argtypes = [vp]
     L.nrc_server_open_session.argtypes = [vp, ctypes.POINTER(SessionDesc), ctypes.POINTER(u32)]
@@ -535,6 +537,20 @@ def train_many(jobs: Sequence[TrainJob], ctas=None, stream=None) -> None:
     arr = (TrainJob * len(jobs))(*jobs)
     c = _ctas(ctas)
     check(lib().nrc_train_many(arr, len(jobs), c[0] if c else None, _stream(stream)), "nrc_train_many")
+
+
+def autotune_many(qjobs: Sequence[QueryJob], tjobs: Sequence[TrainJob]):
+    """nrc_autotune_many: (query CTA split, training CTA split, query ms, training ms)."""
+    nq, nt = len(qjobs), len(tjobs)
+    qa = (QueryJob * max(1, nq))(*qjobs)
+    ta = (TrainJob * max(1, nt))(*tjobs)
+    qc = np.zeros(max(1, nq), np.uint32)
+    tc = np.zeros(max(1, nt), np.uint32)
+    qms, tms = ctypes.c_float(0.0), ctypes.c_float(0.0)
+    check(lib().nrc_autotune_many(qa, nq, ta, nt, qc.ctypes.data_as(ctypes.c_void_p),
+                                  tc.ctypes.data_as(ctypes.c_void_p), ctypes.byref(qms), ctypes.byref(tms)),
+          "nrc_autotune_many")
+    return [int(x) for x in qc[:nq]], [int(x) for x in tc[:nt]], qms.value, tms.value
 
 
 def plan_query_ctas(jobs: Sequence[QueryJob]) -> list:
