@@ -649,7 +649,7 @@ def render_leg(frames=20, width=1920, height=1080):
     from vknrc_gb300 import Cache, nrc, synthetic as S
 
     sc = S.terrain_scene(S.rng_for(3), n=512)
-    ds = nrc.DeviceScene(sc)
+    ds = nrc.DeviceScene(sc).prepare()  # gather tables, built once per scene (nrc_scene_prepare)
     t0 = time.perf_counter()
     bvh = nrc.Bvh(ds)
     build_s = time.perf_counter() - t0
@@ -830,8 +830,8 @@ PACKED_TRAIN_BYTES = 40  # nrc_packed_train_record
 def packed_leg(cache, stream, E, world, frames=4):
     """The frame on the reference's record formats (nrc_frame_packed): packed
     eval records (20 B) and packed train records (40 B) of a 522,254-triangle
-    scene resident on the device, unpacked inside the query kernel and by one
-    launch before the training. Times (1) the frame with its inputs resident
+    scene resident on the device with its gather tables (nrc_scene_prepare),
+    unpacked by one launch each into the context's workspaces. Times (1) the frame with its inputs resident
     (`frames` distinct record frames rotated, 176 MB: cold in L2), (2) the
     packed-record query alone, and (3) end to end through the C ABI with host
     buffers: each frame's packed records copied from pinned memory and its rgb
@@ -842,7 +842,8 @@ def packed_leg(cache, stream, E, world, frames=4):
     from vknrc_gb300 import nrc, synthetic as S
 
     sc = S.terrain_scene(S.rng_for(3), n=512)
-    ds = nrc.DeviceScene(sc)
+    ds = nrc.DeviceScene(sc).prepare()  # gather tables, built once per scene (nrc_scene_prepare)
+    plain = ds.unprepared()  # the same buffers without the tables
     ev_h = [torch.from_numpy(S.eval_records(S.rng_for(4000, f), sc, Q).view(np.int32)) for f in range(frames)]
     tr_h = [[torch.from_numpy(S.packed_train_records(S.rng_for(5000, f, b), sc, R).view(np.int32)) for b in range(B)]
             for f in range(frames)]
@@ -879,6 +880,21 @@ def packed_leg(cache, stream, E, world, frames=4):
         ev_q[k + 1].record(stream)
     torch.cuda.synchronize()
     q_ms = [ev_q[k].elapsed_time(ev_q[k + 1]) for k in range(QA)]
+    # the eval unpack pass alone, over the tables and over the scene buffers
+    unpack_us = {}
+    ws_in = torch.empty((Q, 14), dtype=torch.float32, device="cuda")
+    for name, scene in (("tables", ds), ("buffers", plain)):
+        for k in range(3):
+            nrc.unpack_eval(scene, ev_d[k % frames], eval_cnt, ws_in, capacity=Q, stream=stream)
+        ev_u = [torch.cuda.Event(enable_timing=True) for _ in range(QA + 1)]
+        torch.cuda.synchronize()
+        ev_u[0].record(stream)
+        for k in range(QA):
+            nrc.unpack_eval(scene, ev_d[k % frames], eval_cnt, ws_in, capacity=Q, stream=stream)
+            ev_u[k + 1].record(stream)
+        torch.cuda.synchronize()
+        unpack_us[name] = statistics.median(ev_u[k].elapsed_time(ev_u[k + 1]) for k in range(QA)) * 1e3
+    del ws_in
 
     # end to end with host buffers
     h_ev = [t.pin_memory() for t in ev_h[:2]]
@@ -938,11 +954,15 @@ def packed_leg(cache, stream, E, world, frames=4):
         "frame_packed": {"ms_per_frame": frame_s * 1e3, "queries_per_s": Q / frame_s,
                          "train_records_per_s": B * R / frame_s, "frames": K,
                          "what": "nrc_frame_packed with resident inputs (4 record frames rotated, L2-cold): "
-                                 "train-record unpack launch, then the training and the packed-record query "
-                                 "overlapped"},
+                                 "train-record and eval-record unpack launches into the context's workspaces, "
+                                 "then the overlapped frame on the unpacked records"},
         "query_packed_alone_ms": {"mean": statistics.mean(q_ms), "p50": statistics.median(q_ms), "launches": QA,
-                                  "what": "nrc_infer_packed of 2,073,600 packed records (scene unpack fused into the "
-                                          "query kernel) on all SMs, timed alone"},
+                                  "what": "nrc_infer_packed of 2,073,600 packed records (the unpack pass, then the "
+                                          "query) on all SMs, timed alone"},
+        "unpack_eval_us": {"tables": unpack_us["tables"], "buffers": unpack_us["buffers"], "launches": QA,
+                           "what": "nrc_unpack_eval of 2,073,600 packed records (uniformly random primitives, "
+                                   "L2-cold record frames), p50 per launch: over the scene's gather tables "
+                                   "(nrc_scene_prepare, as the frame and e2e use them) and over the scene buffers"},
     }
 
 

@@ -503,6 +503,8 @@ typedef struct nrc_texture {
  * texcoord or material index is out of range unpacks to zeros, and a texture
  * id at or beyond texture_count reads as the constant colour (the reference
  * trusts its buffers). */
+typedef struct nrc_scene_tables nrc_scene_tables;
+
 typedef struct nrc_scene {
   const float* vertices;            /* Vertex {x, y, z}, vertex_count */
   const uint32_t* vertex_indices;   /* 3 per primitive */
@@ -513,7 +515,27 @@ typedef struct nrc_scene {
   const float* transforms;          /* per instance: mat3x4, 3 columns of 4 floats (p' = vec4(p, 1) * T) */
   const nrc_texture* textures;      /* device array, texture_count entries */
   uint32_t vertex_count, texcoord_count, material_count, primitive_count, instance_count, texture_count;
+  /* Optional (NULL: the unpack reads the buffers above): gather tables of this
+   * scene made by nrc_scene_prepare. With them the unpack reads one 64-byte row
+   * per record's primitive and one per material instead of the index, vertex,
+   * texcoord, material and texture-table gathers; results are the same bit for
+   * bit. The transforms are still read from `transforms`. */
+  const nrc_scene_tables* tables;
 } nrc_scene;
+
+/* Builds the unpack's gather tables of `scene` on `stream` and returns them in
+ * *out (no counterpart in the reference, whose shaders gather from the scene
+ * buffers of Scene.glsl:30-48 directly). Per primitive one 64-byte row: its
+ * three object-space vertices and texcoords and its material id (marked invalid
+ * when one of its indices is out of range); per material one 64-byte row: the
+ * constant colours, roughness and the two texture descriptors inline. The tables
+ * are a snapshot of the buffers at that point of the stream: after changing the
+ * scene's buffers, prepare again. Allocates device memory (64 bytes per primitive
+ * and per material), so call it outside stream capture. Set scene->tables to
+ * the result to use them; nrc_scene_tables_destroy frees them (after the work
+ * that reads them has finished). */
+NRC_API int nrc_scene_prepare(const nrc_scene* scene, void* stream, nrc_scene_tables** out);
+NRC_API int nrc_scene_tables_destroy(nrc_scene_tables* tables);
 
 /* PackedNRCInput, NRCEvalRecord, NRCTrainRecord (NRCRecord.glsl:6-38). */
 typedef struct nrc_packed_input {

@@ -186,3 +186,28 @@ def test_frame_scatter_packed_equals_unpacked_frame(cuda):
         np.testing.assert_array_equal(a.get_weights(0), b.get_weights(0))
         np.testing.assert_array_equal(a.get_optimizer()[1], b.get_optimizer()[1])
         assert a.error() == 0 and b.error() == 0
+
+
+def test_frame_packed_scene_tables_equal_buffers(cuda):
+    """The packed frame over a prepared scene (nrc_scene_prepare) equals the
+    same frame over the scene buffers: outputs, weights and optimizer entries."""
+    import torch
+
+    from vknrc_gb300 import Cache, nrc
+
+    sc, plain = _scene(63)
+    prepared = nrc.DeviceScene(sc).prepare()
+    q, r = 30000, 2500
+    ev, tr = _packed_frame_inputs(sc, plain, q, r, 64)
+    kw = dict(seed=65, learning_rate=1e-3, beta2=0.99)
+    res = []
+    for ds in (plain, prepared):
+        with Cache(**kw) as c:
+            out = torch.empty((q, 3), dtype=torch.float32, device="cuda")
+            cnt = [count(r) for _ in range(4)]
+            for _ in range(2):
+                c.frame_packed(ds, dev(ev.view(np.int32)), count(q), out, [dev(t.view(np.int32)) for t in tr], cnt)
+            res.append((host(out), c.get_weights(0), c.get_optimizer()[1]))
+            assert c.error() == 0
+    for a, b in zip(res[0], res[1]):
+        np.testing.assert_array_equal(a, b)

@@ -139,3 +139,74 @@ def test_gpu_unpack_train_then_query_with_destinations(cuda, oracle):
     ref_in = oracle.unpack(sc, ev, 1)  # the whole path from the oracle's unpacked records
     pred_o = np.maximum(oracle.forward_f32(w16, oracle.encode(ref_in)), 0)
     assert np.max(np.abs(pred_o - pred)) <= 1e-2 * max(1.0, float(np.abs(pred_o).max()))
+
+
+def _corrupted_scene(seed):
+    """A synthetic scene whose index buffers hold out-of-range entries (vertex,
+    texcoord and material indices) and whose texture table has an empty
+    texture, so every rejection of the unpack is met."""
+    from vknrc_gb300 import synthetic as S
+
+    rng = S.rng_for(seed)
+    sc = S.scene(rng, texture_sizes=((5, 3), (64, 32), (0, 0), (17, 9)))
+    p = sc["vertex_indices"].shape[0]
+    sel = rng.choice(p, 15, replace=False)
+    sc["vertex_indices"][sel[:5], 1] = sc["vertices"].shape[0] + 3
+    sc["texcoord_indices"][sel[5:10], 2] = sc["texcoords"].shape[0]
+    sc["material_ids"][sel[10:]] = sc["materials"].shape[0] + 1
+    ids = sc["materials"].view(np.uint32)
+    ids[0, 3], ids[1, 7] = 2, 2  # the empty texture, on one diffuse and one specular colour
+    return sc
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [1, 255, 256, 257, 20000])
+def test_gpu_unpack_tables_equal_buffers_and_oracle(cuda, oracle, n):
+    """nrc_scene_prepare's gather tables give the buffers' unpack bit for bit,
+    records and index buffers with out-of-range entries included."""
+    import torch
+
+    from vknrc_gb300 import nrc, synthetic as S
+
+    sc = _corrupted_scene(30)
+    ev = S.eval_records(S.rng_for(31, n), sc, n, bad_fraction=0.05)
+    tr = S.packed_train_records(S.rng_for(32, n), sc, n)
+    plain = nrc.DeviceScene(sc)
+    prepared = nrc.DeviceScene(sc).prepare()
+    outs = []
+    for ds in (plain, prepared):
+        o = torch.full((n + 3, 14), -1.0, dtype=torch.float32, device="cuda")
+        d = torch.zeros(n + 3, dtype=torch.int32, device="cuda")
+        nrc.unpack_eval(ds, dev(ev.view(np.int32)), count(n), o, d)
+        t = torch.full((n + 3, 20), -1.0, dtype=torch.float32, device="cuda")
+        nrc.unpack_train(ds, dev(tr.view(np.int32)), count(n), t)
+        outs.append((host(o), host(d), host(t)))
+    for a, b in zip(outs[0], outs[1]):
+        np.testing.assert_array_equal(a, b)
+    got = outs[1][0]
+    assert np.all(got[n:] == -1.0)
+    ref = oracle.unpack(sc, ev, 1)
+    exact = [0, 1, 2, 3, 4, 7, 8, 9, 10, 11, 12, 13]
+    assert np.array_equal(got[:n, exact], ref[:, exact])
+    assert np.max(np.abs(got[:n, 5:7] - ref[:, 5:7])) <= 4e-7
+    ref_t = oracle.unpack(sc, tr, 6)
+    assert np.array_equal(outs[1][2][:n, [6 + k for k in exact]], ref_t[:, exact])
+    if n >= 20000:  # the rejections were met
+        assert (np.all(ref == 0, axis=1)).sum() > 0.05 * n
+
+
+@pytest.mark.gpu
+def test_gpu_unpack_tables_of_another_scene_rejected(cuda):
+    import torch
+
+    from vknrc_gb300 import nrc, synthetic as S
+
+    a = nrc.DeviceScene(S.scene(S.rng_for(33))).prepare()
+    b = nrc.DeviceScene(S.scene(S.rng_for(34), primitives=150))
+    b.s.tables = a.tables.value  # tables whose counts do not match this scene
+    ev = S.eval_records(S.rng_for(35), S.scene(S.rng_for(34), primitives=150), 10)
+    out = torch.zeros((10, 14), dtype=torch.float32, device="cuda")
+    with pytest.raises(nrc.NRCError) as e:
+        nrc.unpack_eval(b, dev(ev.view(np.int32)), count(10), out)
+    assert e.value.status == 1  # NRC_ERROR_INVALID_ARGUMENT
+    b.s.tables = None

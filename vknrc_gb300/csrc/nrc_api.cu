@@ -529,18 +529,33 @@ int nrc_frame(nrc_context* c, const nrc_input* eval_in, const uint32_t* d_eval_c
 
 }  // extern "C"
 
+// Gather tables of one scene (nrc_scene_prepare): primitive_count 64-byte
+// primitive rows, then material_count material rows, in one allocation.
+struct nrc_scene_tables {
+  void* prims;
+  void* mats;
+  uint32_t primitive_count, material_count;
+};
+
 static int scene_check_impl(const nrc_scene* sc) {
   if (sc == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  if (sc->tables != nullptr &&
+      (sc->tables->primitive_count != sc->primitive_count || sc->tables->material_count != sc->material_count))
+    return NRC_ERROR_INVALID_ARGUMENT;  // tables of another scene
   const bool geometry = sc->primitive_count > 0 && sc->instance_count > 0;
   if (geometry && (sc->vertices == nullptr || sc->vertex_indices == nullptr || sc->texcoords == nullptr ||
                    sc->texcoord_indices == nullptr || sc->materials == nullptr || sc->material_ids == nullptr ||
                    sc->transforms == nullptr))
     return NRC_ERROR_INVALID_ARGUMENT;
   if (sc->texture_count > 0 && sc->textures == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
-  if ((reinterpret_cast<uintptr_t>(sc->materials) & 15u) || (reinterpret_cast<uintptr_t>(sc->textures) & 7u))
+  if ((reinterpret_cast<uintptr_t>(sc->materials) & 15u) || (reinterpret_cast<uintptr_t>(sc->textures) & 7u) ||
+      (reinterpret_cast<uintptr_t>(sc->transforms) & 15u) || (reinterpret_cast<uintptr_t>(sc->texcoords) & 7u))
     return NRC_ERROR_MISALIGNED;
   return NRC_OK;
 }
+
+static const void* prim_rows(const nrc_scene* sc) { return sc->tables != nullptr ? sc->tables->prims : nullptr; }
+static const void* mat_rows(const nrc_scene* sc) { return sc->tables != nullptr ? sc->tables->mats : nullptr; }
 
 namespace {
 
@@ -654,8 +669,8 @@ int unpack_eval_ws(nrc_context* c, const nrc_scene* scene, const nrc_eval_record
   if (reinterpret_cast<uintptr_t>(rec) & 3u) return NRC_ERROR_MISALIGNED;
   int s = ensure_eval_ws(c, capacity);
   if (s != NRC_OK) return s;
-  return from_cuda(nrc::launch_unpack(*scene, false, rec, d_count, capacity, c->eval_ws,
-                                      dst ? c->eval_dst_ws : nullptr, c->num_sms, st));
+  return from_cuda(nrc::launch_unpack(*scene, prim_rows(scene), mat_rows(scene), false, rec, d_count, capacity,
+                                      c->eval_ws, dst ? c->eval_dst_ws : nullptr, c->num_sms, st));
 }
 
 // Grows the context's unpacked-train-record workspace to `capacity` records
@@ -693,8 +708,8 @@ int unpack_train_ws(nrc_context* c, const nrc_scene* scene, const nrc_packed_tra
     ws[b] = out[b];
   }
   if (capacity == 0) return NRC_OK;
-  return from_cuda(nrc::launch_unpack_train_batches(*scene, rec, counts, capacity, out, NRC_TRAIN_BATCH_COUNT,
-                                                    c->num_sms, st));
+  return from_cuda(nrc::launch_unpack_train_batches(*scene, prim_rows(scene), mat_rows(scene), rec, counts, capacity,
+                                                    out, NRC_TRAIN_BATCH_COUNT, c->num_sms, st));
 }
 
 }  // namespace
@@ -1309,7 +1324,8 @@ int nrc_unpack_eval(const nrc_scene* sc, const nrc_eval_record* rec, const uint3
   if ((reinterpret_cast<uintptr_t>(rec) & 3u) || (reinterpret_cast<uintptr_t>(out) & 7u) ||
       (reinterpret_cast<uintptr_t>(out_dst) & 3u))
     return NRC_ERROR_MISALIGNED;
-  return from_cuda(nrc::launch_unpack(*sc, false, rec, d_count, capacity, out, out_dst, device_sms(),
+  return from_cuda(nrc::launch_unpack(*sc, prim_rows(sc), mat_rows(sc), false, rec, d_count, capacity, out, out_dst,
+                                      device_sms(),
                                       static_cast<cudaStream_t>(stream)));
 }
 
@@ -1320,8 +1336,44 @@ int nrc_unpack_train(const nrc_scene* sc, const nrc_packed_train_record* rec, co
   if (capacity == 0) return NRC_OK;
   if (rec == nullptr || d_count == nullptr || out == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
   if ((reinterpret_cast<uintptr_t>(rec) & 3u) || !aligned16(out)) return NRC_ERROR_MISALIGNED;
-  return from_cuda(nrc::launch_unpack(*sc, true, rec, d_count, capacity, out, nullptr, device_sms(),
+  return from_cuda(nrc::launch_unpack(*sc, prim_rows(sc), mat_rows(sc), true, rec, d_count, capacity, out, nullptr,
+                                      device_sms(),
                                       static_cast<cudaStream_t>(stream)));
+}
+
+int nrc_scene_prepare(const nrc_scene* sc, void* stream, nrc_scene_tables** out) {
+  if (out == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  *out = nullptr;
+  if (sc == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  nrc_scene plain = *sc;
+  plain.tables = nullptr;  // the tables are made from the buffers
+  int s = scene_check_impl(&plain);
+  if (s != NRC_OK) return s;
+  const size_t prim_bytes = size_t(sc->primitive_count) * 64, mat_bytes = size_t(sc->material_count) * 64;
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, prim_bytes + mat_bytes + 64);
+  if (e != cudaSuccess) return e == cudaErrorMemoryAllocation ? NRC_ERROR_OUT_OF_MEMORY : from_cuda(e);
+  auto* t = new (std::nothrow) nrc_scene_tables{p, static_cast<uint8_t*>(p) + prim_bytes, sc->primitive_count,
+                                                sc->material_count};
+  if (t == nullptr) {
+    cudaFree(p);
+    return NRC_ERROR_OUT_OF_MEMORY;
+  }
+  e = nrc::launch_scene_prepare(plain, t->prims, t->mats, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) {
+    cudaFree(p);
+    delete t;
+    return from_cuda(e);
+  }
+  *out = t;
+  return NRC_OK;
+}
+
+int nrc_scene_tables_destroy(nrc_scene_tables* t) {
+  if (t == nullptr) return NRC_OK;
+  const cudaError_t e = cudaFree(t->prims);
+  delete t;
+  return from_cuda(e);
 }
 
 // ---------------------------------------------------------------- screen --

@@ -230,13 +230,19 @@ cudaError_t launch_encode(const nrc_input* in, const uint32_t* d_count, uint32_t
                           int num_sms, cudaStream_t stream);
 cudaError_t launch_sph_encode(const float* dirs, const uint32_t* d_count, uint32_t capacity, float* out,
                               int num_sms, cudaStream_t stream);
+// The gather tables of nrc_scene_prepare: 64-byte rows, primitive_count of
+// them at prim_rows and material_count at mat_rows (16-byte aligned).
+cudaError_t launch_scene_prepare(const nrc_scene& scene, void* prim_rows, void* mat_rows, cudaStream_t stream);
 // The train records of nbatches batches (min(*counts[b], capacity) each) in one
-// launch, into unpacked arrays out[b].
-cudaError_t launch_unpack_train_batches(const nrc_scene& scene, const nrc_packed_train_record* const* in,
-                                       uint32_t* const* counts, uint32_t capacity, nrc_train_record* const* out,
-                                       int nbatches, int num_sms, cudaStream_t stream);
-cudaError_t launch_unpack(const nrc_scene& scene, bool train, const void* in, const uint32_t* d_count,
-                          uint32_t capacity, void* out, uint32_t* out_dst, int num_sms, cudaStream_t stream);
+// launch, into unpacked arrays out[b]. prim_rows / mat_rows: the scene's
+// prepared tables, or both null to gather from the scene buffers.
+cudaError_t launch_unpack_train_batches(const nrc_scene& scene, const void* prim_rows, const void* mat_rows,
+                                       const nrc_packed_train_record* const* in, uint32_t* const* counts,
+                                       uint32_t capacity, nrc_train_record* const* out, int nbatches, int num_sms,
+                                       cudaStream_t stream);
+cudaError_t launch_unpack(const nrc_scene& scene, const void* prim_rows, const void* mat_rows, bool train,
+                          const void* in, const uint32_t* d_count, uint32_t capacity, void* out, uint32_t* out_dst,
+                          int num_sms, cudaStream_t stream);
 cudaError_t launch_screen(const float* color, float* accum, uint32_t width, uint32_t height, int acc_on,
                           uint32_t acc_count, uint8_t* out8, float* outf, int num_sms, cudaStream_t stream);
 cudaError_t launch_fill_f32(float* p, float v, size_t n, cudaStream_t stream);

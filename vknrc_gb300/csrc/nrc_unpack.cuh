@@ -27,6 +27,8 @@
 
 namespace nrc {
 
+static_assert(sizeof(nrc_material) == 64 && alignof(nrc_material) <= 16, "std430 Material: four 16-byte words");
+
 struct SrgbLut {
   float v[256];
 };
@@ -37,14 +39,13 @@ struct F3 {
 
 __device__ __forceinline__ float unorm16(uint32_t u) { return __fdiv_rn(static_cast<float>(u & 0xFFFFu), 65535.0f); }
 
-// vec4(p, 1) * mat3x4: component i = dot((p, 1), column i).
-__device__ __forceinline__ F3 xform(const float* __restrict__ T, F3 p) {
+// vec4(p, 1) * mat3x4: component i = dot((p, 1), column i); the three columns
+// come in as 16-byte vectors (the transforms are 16-byte aligned).
+__device__ __forceinline__ F3 xform(const float4 (&c)[3], F3 p) {
   float o[3];
 #pragma unroll
-  for (int i = 0; i < 3; ++i) {
-    const float* c = T + 4 * i;
-    o[i] = __fadd_rn(__fmaf_rn(p.z, c[2], __fmaf_rn(p.y, c[1], __fmul_rn(p.x, c[0]))), c[3]);
-  }
+  for (int i = 0; i < 3; ++i)
+    o[i] = __fadd_rn(__fmaf_rn(p.z, c[i].z, __fmaf_rn(p.y, c[i].y, __fmul_rn(p.x, c[i].x))), c[i].w);
   return F3{o[0], o[1], o[2]};
 }
 
@@ -63,9 +64,10 @@ __device__ __forceinline__ uint32_t wrap(float f, uint32_t n) {
   return static_cast<uint32_t>(r);
 }
 
-__device__ inline F3 sample_texture(const nrc_texture& t, float tu, float tv, const float* lut) {
-  const uint32_t w = t.width, h = t.height;
-  if (w == 0 || h == 0 || t.texels == nullptr) return F3{0.f, 0.f, 0.f};
+// `lut` is the sRGB decode table (srgb_lut()) in shared memory (stage_lut).
+__device__ inline F3 sample_texels(const uchar4* __restrict__ px, uint32_t w, uint32_t h, float tu, float tv,
+                                   const float* lut) {
+  if (w == 0 || h == 0 || px == nullptr) return F3{0.f, 0.f, 0.f};
   float u = __fmaf_rn(tu, static_cast<float>(w), -0.5f), v = __fmaf_rn(tv, static_cast<float>(h), -0.5f);
   if (!(fabsf(u) < 8388608.0f)) u = 0.0f;  // NaN or beyond fp32's integer range: texel 0's neighbourhood
   if (!(fabsf(v) < 8388608.0f)) v = 0.0f;
@@ -73,7 +75,6 @@ __device__ inline F3 sample_texture(const nrc_texture& t, float tu, float tv, co
   const float a = __fsub_rn(u, fu), b = __fsub_rn(v, fv);
   const uint32_t i0 = wrap(fu, w), j0 = wrap(fv, h);
   const uint32_t i1 = i0 + 1 == w ? 0 : i0 + 1, j1 = j0 + 1 == h ? 0 : j0 + 1;
-  const uchar4* px = reinterpret_cast<const uchar4*>(t.texels);
   const uchar4 t00 = px[size_t(j0) * w + i0], t10 = px[size_t(j0) * w + i1];
   const uchar4 t01 = px[size_t(j1) * w + i0], t11 = px[size_t(j1) * w + i1];
   auto ch = [&](unsigned char c00, unsigned char c10, unsigned char c01, unsigned char c11) {
@@ -82,23 +83,40 @@ __device__ inline F3 sample_texture(const nrc_texture& t, float tu, float tv, co
   return F3{ch(t00.x, t10.x, t01.x, t11.x), ch(t00.y, t10.y, t01.y, t11.y), ch(t00.z, t10.z, t01.z, t11.z)};
 }
 
-// UnpackNRCInput into 14 floats (nrc_input); false (and zeros) for a record
-// whose indices fall outside the scene. `lut` is the sRGB decode table
-// (srgb_lut()) in shared memory. The loads take no early exit: an out-of-range
-// index is replaced by 0 (in range once the scene's counts are non-zero, checked
-// first) and the record's outputs are zeroed at the end, so a thread can have
-// the loads of several records in flight.
-__device__ __forceinline__ bool unpack_one(const nrc_scene& S, const nrc_packed_input& in, const float* lut, float (&r)[kInFloats]) {
-  if (S.primitive_count == 0 || S.instance_count == 0 || S.vertex_count == 0 || S.texcoord_count == 0 ||
-      S.material_count == 0) {
-#pragma unroll
-    for (int k = 0; k < kInFloats; ++k) r[k] = 0.0f;
-    return false;
-  }
-  const uint32_t prim = in.primitive_id, inst = in.flip_bit_instance_id & 0x7FFFFFFFu;
-  const bool flip = (in.flip_bit_instance_id >> 31) != 0;
-  bool ok = prim < S.primitive_count && inst < S.instance_count;
-  const uint32_t pr = ok ? prim : 0u, in_id = ok ? inst : 0u;
+// The gather tables of nrc_scene_prepare (nrc_scene_tables), as 16-byte words.
+// Primitive row (4 words): (v0.xyz, tc0.u), (v1.xyz, tc0.v), (v2.xyz, tc1.u),
+// (tc1.v, tc2.u, tc2.v, material id), the vertices in object space; the
+// material id is kInvalidRow when one of the primitive's indices is out of
+// range. Material row (4 words): (diffuse.rgb, roughness), (specular.rgb,
+// flags: bit 0 diffuse textured, bit 1 specular textured), then the diffuse and
+// the specular texture as (texels address low, high, width, height).
+struct SceneRows {
+  const uint4* prims;
+  const uint4* mats;
+};
+constexpr uint32_t kInvalidRow = 0xFFFFFFFFu;
+
+// What UnpackNRCInput reads for one record, gathered from either form of the scene.
+struct Gathered {
+  F3 p[3];         // object-space vertices
+  float2 tc[3];    // texcoords
+  uint4 col[2];    // diffuse / specular constant rgb in x..z
+  float roughness;
+  const uchar4* tex[2];  // texture of each colour (sampled when `textured`)
+  uint32_t tw[2], th[2];
+  bool textured[2];
+  bool ok;         // every index in range
+};
+
+__device__ __forceinline__ bool scene_empty(const nrc_scene& S) {
+  return S.primitive_count == 0 || S.instance_count == 0 || S.vertex_count == 0 || S.texcoord_count == 0 ||
+         S.material_count == 0;
+}
+
+// Gathers from the scene buffers (Scene.glsl:50-58: indices, then vertices,
+// texcoords and the material). An out-of-range index is replaced by 0 (in range
+// once the scene's counts are non-zero) and clears `ok`; no early exit.
+__device__ __forceinline__ void gather_buffers(const nrc_scene& S, uint32_t pr, bool ok, Gathered& g) {
   uint32_t vi[3], ti[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
@@ -115,13 +133,93 @@ __device__ __forceinline__ bool unpack_one(const nrc_scene& S, const nrc_packed_
     ti[k] = ok ? ti[k] : 0u;
   }
   mid = ok ? mid : 0u;
-  const float* T = S.transforms + size_t(in_id) * 12;
-  F3 v[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     const float* p = S.vertices + size_t(vi[k]) * 3;
-    v[k] = xform(T, F3{p[0], p[1], p[2]});
+    g.p[k] = F3{p[0], p[1], p[2]};
   }
+  const float2* tc2 = reinterpret_cast<const float2*>(S.texcoords);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) g.tc[k] = tc2[ti[k]];
+  // the material's words 0..7 (diffuse, its texture, specular, its texture) and
+  // 12..15 (metallic, roughness, ior) in three 16-byte loads (std430, 16-byte aligned)
+  const uint4* m4 = reinterpret_cast<const uint4*>(S.materials + mid);
+  const uint4 md = m4[0], ms = m4[1], mr = m4[3];
+  g.roughness = __uint_as_float(mr.y);
+  g.col[0] = md;
+  g.col[1] = ms;
+  const uint32_t ids[2] = {md.w, ms.w};
+#pragma unroll
+  for (int c = 0; c < 2; ++c) {
+    g.textured[c] = ok && ids[c] != 0xFFFFFFFFu && ids[c] < S.texture_count;
+    g.tex[c] = nullptr;
+    g.tw[c] = g.th[c] = 0;
+    if (g.textured[c]) {
+      const nrc_texture t = S.textures[ids[c]];
+      g.tex[c] = reinterpret_cast<const uchar4*>(t.texels);
+      g.tw[c] = t.width;
+      g.th[c] = t.height;
+    }
+  }
+  g.ok = ok;
+}
+
+// Gathers from the prepared rows: one primitive row, then one material row.
+__device__ __forceinline__ void gather_rows(const SceneRows& R, uint32_t pr, bool ok, Gathered& g) {
+  const uint4* row = R.prims + size_t(pr) * 4;
+  const uint4 q0 = row[0], q1 = row[1], q2 = row[2], q3 = row[3];
+  ok = ok && q3.w != kInvalidRow;
+  const uint32_t mid = ok ? q3.w : 0u;
+  g.p[0] = F3{__uint_as_float(q0.x), __uint_as_float(q0.y), __uint_as_float(q0.z)};
+  g.p[1] = F3{__uint_as_float(q1.x), __uint_as_float(q1.y), __uint_as_float(q1.z)};
+  g.p[2] = F3{__uint_as_float(q2.x), __uint_as_float(q2.y), __uint_as_float(q2.z)};
+  g.tc[0] = make_float2(__uint_as_float(q0.w), __uint_as_float(q1.w));
+  g.tc[1] = make_float2(__uint_as_float(q2.w), __uint_as_float(q3.x));
+  g.tc[2] = make_float2(__uint_as_float(q3.y), __uint_as_float(q3.z));
+  const uint4* m = R.mats + size_t(mid) * 4;
+  const uint4 m0 = m[0], m1 = m[1], m2 = m[2], m3 = m[3];
+  g.col[0] = m0;
+  g.col[1] = m1;
+  g.roughness = __uint_as_float(m0.w);
+  const uint4 t[2] = {m2, m3};
+#pragma unroll
+  for (int c = 0; c < 2; ++c) {
+    g.textured[c] = ok && ((m1.w >> c) & 1u);
+    g.tex[c] = reinterpret_cast<const uchar4*>((static_cast<uint64_t>(t[c].y) << 32) | t[c].x);
+    g.tw[c] = t[c].z;
+    g.th[c] = t[c].w;
+  }
+  g.ok = ok;
+}
+
+// UnpackNRCInput into 14 floats (nrc_input); false (and zeros) for a record
+// whose indices fall outside the scene. `lut` is the sRGB decode table in
+// shared memory (stage_lut). kRows: gather from the prepared tables `rows`, else from the
+// scene buffers. The loads take no early exit: an out-of-range index is
+// replaced by 0 and the record's outputs are zeroed at the end, so a thread can
+// have the loads of several records in flight.
+template <bool kRows>
+__device__ __forceinline__ bool unpack_one(const nrc_scene& S, const SceneRows& rows, const nrc_packed_input& in,
+                                           const float* lut, float (&r)[kInFloats]) {
+  if (scene_empty(S)) {
+#pragma unroll
+    for (int k = 0; k < kInFloats; ++k) r[k] = 0.0f;
+    return false;
+  }
+  const uint32_t prim = in.primitive_id, inst = in.flip_bit_instance_id & 0x7FFFFFFFu;
+  const bool flip = (in.flip_bit_instance_id >> 31) != 0;
+  const bool ok0 = prim < S.primitive_count && inst < S.instance_count;
+  const uint32_t pr = ok0 ? prim : 0u, in_id = ok0 ? inst : 0u;
+  Gathered g;
+  if constexpr (kRows)
+    gather_rows(rows, pr, ok0, g);
+  else
+    gather_buffers(S, pr, ok0, g);
+  const float4* T4 = reinterpret_cast<const float4*>(S.transforms + size_t(in_id) * 12);
+  const float4 T[3] = {T4[0], T4[1], T4[2]};
+  F3 v[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) v[k] = xform(T, g.p[k]);
   // normal = normalize(cross(v1 - v0, v2 - v0)), negated when flipped
   const F3 e1{__fsub_rn(v[1].x, v[0].x), __fsub_rn(v[1].y, v[0].y), __fsub_rn(v[1].z, v[0].z)};
   const F3 e2{__fsub_rn(v[2].x, v[0].x), __fsub_rn(v[2].y, v[0].y), __fsub_rn(v[2].z, v[0].z)};
@@ -142,31 +240,34 @@ __device__ __forceinline__ bool unpack_one(const nrc_scene& S, const nrc_packed_
   const float pi = 3.14159265358979323846f;
   r[5] = (n.x == 0.0f && n.y == 0.0f) ? 0.5f : __fadd_rn(0.5f, __fdiv_rn(atan2f(n.y, n.x), 2.0f * pi));
   r[6] = __fdiv_rn(acosf(fminf(fmaxf(n.z, -1.0f), 1.0f)), pi);
-  const nrc_material& m = S.materials[mid];
-  r[7] = m.roughness;
-  const float* tc[3];
-#pragma unroll
-  for (int k = 0; k < 3; ++k) tc[k] = S.texcoords + size_t(ti[k]) * 2;
-  const float tu = interp(tc[0][0], tc[1][0], tc[2][0], b0, b1, b2);
-  const float tv = interp(tc[0][1], tc[1][1], tc[2][1], b0, b1, b2);
-  const uint32_t ids[2] = {m.diffuse_texture_id, m.specular_texture_id};
-  const float* konst[2] = {m.diffuse, m.specular};
+  r[7] = g.roughness;
+  const float tu = interp(g.tc[0].x, g.tc[1].x, g.tc[2].x, b0, b1, b2);
+  const float tv = interp(g.tc[0].y, g.tc[1].y, g.tc[2].y, b0, b1, b2);
 #pragma unroll
   for (int c = 0; c < 2; ++c) {
-    F3 col{konst[c][0], konst[c][1], konst[c][2]};
-    if (ok && ids[c] != 0xFFFFFFFFu && ids[c] < S.texture_count) col = sample_texture(S.textures[ids[c]], tu, tv, lut);
+    F3 col{__uint_as_float(g.col[c].x), __uint_as_float(g.col[c].y), __uint_as_float(g.col[c].z)};
+    if (g.textured[c]) col = sample_texels(g.tex[c], g.tw[c], g.th[c], tu, tv, lut);
     r[8 + 3 * c] = col.x;
     r[9 + 3 * c] = col.y;
     r[10 + 3 * c] = col.z;
   }
-  if (!ok) {
+  if (!g.ok) {
 #pragma unroll
     for (int k = 0; k < kInFloats; ++k) r[k] = 0.0f;
   }
-  return ok;
+  return g.ok;
 }
 
 // sRGB -> linear of the 256 byte values, in double, rounded once (host).
 const SrgbLut& srgb_lut();
+
+// The table into shared memory (1 KB: a larger copy, one per bank to avoid
+// conflicts, measured slower, as it takes L1 capacity from the scene gathers).
+// Block-wide.
+__device__ __forceinline__ const float* stage_lut(float* lut, const SrgbLut& src) {
+  for (uint32_t i = threadIdx.x; i < 256u; i += blockDim.x) lut[i] = src.v[i];
+  __syncthreads();
+  return lut;
+}
 
 }  // namespace nrc

@@ -37,7 +37,8 @@ EXPORTS = [
     "nrc_unpack_eval", "nrc_unpack_train", "nrc_infer_fp8", "nrc_fp8_refresh", "nrc_get_fp8",
     "nrc_frame_overlapped", "nrc_autotune_frame", "nrc_bvh_build", "nrc_bvh_destroy", "nrc_bvh_info",
     "nrc_path_trace", "nrc_optimize", "nrc_loss_gradient", "nrc_infer_packed", "nrc_infer_scatter_packed",
-    "nrc_frame_packed", "nrc_frame_scatter_packed", "nrc_autotune_many",
+    "nrc_frame_packed", "nrc_frame_scatter_packed", "nrc_autotune_many", "nrc_scene_prepare",
+    "nrc_scene_tables_destroy",
 ]
 
 
@@ -150,7 +151,8 @@ class SceneStruct(ctypes.Structure):
                 ("material_ids", ctypes.c_void_p), ("transforms", ctypes.c_void_p), ("textures", ctypes.c_void_p),
                 ("vertex_count", ctypes.c_uint32), ("texcoord_count", ctypes.c_uint32),
                 ("material_count", ctypes.c_uint32), ("primitive_count", ctypes.c_uint32),
-                ("instance_count", ctypes.c_uint32), ("texture_count", ctypes.c_uint32)]
+                ("instance_count", ctypes.c_uint32), ("texture_count", ctypes.c_uint32),
+                ("tables", ctypes.c_void_p)]
 
 
 _lib: Optional[ctypes.CDLL] = None
@@ -228,6 +230,8 @@ def lib(build_if_missing: bool = True) -> ctypes.CDLL:
     L.nrc_path_trace.argtypes = [ctypes.POINTER(SceneStruct), vp, ctypes.POINTER(TraceParams),
                                  ctypes.POINTER(TraceTargets), vp]
     L.nrc_unpack_eval.argtypes = [ctypes.POINTER(SceneStruct), vp, vp, u32, vp, vp, vp]
+    L.nrc_scene_prepare.argtypes = [ctypes.POINTER(SceneStruct), vp, ctypes.POINTER(vp)]
+    L.nrc_scene_tables_destroy.argtypes = [vp]
     L.nrc_infer_packed.argtypes = [vp, ctypes.POINTER(SceneStruct), vp, vp, u32, vp, i32, vp]
     L.nrc_infer_scatter_packed.argtypes = [vp, ctypes.POINTER(SceneStruct), vp, vp, u32,
                                            ctypes.POINTER(ScatterTargets), vp, i32, vp]
@@ -703,7 +707,38 @@ class DeviceScene:
                              k["texcoord_indices"].data_ptr(), k["materials"].data_ptr(), k["material_ids"].data_ptr(),
                              k["transforms"].data_ptr(), self.table.data_ptr(), k["vertices"].shape[0],
                              k["texcoords"].shape[0], k["materials"].shape[0], k["vertex_indices"].shape[0],
-                             k["transforms"].shape[0], len(self.tex))
+                             k["transforms"].shape[0], len(self.tex), None)
+        self.tables = None
+
+    def prepare(self, stream=None) -> "DeviceScene":
+        """nrc_scene_prepare: build the gather tables and use them from now on."""
+        self.release()
+        h = ctypes.c_void_p()
+        check(lib().nrc_scene_prepare(ctypes.byref(self.s), _stream(stream), ctypes.byref(h)), "nrc_scene_prepare")
+        self.tables = h
+        self.s.tables = h.value
+        return self
+
+    def unprepared(self) -> "DeviceScene":
+        """A view of the same buffers without the tables (shares them; keep self alive)."""
+        v = DeviceScene.__new__(DeviceScene)
+        v.keep, v.ranges, v.tex, v.table, v.tables = self.keep, self.ranges, self.tex, self.table, None
+        v.s = SceneStruct.from_buffer_copy(self.s)
+        v.s.tables = None
+        return v
+
+    def release(self) -> None:
+        """nrc_scene_tables_destroy of the tables made by prepare()."""
+        if getattr(self, "tables", None) is not None:
+            self.s.tables = None
+            check(lib().nrc_scene_tables_destroy(self.tables), "nrc_scene_tables_destroy")
+            self.tables = None
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
 
 
 def unpack_eval(scene: DeviceScene, records, count, out_inputs, out_dst=None, capacity=None, stream=None) -> None:
