@@ -1156,6 +1156,7 @@ def ours_arm(args, world, rank, local):
                                              "about 210 GB/s)"},
         "frame_packed": packed["frame_packed"],
         "query_packed_alone_ms": packed["query_packed_alone_ms"],
+        "unpack_eval_us": packed["unpack_eval_us"],
         "clocks": clocks,
     }
     if plain is not None:

@@ -528,12 +528,16 @@ typedef struct nrc_scene {
  * buffers of Scene.glsl:30-48 directly). Per primitive one 64-byte row: its
  * three object-space vertices and texcoords and its material id (marked invalid
  * when one of its indices is out of range); per material one 64-byte row: the
- * constant colours, roughness and the two texture descriptors inline. The tables
- * are a snapshot of the buffers at that point of the stream: after changing the
- * scene's buffers, prepare again. Allocates device memory (64 bytes per primitive
- * and per material), so call it outside stream capture. Set scene->tables to
- * the result to use them; nrc_scene_tables_destroy frees them (after the work
- * that reads them has finished). */
+ * constant colours, roughness and the two texture descriptors inline; per
+ * texture a footprint array: for each texel, it and its right, lower and
+ * lower-right neighbours (wrapped) in one 16-byte word, so a bilinear sample is
+ * one load. The tables are a snapshot of the buffers at that point of the
+ * stream: after changing the scene's buffers, prepare again. Allocates device
+ * memory (64 bytes per primitive and per material, 16 per texel) and waits for
+ * the stream, so call it outside stream capture. Texels must be 4-byte aligned
+ * (NRC_ERROR_MISALIGNED). Set scene->tables to the result to use them;
+ * nrc_scene_tables_destroy frees them (after the work that reads them has
+ * finished). */
 NRC_API int nrc_scene_prepare(const nrc_scene* scene, void* stream, nrc_scene_tables** out);
 NRC_API int nrc_scene_tables_destroy(nrc_scene_tables* tables);
 

@@ -1349,17 +1349,49 @@ int nrc_scene_prepare(const nrc_scene* sc, void* stream, nrc_scene_tables** out)
   plain.tables = nullptr;  // the tables are made from the buffers
   int s = scene_check_impl(&plain);
   if (s != NRC_OK) return s;
+  const cudaStream_t st = static_cast<cudaStream_t>(stream);
+  // the texture descriptors (device array), to size the footprint arrays
+  std::vector<nrc_texture> tex(sc->texture_count);
+  cudaError_t e = cudaSuccess;
+  if (!tex.empty()) {
+    e = cudaMemcpyAsync(tex.data(), sc->textures, tex.size() * sizeof(nrc_texture), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return from_cuda(e);
+  }
   const size_t prim_bytes = size_t(sc->primitive_count) * 64, mat_bytes = size_t(sc->material_count) * 64;
+  const size_t table_bytes = up256(tex.size() * sizeof(nrc_texture));
+  size_t fp_bytes = 0;
+  std::vector<size_t> fp_off(tex.size(), 0);
+  for (size_t i = 0; i < tex.size(); ++i) {
+    if (reinterpret_cast<uintptr_t>(tex[i].texels) & 3u) return NRC_ERROR_MISALIGNED;
+    fp_off[i] = fp_bytes;
+    if (tex[i].texels != nullptr) fp_bytes += size_t(tex[i].width) * tex[i].height * 16;
+  }
+  const size_t head = up256(prim_bytes + mat_bytes) + table_bytes;
   void* p = nullptr;
-  cudaError_t e = cudaMalloc(&p, prim_bytes + mat_bytes + 64);
+  e = cudaMalloc(&p, head + fp_bytes + 64);
   if (e != cudaSuccess) return e == cudaErrorMemoryAllocation ? NRC_ERROR_OUT_OF_MEMORY : from_cuda(e);
-  auto* t = new (std::nothrow) nrc_scene_tables{p, static_cast<uint8_t*>(p) + prim_bytes, sc->primitive_count,
-                                                sc->material_count};
+  uint8_t* base = static_cast<uint8_t*>(p);
+  auto* t = new (std::nothrow) nrc_scene_tables{p, base + prim_bytes, sc->primitive_count, sc->material_count};
   if (t == nullptr) {
     cudaFree(p);
     return NRC_ERROR_OUT_OF_MEMORY;
   }
-  e = nrc::launch_scene_prepare(plain, t->prims, t->mats, static_cast<cudaStream_t>(stream));
+  // descriptors of the footprint arrays, in texture order
+  nrc_texture* d_fp = reinterpret_cast<nrc_texture*>(base + up256(prim_bytes + mat_bytes));
+  std::vector<nrc_texture> fp(tex.size());
+  for (size_t i = 0; i < tex.size(); ++i) {
+    const bool any = tex[i].texels != nullptr && tex[i].width > 0 && tex[i].height > 0;
+    fp[i].texels = any ? base + head + fp_off[i] : nullptr;
+    fp[i].width = tex[i].width;
+    fp[i].height = tex[i].height;
+  }
+  if (!fp.empty()) e = cudaMemcpyAsync(d_fp, fp.data(), fp.size() * sizeof(nrc_texture), cudaMemcpyHostToDevice, st);
+  for (size_t i = 0; i < tex.size() && e == cudaSuccess; ++i)
+    if (fp[i].texels != nullptr)
+      e = nrc::launch_texture_footprints(tex[i], const_cast<uint8_t*>(fp[i].texels), device_sms(), st);
+  if (e == cudaSuccess) e = nrc::launch_scene_prepare(plain, d_fp, t->prims, t->mats, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // the host descriptor arrays are read by then
   if (e != cudaSuccess) {
     cudaFree(p);
     delete t;

@@ -231,8 +231,13 @@ cudaError_t launch_encode(const nrc_input* in, const uint32_t* d_count, uint32_t
 cudaError_t launch_sph_encode(const float* dirs, const uint32_t* d_count, uint32_t capacity, float* out,
                               int num_sms, cudaStream_t stream);
 // The gather tables of nrc_scene_prepare: 64-byte rows, primitive_count of
-// them at prim_rows and material_count at mat_rows (16-byte aligned).
-cudaError_t launch_scene_prepare(const nrc_scene& scene, void* prim_rows, void* mat_rows, cudaStream_t stream);
+// them at prim_rows and material_count at mat_rows (16-byte aligned);
+// footprints: device array of texture_count descriptors of the textures'
+// footprint arrays (launch_texture_footprints), which the material rows point at.
+cudaError_t launch_scene_prepare(const nrc_scene& scene, const nrc_texture* footprints, void* prim_rows,
+                                 void* mat_rows, cudaStream_t stream);
+// One texture's footprint array (16 bytes per texel, 16-byte aligned `out`).
+cudaError_t launch_texture_footprints(const nrc_texture& tex, void* out, int num_sms, cudaStream_t stream);
 // The train records of nbatches batches (min(*counts[b], capacity) each) in one
 // launch, into unpacked arrays out[b]. prim_rows / mat_rows: the scene's
 // prepared tables, or both null to gather from the scene buffers.

@@ -64,23 +64,68 @@ __device__ __forceinline__ uint32_t wrap(float f, uint32_t n) {
   return static_cast<uint32_t>(r);
 }
 
-// `lut` is the sRGB decode table (srgb_lut()) in shared memory (stage_lut).
-__device__ inline F3 sample_texels(const uchar4* __restrict__ px, uint32_t w, uint32_t h, float tu, float tv,
-                                   const float* lut) {
-  if (w == 0 || h == 0 || px == nullptr) return F3{0.f, 0.f, 0.f};
+// `lut` is this thread's copy of the sRGB decode table (srgb_lut()) in shared
+// memory: entry c at lut[c * kLutCopies] (stage_lut). One copy: interleaved
+// copies that spread a warp's lookups over the banks (16 or 32 of them) were
+// measured no faster, and they take shared memory from the L1 capacity the
+// scene gathers use.
+constexpr uint32_t kLutCopies = 1;
+// Bilinear footprint of (tu, tv) on a w x h texture with REPEAT addressing:
+// texel (i0, j0), its neighbours i1 = i0 + 1 and j1 = j0 + 1 (wrapped), and
+// the filter weights a (along u) and b (along v).
+struct Footprint {
+  uint32_t i0, j0, i1, j1;
+  float a, b;
+};
+
+__device__ __forceinline__ Footprint footprint(uint32_t w, uint32_t h, float tu, float tv) {
   float u = __fmaf_rn(tu, static_cast<float>(w), -0.5f), v = __fmaf_rn(tv, static_cast<float>(h), -0.5f);
   if (!(fabsf(u) < 8388608.0f)) u = 0.0f;  // NaN or beyond fp32's integer range: texel 0's neighbourhood
   if (!(fabsf(v) < 8388608.0f)) v = 0.0f;
   const float fu = floorf(u), fv = floorf(v);
-  const float a = __fsub_rn(u, fu), b = __fsub_rn(v, fv);
-  const uint32_t i0 = wrap(fu, w), j0 = wrap(fv, h);
-  const uint32_t i1 = i0 + 1 == w ? 0 : i0 + 1, j1 = j0 + 1 == h ? 0 : j0 + 1;
-  const uchar4 t00 = px[size_t(j0) * w + i0], t10 = px[size_t(j0) * w + i1];
-  const uchar4 t01 = px[size_t(j1) * w + i0], t11 = px[size_t(j1) * w + i1];
+  Footprint f;
+  f.a = __fsub_rn(u, fu);
+  f.b = __fsub_rn(v, fv);
+  f.i0 = wrap(fu, w);
+  f.j0 = wrap(fv, h);
+  f.i1 = f.i0 + 1 == w ? 0 : f.i0 + 1;
+  f.j1 = f.j0 + 1 == h ? 0 : f.j0 + 1;
+  return f;
+}
+
+// sRGB-decode and filter the four texels t00 (i0, j0), t10 (i1, j0), t01 (i0, j1), t11 (i1, j1).
+__device__ __forceinline__ F3 filter(uchar4 t00, uchar4 t10, uchar4 t01, uchar4 t11, float a, float b,
+                                     const float* lut) {
   auto ch = [&](unsigned char c00, unsigned char c10, unsigned char c01, unsigned char c11) {
-    return lerp(lerp(lut[c00], lut[c10], a), lerp(lut[c01], lut[c11], a), b);
+    return lerp(lerp(lut[c00 * kLutCopies], lut[c10 * kLutCopies], a), lerp(lut[c01 * kLutCopies], lut[c11 * kLutCopies], a),
+                b);
   };
   return F3{ch(t00.x, t10.x, t01.x, t11.x), ch(t00.y, t10.y, t01.y, t11.y), ch(t00.z, t10.z, t01.z, t11.z)};
+}
+
+__device__ __forceinline__ uchar4 as_uchar4(uint32_t v) {
+  return make_uchar4(v & 0xFFu, (v >> 8) & 0xFFu, (v >> 16) & 0xFFu, v >> 24);
+}
+
+// A texture of the scene buffers: four texel loads.
+__device__ inline F3 sample_texels(const uchar4* __restrict__ px, uint32_t w, uint32_t h, float tu, float tv,
+                                   const float* lut) {
+  if (w == 0 || h == 0 || px == nullptr) return F3{0.f, 0.f, 0.f};
+  const Footprint f = footprint(w, h, tu, tv);
+  const uchar4 t00 = px[size_t(f.j0) * w + f.i0], t10 = px[size_t(f.j0) * w + f.i1];
+  const uchar4 t01 = px[size_t(f.j1) * w + f.i0], t11 = px[size_t(f.j1) * w + f.i1];
+  return filter(t00, t10, t01, t11, f.a, f.b, lut);
+}
+
+// A texture of the gather tables, stored as footprints: entry (j, i) holds the
+// texels (i, j), (i + 1, j), (i, j + 1), (i + 1, j + 1) (wrapped) in one
+// 16-byte word, so a sample is one load.
+__device__ inline F3 sample_quads(const uint4* __restrict__ q, uint32_t w, uint32_t h, float tu, float tv,
+                                  const float* lut) {
+  if (w == 0 || h == 0 || q == nullptr) return F3{0.f, 0.f, 0.f};
+  const Footprint f = footprint(w, h, tu, tv);
+  const uint4 t = q[size_t(f.j0) * w + f.i0];
+  return filter(as_uchar4(t.x), as_uchar4(t.y), as_uchar4(t.z), as_uchar4(t.w), f.a, f.b, lut);
 }
 
 // The gather tables of nrc_scene_prepare (nrc_scene_tables), as 16-byte words.
@@ -89,7 +134,8 @@ __device__ inline F3 sample_texels(const uchar4* __restrict__ px, uint32_t w, ui
 // material id is kInvalidRow when one of the primitive's indices is out of
 // range. Material row (4 words): (diffuse.rgb, roughness), (specular.rgb,
 // flags: bit 0 diffuse textured, bit 1 specular textured), then the diffuse and
-// the specular texture as (texels address low, high, width, height).
+// the specular texture as (footprint array address low, high, width, height);
+// the footprint arrays (sample_quads) are part of the tables.
 struct SceneRows {
   const uint4* prims;
   const uint4* mats;
@@ -102,7 +148,7 @@ struct Gathered {
   float2 tc[3];    // texcoords
   uint4 col[2];    // diffuse / specular constant rgb in x..z
   float roughness;
-  const uchar4* tex[2];  // texture of each colour (sampled when `textured`)
+  const void* tex[2];    // texture of each colour (sampled when `textured`): texels, or footprints with kRows
   uint32_t tw[2], th[2];
   bool textured[2];
   bool ok;         // every index in range
@@ -156,7 +202,7 @@ __device__ __forceinline__ void gather_buffers(const nrc_scene& S, uint32_t pr, 
     g.tw[c] = g.th[c] = 0;
     if (g.textured[c]) {
       const nrc_texture t = S.textures[ids[c]];
-      g.tex[c] = reinterpret_cast<const uchar4*>(t.texels);
+      g.tex[c] = t.texels;
       g.tw[c] = t.width;
       g.th[c] = t.height;
     }
@@ -164,19 +210,18 @@ __device__ __forceinline__ void gather_buffers(const nrc_scene& S, uint32_t pr, 
   g.ok = ok;
 }
 
-// Gathers from the prepared rows: one primitive row, then one material row.
-__device__ __forceinline__ void gather_rows(const SceneRows& R, uint32_t pr, bool ok, Gathered& g) {
-  const uint4* row = R.prims + size_t(pr) * 4;
-  const uint4 q0 = row[0], q1 = row[1], q2 = row[2], q3 = row[3];
-  ok = ok && q3.w != kInvalidRow;
-  const uint32_t mid = ok ? q3.w : 0u;
-  g.p[0] = F3{__uint_as_float(q0.x), __uint_as_float(q0.y), __uint_as_float(q0.z)};
-  g.p[1] = F3{__uint_as_float(q1.x), __uint_as_float(q1.y), __uint_as_float(q1.z)};
-  g.p[2] = F3{__uint_as_float(q2.x), __uint_as_float(q2.y), __uint_as_float(q2.z)};
-  g.tc[0] = make_float2(__uint_as_float(q0.w), __uint_as_float(q1.w));
-  g.tc[1] = make_float2(__uint_as_float(q2.w), __uint_as_float(q3.x));
-  g.tc[2] = make_float2(__uint_as_float(q3.y), __uint_as_float(q3.z));
-  const uint4* m = R.mats + size_t(mid) * 4;
+// Gathers from the prepared rows: the record's primitive row (its four words
+// q, loaded by the caller), then its material row.
+__device__ __forceinline__ void gather_row(const uint4 (&q)[4], const uint4* __restrict__ mats, bool ok, Gathered& g) {
+  ok = ok && q[3].w != kInvalidRow;
+  const uint32_t mid = ok ? q[3].w : 0u;
+  g.p[0] = F3{__uint_as_float(q[0].x), __uint_as_float(q[0].y), __uint_as_float(q[0].z)};
+  g.p[1] = F3{__uint_as_float(q[1].x), __uint_as_float(q[1].y), __uint_as_float(q[1].z)};
+  g.p[2] = F3{__uint_as_float(q[2].x), __uint_as_float(q[2].y), __uint_as_float(q[2].z)};
+  g.tc[0] = make_float2(__uint_as_float(q[0].w), __uint_as_float(q[1].w));
+  g.tc[1] = make_float2(__uint_as_float(q[2].w), __uint_as_float(q[3].x));
+  g.tc[2] = make_float2(__uint_as_float(q[3].y), __uint_as_float(q[3].z));
+  const uint4* m = mats + size_t(mid) * 4;
   const uint4 m0 = m[0], m1 = m[1], m2 = m[2], m3 = m[3];
   g.col[0] = m0;
   g.col[1] = m1;
@@ -185,37 +230,69 @@ __device__ __forceinline__ void gather_rows(const SceneRows& R, uint32_t pr, boo
 #pragma unroll
   for (int c = 0; c < 2; ++c) {
     g.textured[c] = ok && ((m1.w >> c) & 1u);
-    g.tex[c] = reinterpret_cast<const uchar4*>((static_cast<uint64_t>(t[c].y) << 32) | t[c].x);
+    g.tex[c] = reinterpret_cast<const void*>((static_cast<uint64_t>(t[c].y) << 32) | t[c].x);
     g.tw[c] = t[c].z;
     g.th[c] = t[c].w;
   }
   g.ok = ok;
 }
 
-// UnpackNRCInput into 14 floats (nrc_input); false (and zeros) for a record
-// whose indices fall outside the scene. `lut` is the sRGB decode table in
-// shared memory (stage_lut). kRows: gather from the prepared tables `rows`, else from the
-// scene buffers. The loads take no early exit: an out-of-range index is
-// replaced by 0 and the record's outputs are zeroed at the end, so a thread can
-// have the loads of several records in flight.
-template <bool kRows>
-__device__ __forceinline__ bool unpack_one(const nrc_scene& S, const SceneRows& rows, const nrc_packed_input& in,
-                                           const float* lut, float (&r)[kInFloats]) {
-  if (scene_empty(S)) {
-#pragma unroll
-    for (int k = 0; k < kInFloats; ++k) r[k] = 0.0f;
-    return false;
-  }
+// A record's primitive and instance, clamped to 0 (in range once the scene is
+// not empty) when out of range, which clears `ok`.
+struct RecordRef {
+  uint32_t prim, inst;
+  bool ok, flip;
+};
+
+__device__ __forceinline__ RecordRef record_ref(const nrc_scene& S, const nrc_packed_input& in) {
   const uint32_t prim = in.primitive_id, inst = in.flip_bit_instance_id & 0x7FFFFFFFu;
-  const bool flip = (in.flip_bit_instance_id >> 31) != 0;
-  const bool ok0 = prim < S.primitive_count && inst < S.instance_count;
-  const uint32_t pr = ok0 ? prim : 0u, in_id = ok0 ? inst : 0u;
-  Gathered g;
-  if constexpr (kRows)
-    gather_rows(rows, pr, ok0, g);
-  else
-    gather_buffers(S, pr, ok0, g);
-  const float4* T4 = reinterpret_cast<const float4*>(S.transforms + size_t(in_id) * 12);
+  RecordRef f;
+  f.flip = (in.flip_bit_instance_id >> 31) != 0;
+  f.ok = prim < S.primitive_count && inst < S.instance_count;
+  f.prim = f.ok ? prim : 0u;
+  f.inst = f.ok ? inst : 0u;
+  return f;
+}
+
+// The primitive rows of a warp's 32 records (lane l's row index `prim`),
+// loaded cooperatively: load r fetches the rows of records 8r..8r+7, four
+// lanes per row (16 bytes each), so each load instruction touches 8 rows
+// instead of 32. warp_rows_load issues the loads; warp_rows_share passes the
+// rows through `buf` (2 KB of the warp's shared memory, 16-byte slots swizzled
+// so that neither the stores nor the loads conflict) to their lanes. Warp-wide.
+__device__ __forceinline__ void warp_rows_load(const uint4* __restrict__ rows, uint32_t prim, uint4 (&v)[4]) {
+  const uint32_t lane = threadIdx.x & 31u;
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const uint32_t p = __shfl_sync(0xffffffffu, prim, 8 * r + (lane >> 2));
+    v[r] = rows[size_t(p) * 4 + (lane & 3u)];
+  }
+}
+
+__device__ __forceinline__ void warp_rows_share(const uint4 (&v)[4], uint4* __restrict__ buf, uint4 (&q)[4]) {
+  const uint32_t lane = threadIdx.x & 31u;
+  __syncwarp();  // the buffer's previous contents have been read
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const uint32_t rec = 8 * r + (lane >> 2);
+    buf[rec * 4 + ((lane & 3u) ^ ((rec >> 1) & 3u))] = v[r];
+  }
+  __syncwarp();
+#pragma unroll
+  for (int k = 0; k < 4; ++k) q[k] = buf[lane * 4 + (k ^ ((lane >> 1) & 3u))];
+}
+
+// UnpackNRCInput into 14 floats (nrc_input) from a record's gathered scene
+// data; false (and zeros) for a record whose indices fall outside the scene.
+// `lut` is this thread's copy of the sRGB decode table (stage_lut). kRows: the
+// textures are the tables' footprint arrays. The loads take no early exit: an
+// out-of-range index is replaced by 0 and the record's outputs are zeroed at
+// the end, so a thread can have the loads of several records in flight.
+template <bool kRows>
+__device__ __forceinline__ bool finish_unpack(const nrc_scene& S, const nrc_packed_input& in, const RecordRef& ref,
+                                              const Gathered& g, const float* lut, float (&r)[kInFloats]) {
+  const bool flip = ref.flip;
+  const float4* T4 = reinterpret_cast<const float4*>(S.transforms + size_t(ref.inst) * 12);
   const float4 T[3] = {T4[0], T4[1], T4[2]};
   F3 v[3];
 #pragma unroll
@@ -246,7 +323,12 @@ __device__ __forceinline__ bool unpack_one(const nrc_scene& S, const SceneRows& 
 #pragma unroll
   for (int c = 0; c < 2; ++c) {
     F3 col{__uint_as_float(g.col[c].x), __uint_as_float(g.col[c].y), __uint_as_float(g.col[c].z)};
-    if (g.textured[c]) col = sample_texels(g.tex[c], g.tw[c], g.th[c], tu, tv, lut);
+    if (g.textured[c]) {
+      if constexpr (kRows)
+        col = sample_quads(static_cast<const uint4*>(g.tex[c]), g.tw[c], g.th[c], tu, tv, lut);
+      else
+        col = sample_texels(static_cast<const uchar4*>(g.tex[c]), g.tw[c], g.th[c], tu, tv, lut);
+    }
     r[8 + 3 * c] = col.x;
     r[9 + 3 * c] = col.y;
     r[10 + 3 * c] = col.z;
@@ -258,16 +340,30 @@ __device__ __forceinline__ bool unpack_one(const nrc_scene& S, const SceneRows& 
   return g.ok;
 }
 
+// UnpackNRCInput of one record from the scene buffers (one thread's gathers).
+__device__ __forceinline__ bool unpack_one(const nrc_scene& S, const nrc_packed_input& in, const float* lut,
+                                           float (&r)[kInFloats]) {
+  if (scene_empty(S)) {
+#pragma unroll
+    for (int k = 0; k < kInFloats; ++k) r[k] = 0.0f;
+    return false;
+  }
+  const RecordRef ref = record_ref(S, in);
+  Gathered g;
+  gather_buffers(S, ref.prim, ref.ok, g);
+  return finish_unpack<false>(S, in, ref, g, lut, r);
+}
+
 // sRGB -> linear of the 256 byte values, in double, rounded once (host).
 const SrgbLut& srgb_lut();
 
-// The table into shared memory (1 KB: a larger copy, one per bank to avoid
-// conflicts, measured slower, as it takes L1 capacity from the scene gathers).
-// Block-wide.
+// The table into shared memory as kLutCopies interleaved copies (entry c of
+// copy k at lut[c * kLutCopies + k]); returns this thread's copy
+// (thread % kLutCopies). Block-wide.
 __device__ __forceinline__ const float* stage_lut(float* lut, const SrgbLut& src) {
-  for (uint32_t i = threadIdx.x; i < 256u; i += blockDim.x) lut[i] = src.v[i];
+  for (uint32_t i = threadIdx.x; i < 256u * kLutCopies; i += blockDim.x) lut[i] = src.v[i / kLutCopies];
   __syncthreads();
-  return lut;
+  return lut + (threadIdx.x % kLutCopies);
 }
 
 }  // namespace nrc
