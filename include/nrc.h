@@ -371,7 +371,10 @@ typedef struct nrc_train_job {
 NRC_API int nrc_infer_many(const nrc_query_job* jobs, uint32_t njobs, const uint32_t* ctas, void* stream);
 
 /* nrc_train_batches for every job, one cooperative launch per 32 jobs. `ctas`
- * may be NULL. */
+ * may be NULL. Training launches (this, nrc_train*, nrc_frame*) that run at
+ * the same time on different streams should be ordered with events: each grid
+ * waits at its grid barrier until all of its CTAs run, and two grids that each
+ * hold SMs the other needs end in NRC_ERROR_DEVICE_TIMEOUT after the 2 s bound. */
 NRC_API int nrc_train_many(const nrc_train_job* jobs, uint32_t njobs, const uint32_t* ctas, void* stream);
 
 /* CTA split that nrc_infer_many / nrc_train_many use when `ctas` is NULL, for

@@ -16,7 +16,10 @@
 //     event) on the next of max_inflight_batches streams and goes on forming the
 //     next batch while this one runs: batches hold disjoint sessions, so they
 //     are independent, and their kernels share the SMs (a batch's small
-//     training groups run beside the next batch's queries);
+//     training groups run beside the next batch's queries); training launches
+//     of different batches run one after another (an event chain across the
+//     streams), so two cooperative training grids never wait for each other's
+//     SMs;
 //   - finished batches are retired by polling their events; a request's latency
 //     runs from its submission to the moment the worker sees its batch's event
 //     complete.
@@ -107,6 +110,10 @@ struct nrc_server {
   int device = 0;
   int sms = 0;
   std::vector<cudaStream_t> streams;  // one per in-flight batch
+  // Recorded after each batch's training launch; the next batch's training
+  // waits for it, so training grids of batches on different streams never
+  // compete for SMs while their grid barriers wait (used by the worker only).
+  cudaEvent_t train_tail = nullptr;
   uint64_t launched = 0;
   std::mutex m;
   std::condition_variable cv_work;  // new requests, or stop
@@ -193,7 +200,7 @@ std::vector<Request> pick(nrc_server* S, std::vector<LaunchItem>& items) {
   return out;
 }
 
-int launch_batch(const std::vector<LaunchItem>& items, cudaStream_t stream, cudaEvent_t done) {
+int launch_batch(nrc_server* S, const std::vector<LaunchItem>& items, cudaStream_t stream, cudaEvent_t done) {
   nrc_query_job q[kMaxBatch];
   nrc_train_job t[kMaxBatch];
   uint32_t ctas[kMaxBatch];
@@ -215,7 +222,13 @@ int launch_batch(const std::vector<LaunchItem>& items, cudaStream_t stream, cuda
     ctas[j] = it.train_ctas;
   }
   int st = nrc_infer_many(q, n, nullptr, stream);
+  // One training grid at a time across the streams: a cooperative grid whose
+  // CTAs wait at its grid barrier for SMs that another batch's training grid
+  // holds (and the other way round) would stall both until their bounded
+  // waits give up. Queries of other batches still overlap the training.
+  if (st == NRC_OK && cudaStreamWaitEvent(stream, S->train_tail, 0) != cudaSuccess) st = NRC_ERROR_CUDA;
   if (st == NRC_OK) st = nrc_train_many(t, n, ctas, stream);
+  if (st == NRC_OK && cudaEventRecord(S->train_tail, stream) != cudaSuccess) st = NRC_ERROR_CUDA;
   if (st == NRC_OK && cudaEventRecord(done, stream) != cudaSuccess) st = NRC_ERROR_CUDA;
   return st;
 }
@@ -234,7 +247,7 @@ void worker_main(nrc_server* S) {
         cudaEvent_t ev = take_event(S);
         cudaStream_t stream = S->streams[S->launched++ % S->streams.size()];
         lk.unlock();  // launches are asynchronous; submitters need not wait for them
-        const int st = ev ? launch_batch(items, stream, ev) : NRC_ERROR_CUDA;
+        const int st = ev ? launch_batch(S, items, stream, ev) : NRC_ERROR_CUDA;
         lk.lock();
         if (st != NRC_OK) {
           // the requests complete as failed: unblock their sessions and waiters
@@ -302,6 +315,11 @@ int nrc_server_create(const nrc_server_config* cfg, nrc_server** out) {
     }
     S->streams.push_back(st);
   }
+  if (cudaEventCreateWithFlags(&S->train_tail, cudaEventDisableTiming) != cudaSuccess) {
+    for (cudaStream_t x : S->streams) cudaStreamDestroy(x);
+    delete S;
+    return NRC_ERROR_CUDA;
+  }
   S->worker = std::thread(worker_main, S);
   *out = S;
   return NRC_OK;
@@ -322,6 +340,7 @@ int nrc_server_destroy(nrc_server* S) {
     cudaFree(s.block);
   }
   for (cudaEvent_t e : S->free_events) cudaEventDestroy(e);
+  cudaEventDestroy(S->train_tail);
   for (cudaStream_t x : S->streams) cudaStreamDestroy(x);
   const int st = S->worker_status;
   delete S;
