@@ -370,9 +370,9 @@ __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_co
     if (threadIdx.x == 0) {
       __threadfence();
       *last = atomicAdd(J.tiles + 1, 1u) == gridDim.x - 1 ? 1u : 0u;
-      if (*last != 0u) {
-        atomicExch(J.tiles, 0u);
-        atomicExch(J.tiles + 1, 0u);
+      if (*last != 0u) {  // every CTA has taken its last tile and counted itself out
+        reinterpret_cast<volatile uint32_t*>(J.tiles)[0] = 0u;
+        reinterpret_cast<volatile uint32_t*>(J.tiles)[1] = 0u;
         __threadfence();
       }
     }

@@ -83,11 +83,26 @@ __device__ __forceinline__ void frame_join(const FrameJoin& j, uint32_t* slot) {
   }
   __syncthreads();
   if (*slot != 0u) {
-    for (uint32_t i = threadIdx.x; i < kJoinChunks; i += blockDim.x) j.dst[i] = j.src[i];
+    // all of a thread's loads (from L2: other CTAs wrote the source) are in
+    // flight before its stores, so the copy costs about one memory round trip
+    constexpr uint32_t kUnroll = 8;
+    for (uint32_t base = 0; base < kJoinChunks; base += kUnroll * blockDim.x) {
+      uint4 v[kUnroll];
+#pragma unroll
+      for (uint32_t u = 0; u < kUnroll; ++u) {
+        const uint32_t i = base + u * blockDim.x + threadIdx.x;
+        if (i < kJoinChunks) v[u] = __ldcg(j.src + i);
+      }
+#pragma unroll
+      for (uint32_t u = 0; u < kUnroll; ++u) {
+        const uint32_t i = base + u * blockDim.x + threadIdx.x;
+        if (i < kJoinChunks) j.dst[i] = v[u];
+      }
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
       __threadfence();
-      atomicExch(j.counter, 0u);
+      *reinterpret_cast<volatile uint32_t*>(j.counter) = 0u;
     }
   }
 }
