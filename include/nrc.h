@@ -421,7 +421,19 @@ typedef struct nrc_server nrc_server;
 typedef struct nrc_server_config {
   uint64_t hbm_budget_bytes;    /* device memory for session state and frame slots */
   uint32_t max_batch_sessions;  /* requests per batched launch, 1..32 */
-  uint32_t max_inflight_batches;/* launched, unfinished batches, 1..8 */
+  uint32_t max_inflight_batches;/* launched, unfinished batches, 1..8 (host worker only) */
+  /* 0: a host worker thread forms the batches and launches them on
+   * max_inflight_batches streams. 1: the loop runs on the device: a CUDA graph
+   * whose while node repeats scheduler kernel -> batched query -> batched
+   * training -> completion kernel while requests keep coming (a launch ends
+   * after 200 us without one; the next submit launches it again), taking the
+   * requests that nrc_server_submit writes into a ring in host-mapped memory
+   * (batches then run one after another; requests that arrive during one join
+   * the next). Sessions must be fp16 caches without fp8_inference; opening or
+   * closing a session pauses the loop (its requests complete first) while
+   * device memory is allocated or freed; a submit's ready_event is waited on
+   * by the submitting thread. */
+  uint32_t device_loop;
 } nrc_server_config;
 
 typedef struct nrc_session_desc {

@@ -7,7 +7,11 @@ then four chained training steps, the last writing use_weights. A session's
 results must be the same alone and in any mix of sessions: its query answers
 are per-record computations and its training runs in a CTA group of a fixed
 size, so the comparison is bit for bit, and it is also checked against the
-same schedule driven through the batched-cache calls directly."""
+same schedule driven through the batched-cache calls directly.
+
+Every test runs on both forms of the loop: the host worker thread, and the
+device-resident loop (a CUDA graph whose while node runs scheduler, batched
+query, batched training and completion kernels on the GPU)."""
 import numpy as np
 import pytest
 
@@ -64,19 +68,20 @@ def _run_session_frames(srv, sid, spec, frames, slots=2):
 SPECS = {"a": (11, 50000, 4096), "b": (12, 120000, 16384), "c": (13, 7000, 1000), "d": (14, 300000, 8192)}
 
 
-def test_session_alone_equals_in_mix_and_direct_calls(cuda):
+@pytest.mark.parametrize("device_loop", [False, True])
+def test_session_alone_equals_in_mix_and_direct_calls(cuda, device_loop):
     import threading
 
     from vknrc_gb300 import Cache, nrc
 
     frames = 3
     seed, q, r = SPECS["a"]
-    with nrc.Server(8 * GB) as srv:
+    with nrc.Server(8 * GB, device_loop=device_loop) as srv:
         sa = srv.open_session(q, r, seed=seed)
         alone = _run_session_frames(srv, sa, SPECS["a"], frames)
         c = srv.cache(sa)
         alone_w, alone_ent = c.get_weights(0), c.get_optimizer()[1]
-    with nrc.Server(8 * GB, max_batch_sessions=4) as srv:
+    with nrc.Server(8 * GB, max_batch_sessions=4, device_loop=device_loop) as srv:
         ids = {k: srv.open_session(SPECS[k][1], SPECS[k][2], seed=SPECS[k][0]) for k in SPECS}
         results = {}
         threads = [threading.Thread(target=lambda k=k: results.__setitem__(
@@ -106,10 +111,11 @@ def test_session_alone_equals_in_mix_and_direct_calls(cuda):
         assert np.array_equal(ref.get_optimizer()[1], alone_ent)
 
 
-def test_budget_admission_and_release(cuda):
+@pytest.mark.parametrize("device_loop", [False, True])
+def test_budget_admission_and_release(cuda, device_loop):
     from vknrc_gb300 import NRCError, nrc
 
-    with nrc.Server(200 << 20) as srv:  # 200 MB
+    with nrc.Server(200 << 20, device_loop=device_loop) as srv:  # 200 MB
         ids = []
         with pytest.raises(NRCError) as e:
             for _ in range(64):
@@ -127,7 +133,8 @@ def test_budget_admission_and_release(cuda):
             srv.open_session(1000, 1000, frame_slots=0)
 
 
-def test_requests_batch_and_complete_in_session_order(cuda):
+@pytest.mark.parametrize("device_loop", [False, True])
+def test_requests_batch_and_complete_in_session_order(cuda, device_loop):
     """Many sessions submitting back to back: requests are batched (more than
     one session per launch on average), every request completes, and each
     session's step count equals its frames (its requests ran in order, one at
@@ -137,7 +144,7 @@ def test_requests_batch_and_complete_in_session_order(cuda):
     from vknrc_gb300 import nrc
 
     n_sess, frames, q, r = 8, 4, 20000, 2048
-    with nrc.Server(8 * GB, max_batch_sessions=8, max_inflight_batches=2) as srv:
+    with nrc.Server(8 * GB, max_batch_sessions=8, max_inflight_batches=2, device_loop=device_loop) as srv:
         ids = [srv.open_session(q, r, frame_slots=frames, seed=900 + s) for s in range(n_sess)]
         for s in ids:
             for k in range(frames):
@@ -154,3 +161,28 @@ def test_requests_batch_and_complete_in_session_order(cuda):
             c = srv.cache(s)
             assert c.get_optimizer()[0][0] == 4 * frames
             assert c.error() == 0
+
+
+def test_device_loop_matches_host_worker_and_rejects_other_formats(cuda):
+    """The same session frames through both loops give the same outputs and
+    cache state bit for bit; the device loop takes fp16 caches only."""
+    from vknrc_gb300 import NRCError, nrc
+
+    frames = 3
+    res = []
+    for device_loop in (False, True):
+        with nrc.Server(4 * GB, device_loop=device_loop) as srv:
+            sid = srv.open_session(SPECS["c"][1], SPECS["c"][2], seed=SPECS["c"][0])
+            outs = _run_session_frames(srv, sid, SPECS["c"], frames)
+            c = srv.cache(sid)
+            res.append((outs, c.get_weights(0), c.get_optimizer()[1]))
+            if device_loop:
+                with pytest.raises(NRCError) as e:
+                    srv.open_session(1000, 1000, precision=1)
+                assert e.value.status == 1
+                st = srv.stats()
+                assert st["batches"] >= frames and st["completed"] == frames
+    for k in range(frames):
+        assert np.array_equal(res[0][0][k], res[1][0][k]), k
+    assert np.array_equal(res[0][1], res[1][1])
+    assert np.array_equal(res[0][2], res[1][2])

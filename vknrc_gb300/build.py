@@ -17,7 +17,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libnrc.so")
-SOURCES = ["nrc_api.cu", "nrc_infer.cu", "nrc_train.cu", "nrc_encode.cu", "nrc_noalloc.cu", "nrc_server.cu", "nrc_screen.cu", "nrc_unpack.cu", "nrc_fp8.cu", "nrc_trace.cu", "nrc_optimize.cu"]
+SOURCES = ["nrc_api.cu", "nrc_infer.cu", "nrc_train.cu", "nrc_encode.cu", "nrc_noalloc.cu", "nrc_server.cu", "nrc_server_loop.cu", "nrc_screen.cu", "nrc_unpack.cu", "nrc_fp8.cu", "nrc_trace.cu", "nrc_optimize.cu"]
 # per-file flags: the path tracer keeps every multiply and add separate (its CPU
 # oracle repeats the same IEEE operations)
 FILE_FLAGS = {"nrc_trace.cu": ["-fmad=false"]}

@@ -529,6 +529,31 @@ int nrc_frame(nrc_context* c, const nrc_input* eval_in, const uint32_t* d_eval_c
 
 }  // extern "C"
 
+namespace nrc {
+int loop_slot_jobs(nrc_context* c, const nrc_frame_buffers& f, uint32_t max_queries, uint32_t train_records,
+                   InferJob* ij, TrainJob* tj) {
+  const int s = check_ctx(c);
+  if (s != NRC_OK) return s;
+  if (c->bf16 || c->fp8) return NRC_ERROR_INVALID_ARGUMENT;
+  *ij = InferJob{};
+  ij->wmap = *weight_map_of(c, NRC_WEIGHTS_USE);
+  ij->input = f.queries;
+  ij->d_count = f.query_count;
+  ij->capacity = max_queries;
+  ij->err = c->err;
+  ij->q.out = f.out_rgb;
+  ij->q.clamp = 1;
+  TrainParams p = train_params(c, NRC_TRAIN_BATCH_COUNT, kTrainStep);
+  for (int b = 0; b < NRC_TRAIN_BATCH_COUNT; ++b)
+    p.batch[b] = TrainBatch{f.train[b], f.train_count[b], train_records, b == NRC_TRAIN_BATCH_COUNT - 1 ? 1 : 0};
+  *tj = TrainJob{};
+  tj->wmap = c->map_w16;
+  tj->p = p;
+  return NRC_OK;
+}
+}  // namespace nrc
+
+
 // Gather tables of one scene (nrc_scene_prepare): primitive_count 64-byte
 // primitive rows, then material_count material rows, in one allocation.
 struct nrc_scene_tables {

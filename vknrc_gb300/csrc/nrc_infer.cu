@@ -121,10 +121,13 @@ __device__ __forceinline__ void scatter_query(const QueryOut& Q, uint32_t dst, f
 // layer's fp32 sum multiplied by its scale constant before the ReLU and the
 // conversion; the weights keep the 128-byte rows of the 16-bit layout, K bytes
 // 64..127 being zero and never read).
-template <bool kEncoded, bool kScatter, int N, int kFmt>
-__global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_constant__ InferLaunch<N> L) {
-
+// kTable: the launch's parameters come from a table in global memory (the
+// serving loop's batches, written by its scheduler kernel) instead of the
+// kernel parameters; CTAs past the table's groups return at once.
+template <bool kEncoded, bool kScatter, int N, int kFmt, bool kTable>
+__device__ __forceinline__ void infer_body(const InferLaunch<N>& L) {
   constexpr bool kBF16 = kFmt == 1, kF8 = kFmt == 2;
+  if (kTable && blockIdx.x >= L.group_start[L.njobs]) return;
   int job = 0;
   while (job + 1 < L.njobs && blockIdx.x >= L.group_start[job + 1]) ++job;
   const InferJob& J = L.job[job];
@@ -169,7 +172,10 @@ __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_co
     tmem_alloc(tmem_slot, 512);
     tmem_relinquish();
   }
-  if (threadIdx.x == 0) stage_weights_tma(smem_w, &J.wmap, w_full);
+  if (threadIdx.x == 0) {
+    if (kTable) tensormap_acquire(&J.wmap);
+    stage_weights_tma(smem_w, &J.wmap, w_full);
+  }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
@@ -390,6 +396,16 @@ __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_co
 }
 
 template <bool kEncoded, bool kScatter, int N, int kFmt>
+__global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(const __grid_constant__ InferLaunch<N> L) {
+  infer_body<kEncoded, kScatter, N, kFmt, false>(L);
+}
+
+// The batched record query over a launch table in global memory.
+__global__ void __launch_bounds__(kInferThreads, 1) infer_table_kernel(const InferLaunch<kMaxInferJobs>* __restrict__ L) {
+  infer_body<false, false, kMaxInferJobs, 0, true>(*L);
+}
+
+template <bool kEncoded, bool kScatter, int N, int kFmt>
 cudaError_t launch(const InferLaunch<N>& L, uint32_t grid, cudaStream_t stream) {
   cudaLaunchAttribute attr;
   attr.id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -427,7 +443,16 @@ cudaError_t configure_infer_kernels() {
   if (e == cudaSuccess) e = set_smem<false, true, 1, 1>();
   if (e == cudaSuccess) e = set_smem<false, false, kMaxInferJobs, 1>();
   if (e == cudaSuccess) e = set_smem<false, false, 1, 2>();
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(infer_table_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(infer_table_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared);
   return e;
+}
+
+cudaError_t launch_infer_table(const InferLaunch<kMaxInferJobs>* table, uint32_t grid, cudaStream_t stream) {
+  infer_table_kernel<<<grid, kInferThreads, kSmemBytes, stream>>>(table);
+  return cudaGetLastError();
 }
 
 uint32_t infer_smem_bytes() { return kSmemBytes; }

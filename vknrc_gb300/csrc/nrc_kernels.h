@@ -218,6 +218,13 @@ struct TrainLaunch {
 
 constexpr int kMaxTrainJobs = 32;  // caches per batched training launch
 
+// The batched query and training over launch tables in global memory (the
+// serving loop's batches, written on the device): CTAs past the table's groups
+// return at once; fp16 caches only.
+cudaError_t launch_infer_table(const InferLaunch<kMaxInferJobs>* table, uint32_t grid, cudaStream_t stream);
+cudaError_t launch_train_table(const TrainLaunch<kMaxTrainJobs>* table, uint32_t grid, bool cooperative,
+                               cudaStream_t stream);
+
 // The reference's prepare + optimizer passes over a given gradient sum
 // (p supplies the hyper-parameters and the cache's buffers), and the relative-L2
 // gradient rows of given predictions (nrc_optimize.cu).
@@ -240,6 +247,13 @@ cudaError_t launch_train_many(const TrainJob* jobs, int njobs, const uint32_t* g
 // context about to be created on a device with num_sms SMs.
 size_t context_device_bytes(const nrc_context* c);
 size_t context_device_bytes_for(int num_sms);
+// The serving loop's jobs for one frame slot of a session's cache: the query of
+// the slot's records with the rendering weights, and the four chained training
+// steps on its train records (the last writing use_weights), as
+// nrc_infer_many / nrc_train_many build them. NRC_ERROR_INVALID_ARGUMENT for a
+// bf16 or fp8 cache (the loop's kernels are the fp16 forms).
+int loop_slot_jobs(nrc_context* ctx, const nrc_frame_buffers& f, uint32_t max_queries, uint32_t train_records,
+                   InferJob* infer, TrainJob* train);
 
 cudaError_t launch_encode(const nrc_input* in, const uint32_t* d_count, uint32_t capacity, uint16_t* out,
                           int num_sms, cudaStream_t stream);

@@ -26,17 +26,21 @@
 //   - sessions are admitted against a device-memory budget (cache state + frame
 //     slots), so the set of resident sessions never exceeds it.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
+#include <cstring>
 #include <deque>
 #include <mutex>
 #include <new>
+#include <set>
 #include <thread>
 #include <unordered_map>
 #include <vector>
 
 #include "nrc_common.cuh"
 #include "nrc_kernels.h"
+#include "nrc_server_loop.h"
 
 namespace {
 
@@ -130,6 +134,18 @@ struct nrc_server {
   bool stop = false;
   int worker_status = NRC_OK;
   std::thread worker;
+  // the device-resident loop (cfg.device_loop): no worker thread
+  bool device_loop = false;
+  nrc::LoopShared* shared = nullptr;      // pinned, host-mapped: the host's view
+  nrc::LoopShared* shared_dev = nullptr;  // the device's view
+  nrc::LoopDevice* ldev = nullptr;
+  nrc::LoopSlot* lslots = nullptr;        // kLoopMaxSessions x kLoopMaxSlots
+  nrc::LoopGraph lgraph;
+  cudaStream_t loop_stream = nullptr;
+  int64_t clock_offset = 0;  // device clock minus host clock, ns
+  std::unordered_map<uint64_t, std::pair<int64_t, uint32_t>> submitted_at;  // ticket -> (submit ns, session)
+  std::set<uint64_t> outstanding;  // submitted, completion not yet seen
+  uint64_t base_batches = 0, base_batched = 0;  // the loop's counters at the last stats reset
 };
 
 namespace {
@@ -283,6 +299,155 @@ void worker_main(nrc_server* S) {
 
 bool valid_session(nrc_server* S, uint32_t id) { return id < S->sessions.size() && S->sessions[id].open; }
 
+// A session's cache and frame slots (one allocation, `slots` bytes).
+int make_session(nrc_server* S, const nrc_session_desc* d, size_t slots, size_t bytes, Session* out) {
+  Session& s = *out;
+  s.desc = *d;
+  s.bytes = bytes;
+  s.train_ctas = d->train_ctas ? d->train_ctas : default_train_ctas(d->train_records, S->sms);
+  int st = nrc_create(&d->cache, &s.ctx);
+  if (st == NRC_OK && cudaMalloc(&s.block, slots) != cudaSuccess) st = NRC_ERROR_OUT_OF_MEMORY;
+  if (st == NRC_OK && cudaMemset(s.block, 0, slots) != cudaSuccess) st = NRC_ERROR_CUDA;
+  if (st != NRC_OK) return st;
+  uint8_t* p = static_cast<uint8_t*>(s.block);
+  for (uint32_t k = 0; k < d->frame_slots; ++k) {
+    nrc_frame_buffers f{};
+    f.queries = reinterpret_cast<nrc_input*>(p);
+    p += up256(size_t(d->max_queries) * sizeof(nrc_input));
+    f.query_count = reinterpret_cast<uint32_t*>(p);
+    for (int b = 0; b < NRC_TRAIN_BATCH_COUNT; ++b) f.train_count[b] = reinterpret_cast<uint32_t*>(p) + 4 + b;
+    p += 256;
+    f.out_rgb = reinterpret_cast<float*>(p);
+    p += up256(size_t(d->max_queries) * 3 * sizeof(float));
+    for (int b = 0; b < NRC_TRAIN_BATCH_COUNT; ++b) {
+      f.train[b] = reinterpret_cast<nrc_train_record*>(p);
+      p += up256(size_t(d->train_records) * sizeof(nrc_train_record));
+    }
+    p += 256;
+    s.slots.push_back(f);
+  }
+  s.open = true;
+  return NRC_OK;
+}
+
+// ------------------------------------------------------ device-resident loop --
+// Caller holds the lock for all of these.
+
+// Launches the loop unless a launch of it runs (called after a request was
+// published). A launch that is ending sees the request itself; launching once
+// more then only queues an idle pass behind it on the loop's stream.
+int loop_kick(nrc_server* S) {
+  std::atomic_thread_fence(std::memory_order_seq_cst);  // the published head before the read of `active`
+  if (S->shared->active != 0u) return NRC_OK;
+  S->shared->active = 1u;
+  return cudaGraphLaunch(S->lgraph.exec, S->loop_stream) == cudaSuccess ? NRC_OK : NRC_ERROR_CUDA;
+}
+
+// Every request written to the ring completes and the loop's launches end (so
+// that device memory can be allocated or freed: both may wait for the device).
+int loop_pause(nrc_server* S) {
+  S->shared->stop = 1u;
+  std::atomic_thread_fence(std::memory_order_seq_cst);
+  // bounded: the loop ends once the requests written have run (each kernel's
+  // own waits are bounded too)
+  const int64_t t0 = now_ns();
+  cudaError_t e = cudaStreamQuery(S->loop_stream);
+  while (e == cudaErrorNotReady && now_ns() - t0 < 60000000000ll) {
+    std::this_thread::sleep_for(std::chrono::microseconds(50));
+    e = cudaStreamQuery(S->loop_stream);
+  }
+  if (e == cudaErrorNotReady) return NRC_ERROR_DEVICE_TIMEOUT;  // still running: left as it is
+  S->shared->stop = 0u;
+  return e == cudaSuccess ? NRC_OK : NRC_ERROR_CUDA;
+}
+
+// Collects the completions the loop has published.
+void loop_poll(nrc_server* S) {
+  for (auto it = S->outstanding.begin(); it != S->outstanding.end();) {
+    const uint64_t t = *it;
+    const uint32_t k = static_cast<uint32_t>(t & (nrc::kLoopRing - 1));
+    if (S->shared->done_ticket[k] != t) {
+      ++it;
+      continue;
+    }
+    std::atomic_thread_fence(std::memory_order_acquire);  // the completion time was written first
+    const auto sub = S->submitted_at[t];
+    int64_t lat = static_cast<int64_t>(S->shared->done_ns[k]) - S->clock_offset - sub.first;
+    if (lat < 0) lat = 0;  // within the clock calibration's error
+    S->done[t] = lat;
+    S->latencies.push_back(lat);
+    S->submitted_at.erase(t);
+    if (sub.second < S->sessions.size()) --S->sessions[sub.second].pending;
+    ++S->completed;
+    it = S->outstanding.erase(it);
+  }
+}
+
+int loop_create(nrc_server* S) {
+  void* h = nullptr;
+  if (cudaHostAlloc(&h, sizeof(nrc::LoopShared), cudaHostAllocMapped) != cudaSuccess) return NRC_ERROR_OUT_OF_MEMORY;
+  std::memset(h, 0, sizeof(nrc::LoopShared));
+  S->shared = static_cast<nrc::LoopShared*>(h);
+  void* d = nullptr;
+  if (cudaHostGetDevicePointer(&d, h, 0) != cudaSuccess) return NRC_ERROR_CUDA;
+  S->shared_dev = static_cast<nrc::LoopShared*>(d);
+  const size_t slot_table = size_t(nrc::kLoopMaxSessions) * nrc::kLoopMaxSlots * sizeof(nrc::LoopSlot);
+  if (cudaMalloc(&S->ldev, sizeof(nrc::LoopDevice)) != cudaSuccess) return NRC_ERROR_OUT_OF_MEMORY;
+  if (cudaMalloc(&S->lslots, slot_table) != cudaSuccess) return NRC_ERROR_OUT_OF_MEMORY;
+  if (cudaMemset(S->ldev, 0, sizeof(nrc::LoopDevice)) != cudaSuccess ||
+      cudaMemset(S->lslots, 0, slot_table) != cudaSuccess)
+    return NRC_ERROR_CUDA;
+  if (cudaStreamCreateWithFlags(&S->loop_stream, cudaStreamNonBlocking) != cudaSuccess) return NRC_ERROR_CUDA;
+  if (nrc::loop_calibrate(S->shared, S->shared_dev, S->loop_stream, now_ns, &S->clock_offset) != cudaSuccess)
+    return NRC_ERROR_CUDA;
+  const uint32_t sms = static_cast<uint32_t>(std::min(S->sms, 152));
+  const uint32_t kIdlePollNs = 200000;  // a launch of the loop ends after 200 us without requests
+  // the training launch node with the cooperative attribute; without it if the
+  // graph cannot hold one (its groups still fit on the SMs at once)
+  cudaError_t e = nrc::loop_build(S->shared_dev, S->ldev, S->lslots, S->cfg.max_batch_sessions, sms, kIdlePollNs,
+                                  true, &S->lgraph);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    e = nrc::loop_build(S->shared_dev, S->ldev, S->lslots, S->cfg.max_batch_sessions, sms, kIdlePollNs, false,
+                        &S->lgraph);
+  }
+  return e == cudaSuccess ? NRC_OK : NRC_ERROR_CUDA;  // the first request launches the loop
+}
+
+void loop_free(nrc_server* S) {
+  nrc::loop_destroy(&S->lgraph);
+  if (S->loop_stream) cudaStreamDestroy(S->loop_stream);
+  if (S->lslots) cudaFree(S->lslots);
+  if (S->ldev) cudaFree(S->ldev);
+  if (S->shared) cudaFreeHost(S->shared);
+  S->loop_stream = nullptr;
+  S->lslots = nullptr;
+  S->ldev = nullptr;
+  S->shared = nullptr;
+}
+
+// The session's slots as the loop reads them (or zeros: no longer valid).
+int loop_write_slots(nrc_server* S, uint32_t id, const Session* s) {
+  std::vector<nrc::LoopSlot> rows(nrc::kLoopMaxSlots);
+  std::memset(static_cast<void*>(rows.data()), 0, rows.size() * sizeof(nrc::LoopSlot));
+  if (s != nullptr) {
+    for (uint32_t k = 0; k < s->slots.size(); ++k) {
+      nrc::LoopSlot& r = rows[k];
+      const int st = nrc::loop_slot_jobs(s->ctx, s->slots[k], s->desc.max_queries, s->desc.train_records, &r.infer,
+                                         &r.train);
+      if (st != NRC_OK) return st;
+      r.train_ctas = s->train_ctas;
+      r.query_tiles = (s->desc.max_queries + nrc::kTile - 1) / nrc::kTile;
+      r.query_cap = std::max(1u, nrc::infer_grid(s->desc.max_queries, std::min(S->sms, 152)));
+      r.valid = 1u;
+    }
+  }
+  return cudaMemcpy(S->lslots + size_t(id) * nrc::kLoopMaxSlots, rows.data(), rows.size() * sizeof(nrc::LoopSlot),
+                    cudaMemcpyHostToDevice) == cudaSuccess
+             ? NRC_OK
+             : NRC_ERROR_CUDA;
+}
+
 }  // namespace
 
 extern "C" {
@@ -320,6 +485,19 @@ int nrc_server_create(const nrc_server_config* cfg, nrc_server** out) {
     delete S;
     return NRC_ERROR_CUDA;
   }
+  if (cfg->device_loop != 0) {
+    S->device_loop = true;
+    const int st = loop_create(S);
+    if (st != NRC_OK) {
+      loop_free(S);
+      cudaEventDestroy(S->train_tail);
+      for (cudaStream_t x : S->streams) cudaStreamDestroy(x);
+      delete S;
+      return st;
+    }
+    *out = S;
+    return NRC_OK;
+  }
   S->worker = std::thread(worker_main, S);
   *out = S;
   return NRC_OK;
@@ -333,6 +511,11 @@ int nrc_server_destroy(nrc_server* S) {
   }
   S->cv_work.notify_all();
   if (S->worker.joinable()) S->worker.join();
+  if (S->device_loop) {
+    std::lock_guard<std::mutex> lk(S->m);
+    if (loop_pause(S) != NRC_OK) S->worker_status = NRC_ERROR_CUDA;  // every written request completes first
+    loop_poll(S);
+  }
   for (cudaStream_t x : S->streams) cudaStreamSynchronize(x);
   for (Session& s : S->sessions) {
     if (!s.open) continue;
@@ -341,6 +524,7 @@ int nrc_server_destroy(nrc_server* S) {
   }
   for (cudaEvent_t e : S->free_events) cudaEventDestroy(e);
   cudaEventDestroy(S->train_tail);
+  if (S->device_loop) loop_free(S);
   for (cudaStream_t x : S->streams) cudaStreamDestroy(x);
   const int st = S->worker_status;
   delete S;
@@ -354,18 +538,36 @@ int nrc_server_open_session(nrc_server* S, const nrc_session_desc* d, uint32_t* 
     return NRC_ERROR_INVALID_ARGUMENT;
   const size_t slots = size_t(d->frame_slots) * slot_bytes(*d);
   const size_t bytes = slots + nrc::context_device_bytes_for(S->sms);
+  if (S->device_loop) {
+    // the loop pauses while the session's memory is allocated and its slots
+    // are written; submitters wait on the lock meanwhile
+    std::lock_guard<std::mutex> lk(S->m);
+    if (S->bytes_in_use + bytes > S->cfg.hbm_budget_bytes) return NRC_ERROR_OUT_OF_MEMORY;
+    uint32_t sid = 0;
+    while (sid < S->sessions.size() && S->sessions[sid].open) ++sid;
+    if (sid >= nrc::kLoopMaxSessions) return NRC_ERROR_INVALID_ARGUMENT;
+    int st = loop_pause(S);
+    Session s;
+    if (st == NRC_OK) st = make_session(S, d, slots, bytes, &s);
+    if (st == NRC_OK) st = loop_write_slots(S, sid, &s);
+    if (st == NRC_OK) {
+      if (sid == S->sessions.size()) S->sessions.emplace_back();
+      S->sessions[sid] = std::move(s);
+      S->bytes_in_use += bytes;
+      *id = sid;
+    } else {
+      if (s.ctx) nrc_destroy(s.ctx);
+      if (s.block) cudaFree(s.block);
+    }
+    return st;
+  }
   {
     std::lock_guard<std::mutex> lk(S->m);
     if (S->bytes_in_use + bytes > S->cfg.hbm_budget_bytes) return NRC_ERROR_OUT_OF_MEMORY;
     S->bytes_in_use += bytes;  // reserved while the session is built
   }
   Session s;
-  s.desc = *d;
-  s.bytes = bytes;
-  s.train_ctas = d->train_ctas ? d->train_ctas : default_train_ctas(d->train_records, S->sms);
-  int st = nrc_create(&d->cache, &s.ctx);
-  if (st == NRC_OK && cudaMalloc(&s.block, slots) != cudaSuccess) st = NRC_ERROR_OUT_OF_MEMORY;
-  if (st == NRC_OK && cudaMemset(s.block, 0, slots) != cudaSuccess) st = NRC_ERROR_CUDA;
+  const int st = make_session(S, d, slots, bytes, &s);
   if (st != NRC_OK) {
     if (s.ctx) nrc_destroy(s.ctx);
     if (s.block) cudaFree(s.block);
@@ -373,24 +575,6 @@ int nrc_server_open_session(nrc_server* S, const nrc_session_desc* d, uint32_t* 
     S->bytes_in_use -= bytes;
     return st;
   }
-  uint8_t* p = static_cast<uint8_t*>(s.block);
-  for (uint32_t k = 0; k < d->frame_slots; ++k) {
-    nrc_frame_buffers f{};
-    f.queries = reinterpret_cast<nrc_input*>(p);
-    p += up256(size_t(d->max_queries) * sizeof(nrc_input));
-    f.query_count = reinterpret_cast<uint32_t*>(p);
-    for (int b = 0; b < NRC_TRAIN_BATCH_COUNT; ++b) f.train_count[b] = reinterpret_cast<uint32_t*>(p) + 4 + b;
-    p += 256;
-    f.out_rgb = reinterpret_cast<float*>(p);
-    p += up256(size_t(d->max_queries) * 3 * sizeof(float));
-    for (int b = 0; b < NRC_TRAIN_BATCH_COUNT; ++b) {
-      f.train[b] = reinterpret_cast<nrc_train_record*>(p);
-      p += up256(size_t(d->train_records) * sizeof(nrc_train_record));
-    }
-    p += 256;
-    s.slots.push_back(f);
-  }
-  s.open = true;
   std::lock_guard<std::mutex> lk(S->m);
   for (uint32_t k = 0; k < S->sessions.size(); ++k)
     if (!S->sessions[k].open) {
@@ -406,6 +590,19 @@ int nrc_server_open_session(nrc_server* S, const nrc_session_desc* d, uint32_t* 
 int nrc_server_close_session(nrc_server* S, uint32_t id) {
   if (S == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
   Session s;
+  if (S->device_loop) {
+    std::lock_guard<std::mutex> lk(S->m);
+    if (!valid_session(S, id)) return NRC_ERROR_INVALID_ARGUMENT;
+    int st = loop_pause(S);  // every request written, this session's included, completes
+    loop_poll(S);
+    s = std::move(S->sessions[id]);
+    S->sessions[id] = Session{};
+    S->bytes_in_use -= s.bytes;
+    if (st == NRC_OK) st = loop_write_slots(S, id, nullptr);
+    nrc_destroy(s.ctx);
+    cudaFree(s.block);
+    return st;
+  }
   {
     std::unique_lock<std::mutex> lk(S->m);
     if (!valid_session(S, id)) return NRC_ERROR_INVALID_ARGUMENT;
@@ -437,6 +634,41 @@ int nrc_server_session_cache(nrc_server* S, uint32_t id, nrc_context** ctx) {
 
 int nrc_server_submit(nrc_server* S, uint32_t id, uint32_t slot, void* ready, uint64_t* ticket) {
   if (S == nullptr || ticket == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  if (S->device_loop) {
+    // the device cannot wait on a host-recorded event: the submitter does
+    if (ready != nullptr && cudaEventSynchronize(static_cast<cudaEvent_t>(ready)) != cudaSuccess)
+      return NRC_ERROR_CUDA;
+    std::unique_lock<std::mutex> lk(S->m);
+    if (S->stop || !valid_session(S, id) || slot >= S->sessions[id].slots.size()) return NRC_ERROR_INVALID_ARGUMENT;
+    // room in the ring, and no completion record reused before it is read
+    const int64_t t0 = now_ns();
+    for (;;) {
+      loop_poll(S);
+      const bool ring_full = S->shared->head - S->shared->tail >= nrc::kLoopRing;
+      const bool window_full = !S->outstanding.empty() && S->next_ticket - *S->outstanding.begin() >= nrc::kLoopRing;
+      if (!ring_full && !window_full) break;
+      if (now_ns() - t0 > 10000000000ll) return NRC_ERROR_DEVICE_TIMEOUT;
+      lk.unlock();
+      std::this_thread::sleep_for(std::chrono::microseconds(20));
+      lk.lock();
+    }
+    const uint64_t t = S->next_ticket++;
+    const unsigned long long h = S->shared->head;
+    nrc::LoopEntry& e = S->shared->ring[h & (nrc::kLoopRing - 1)];
+    e.session = id;
+    e.slot = slot;
+    e.ticket = t;
+    std::atomic_thread_fence(std::memory_order_seq_cst);  // the entry before the head that publishes it
+    S->shared->head = h + 1;
+    const int st = loop_kick(S);
+    if (st != NRC_OK) return st;
+    S->submitted_at[t] = {now_ns(), id};
+    S->outstanding.insert(t);
+    ++S->sessions[id].pending;
+    ++S->submitted;
+    *ticket = t;
+    return NRC_OK;
+  }
   {
     std::lock_guard<std::mutex> lk(S->m);
     if (S->stop || !valid_session(S, id) || slot >= S->sessions[id].slots.size()) return NRC_ERROR_INVALID_ARGUMENT;
@@ -452,6 +684,32 @@ int nrc_server_submit(nrc_server* S, uint32_t id, uint32_t slot, void* ready, ui
 
 int nrc_server_wait(nrc_server* S, uint64_t ticket, double timeout_ms, double* latency_ms) {
   if (S == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
+  if (S->device_loop) {
+    const int64_t t0 = now_ns();
+    std::unique_lock<std::mutex> lk(S->m);
+    if (ticket == 0 || ticket >= S->next_ticket) return NRC_ERROR_INVALID_ARGUMENT;
+    for (;;) {
+      if (S->done.count(ticket) == 0) loop_poll(S);
+      if (S->done.count(ticket) != 0) break;
+      if (S->outstanding.count(ticket) == 0) return NRC_ERROR_INVALID_ARGUMENT;  // already waited for
+      if (timeout_ms >= 0 && double(now_ns() - t0) * 1e-6 > timeout_ms) return NRC_ERROR_DEVICE_TIMEOUT;
+      // a request left in the ring with no launch of the loop running (should
+      // the two sides' flags have crossed): launch it again
+      if (now_ns() - t0 > 2000000 && cudaStreamQuery(S->loop_stream) == cudaSuccess &&
+          S->shared->tail != S->shared->head) {
+        S->shared->active = 0u;
+        const int st = loop_kick(S);
+        if (st != NRC_OK) return st;
+      }
+      lk.unlock();
+      std::this_thread::sleep_for(std::chrono::microseconds(5));
+      lk.lock();
+    }
+    const int64_t ns = S->done[ticket];
+    S->done.erase(ticket);
+    if (latency_ms) *latency_ms = double(ns) * 1e-6;
+    return S->worker_status;
+  }
   std::unique_lock<std::mutex> lk(S->m);
   if (ticket == 0 || ticket >= S->next_ticket) return NRC_ERROR_INVALID_ARGUMENT;
   auto ready = [&] { return S->done.count(ticket) != 0; };
@@ -469,6 +727,11 @@ int nrc_server_wait(nrc_server* S, uint64_t ticket, double timeout_ms, double* l
 int nrc_server_get_stats(nrc_server* S, nrc_server_stats* st, int reset) {
   if (S == nullptr || st == nullptr) return NRC_ERROR_INVALID_ARGUMENT;
   std::lock_guard<std::mutex> lk(S->m);
+  if (S->device_loop) {
+    loop_poll(S);
+    S->batches = S->shared->batches - S->base_batches;
+    S->batched_requests = S->shared->batched_requests - S->base_batched;
+  }
   st->submitted = S->submitted;
   st->completed = S->completed;
   st->batches = S->batches;
@@ -482,6 +745,10 @@ int nrc_server_get_stats(nrc_server* S, nrc_server_stats* st, int reset) {
     S->latencies.clear();
     S->batches = 0;
     S->batched_requests = 0;
+    if (S->device_loop) {
+      S->base_batches = S->shared->batches;
+      S->base_batched = S->shared->batched_requests;
+    }
   }
   return S->worker_status;
 }

@@ -223,12 +223,17 @@ __device__ __forceinline__ bool grid_sync(uint32_t* counter, uint32_t target, ui
 // grid.
 // kBF16: weights, activations and gradients in bf16 instead of fp16 (the master
 // weights and moments are fp32 either way).
-template <int N, bool kBF16>
-__global__ void __launch_bounds__(kTrainThreads, 1) train_steps_kernel(const __grid_constant__ TrainLaunch<N> L) {
+// kTable: the launch's parameters come from a table in global memory (the
+// serving loop's batches) instead of the kernel parameters; CTAs past the
+// table's groups return at once (they belong to no group's barrier).
+template <int N, bool kBF16, bool kTable>
+__device__ __forceinline__ void train_body(const TrainLaunch<N>& L) {
+  if (kTable && blockIdx.x >= L.group_start[L.njobs]) return;
   int job = 0;
   while (job + 1 < L.njobs && blockIdx.x >= L.group_start[job + 1]) ++job;
   const TrainParams& P = L.job[job].p;
   const CUtensorMap& wmap = L.job[job].wmap;
+  if (kTable && threadIdx.x == 0) tensormap_acquire(&wmap);  // thread 0 issues the weight copies
   const uint32_t G = L.group_start[job + 1] - L.group_start[job];  // CTAs of this cache
   const uint32_t rank = blockIdx.x - L.group_start[job];           // this CTA within them
   extern __shared__ uint8_t smem_raw[];
@@ -724,6 +729,17 @@ __global__ void __launch_bounds__(kTrainThreads, 1) train_steps_kernel(const __g
   }
 }
 
+template <int N, bool kBF16>
+__global__ void __launch_bounds__(kTrainThreads, 1) train_steps_kernel(const __grid_constant__ TrainLaunch<N> L) {
+  train_body<N, kBF16, false>(L);
+}
+
+// The batched training over a launch table in global memory.
+__global__ void __launch_bounds__(kTrainThreads, 1)
+    train_table_kernel(const TrainLaunch<kMaxTrainJobs>* __restrict__ L) {
+  train_body<kMaxTrainJobs, false, true>(*L);
+}
+
 template <int N>
 cudaError_t launch(const TrainLaunch<N>& L, uint32_t grid, cudaStream_t stream, bool bf16) {
   // Cooperative (the grid barrier needs every CTA resident) and a programmatic
@@ -749,12 +765,13 @@ cudaError_t launch(const TrainLaunch<N>& L, uint32_t grid, cudaStream_t stream, 
 }  // namespace
 
 cudaError_t configure_train_kernels() {
-  const void* k[4] = {reinterpret_cast<const void*>(train_steps_kernel<1, false>),
+  const void* k[5] = {reinterpret_cast<const void*>(train_steps_kernel<1, false>),
                       reinterpret_cast<const void*>(train_steps_kernel<kMaxTrainJobs, false>),
                       reinterpret_cast<const void*>(train_steps_kernel<1, true>),
-                      reinterpret_cast<const void*>(train_steps_kernel<kMaxTrainJobs, true>)};
+                      reinterpret_cast<const void*>(train_steps_kernel<kMaxTrainJobs, true>),
+                      reinterpret_cast<const void*>(train_table_kernel)};
   cudaError_t e = cudaSuccess;
-  for (int i = 0; i < 4 && e == cudaSuccess; ++i)
+  for (int i = 0; i < 5 && e == cudaSuccess; ++i)
     if ((e = cudaFuncSetAttribute(k[i], cudaFuncAttributeMaxDynamicSharedMemorySize, kTrainSmemBytes)) == cudaSuccess)
       e = cudaFuncSetAttribute(k[i], cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
   return e;
@@ -779,6 +796,21 @@ cudaError_t launch_train(const TrainParams& p, const CUtensorMap* wmap, int max_
   L.group_start[1] = grid;
   L.njobs = 1;
   return launch(L, grid, stream, p.bf16 != 0);
+}
+
+cudaError_t launch_train_table(const TrainLaunch<kMaxTrainJobs>* table, uint32_t grid, bool cooperative,
+                               cudaStream_t stream) {
+  cudaLaunchAttribute attr;
+  attr.id = cudaLaunchAttributeCooperative;
+  attr.val.cooperative = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(kTrainThreads);
+  cfg.dynamicSmemBytes = kTrainSmemBytes;
+  cfg.stream = stream;
+  cfg.attrs = &attr;
+  cfg.numAttrs = cooperative ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, train_table_kernel, table);
 }
 
 cudaError_t launch_train_many(const TrainJob* jobs, int njobs, const uint32_t* group_size, cudaStream_t stream) {

@@ -108,6 +108,13 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const void* tmap, int32_t
 // Programmatic dependent launch: wait for the preceding grid's completion (and
 // memory), and allow the next grid in the stream to begin launching.
 __device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+// A tensor map in global memory that generic stores wrote (in an earlier
+// kernel): made visible to the tensor-map proxy before this thread's first
+// bulk tensor copy with it.
+__device__ __forceinline__ void tensormap_acquire(const void* map) {
+  asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(map) : "memory");
+}
 __device__ __forceinline__ void griddep_launch_dependents() {
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }

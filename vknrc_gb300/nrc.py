@@ -124,7 +124,7 @@ class TrainJob(ctypes.Structure):
 
 class ServerConfig(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("max_batch_sessions", ctypes.c_uint32),
-                ("max_inflight_batches", ctypes.c_uint32)]
+                ("max_inflight_batches", ctypes.c_uint32), ("device_loop", ctypes.c_uint32)]
 
 
 class SessionDesc(ctypes.Structure):
@@ -600,10 +600,12 @@ def device_view(ptr: int, shape, dtype):
 
 class Server:
     """nrc_server: device-resident sessions whose frame requests are batched
-    continuously by a worker thread inside libnrc.so."""
+    continuously, by a worker thread inside libnrc.so or (device_loop=True) by
+    a loop that runs on the GPU."""
 
-    def __init__(self, hbm_budget_bytes: int, max_batch_sessions: int = 32, max_inflight_batches: int = 2):
-        cfg = ServerConfig(hbm_budget_bytes, max_batch_sessions, max_inflight_batches)
+    def __init__(self, hbm_budget_bytes: int, max_batch_sessions: int = 32, max_inflight_batches: int = 2,
+                 device_loop: bool = False):
+        cfg = ServerConfig(hbm_budget_bytes, max_batch_sessions, max_inflight_batches, 1 if device_loop else 0)
         h = ctypes.c_void_p()
         check(lib().nrc_server_create(ctypes.byref(cfg), ctypes.byref(h)), "nrc_server_create")
         self.h = h
