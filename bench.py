@@ -779,7 +779,7 @@ def serving_leg(evals, trains, seconds=2.0, sessions=32, rate=2000.0, budget=40 
         raise RuntimeError(f"device error in the serving leg: {errs}")
     sat_fps = m / wall_sat
     sat_q = sum(res[k % sessions][0] * res[k % sessions][1] for k in range(m))
-    out = {
+    report = {
         "workload": "32 sessions (720p/1080p/1440p drawn from a seeded generator), Poisson arrivals at 2000 req/s, "
                     "request = query of the frame's records + 4 x 16,384-record training steps; 40 GB budget",
         "loop": ("on the GPU: CUDA graph while node (scheduler kernel, batched query, batched training, completion "
@@ -802,7 +802,7 @@ def serving_leg(evals, trains, seconds=2.0, sessions=32, rate=2000.0, budget=40 
                        "mean_batch_sessions": st_sat["mean_batch_sessions"]},
     }
     if device_loop:
-        return out
+        return report
     # one request at a time through nrc_frame (the fused single-cache path, same mix of resolutions)
     mix = [res[i] for i in who[:96]]
     solo = {}
@@ -823,11 +823,11 @@ def serving_leg(evals, trains, seconds=2.0, sessions=32, rate=2000.0, budget=40 
             torch.cuda.synchronize()
             solo[(w, h)] = s.elapsed_time(e) / 1e3 / 20
     solo_fps = len(mix) / sum(solo[r] for r in mix)
-    out["single_request_path"] = {"frames_per_s": solo_fps,
+    report["single_request_path"] = {"frames_per_s": solo_fps,
                                   "what": "one request at a time through nrc_frame (fused single-cache path), "
                                           "same resolution mix"}
-    out["saturation_vs_single_request"] = sat_fps / solo_fps
-    return out
+    report["saturation_vs_single_request"] = sat_fps / solo_fps
+    return report
 
 
 PACKED_EVAL_BYTES = 20   # nrc_eval_record
