@@ -186,3 +186,34 @@ def test_device_loop_matches_host_worker_and_rejects_other_formats(cuda):
         assert np.array_equal(res[0][0][k], res[1][0][k]), k
     assert np.array_equal(res[0][1], res[1][1])
     assert np.array_equal(res[0][2], res[1][2])
+
+
+@pytest.mark.parametrize("device_loop", [False, True])
+def test_sessions_open_and_close_while_another_runs(cuda, device_loop):
+    """Sessions opened and closed (their memory allocated and freed, which
+    pauses the device loop) while another session's frames are in flight: the
+    running session's results equal its results alone."""
+    import threading
+
+    from vknrc_gb300 import nrc
+
+    frames = 4
+    seed, q, r = SPECS["c"]
+    with nrc.Server(4 * GB, device_loop=device_loop) as srv:
+        sa = srv.open_session(q, r, seed=seed)
+        alone = _run_session_frames(srv, sa, SPECS["c"], frames)
+    with nrc.Server(4 * GB, device_loop=device_loop) as srv:
+        sa = srv.open_session(q, r, seed=seed)
+        out = {}
+        t = threading.Thread(target=lambda: out.__setitem__("a", _run_session_frames(srv, sa, SPECS["c"], frames)))
+        t.start()
+        for k in range(3):
+            sb = srv.open_session(20000, 2048, seed=70 + k)
+            v = srv.frame_views(sb, 0, 20000, 2048)
+            ev = _fill(v, *_frame(70 + k, 0, 20000, 2048))
+            srv.wait(srv.submit(sb, 0, ev), 60000)
+            srv.close_session(sb)
+        t.join()
+        for k in range(frames):
+            assert np.array_equal(out["a"][k], alone[k]), k
+        assert srv.cache(sa).error() == 0
