@@ -77,7 +77,7 @@ def _state_tuple(st):
 
 
 def train_golden(ref):
-    """Golden vectors of the training shaders (BASELINE config 1's records: 16,384
+    """Golden vectors of the training shaders (the single-step training case: 16,384
     records, lognormal(0, 1.5) targets, He weights)."""
     rng = S.rng_for(20240224, 0, 0)
     # --- prepare: every count from the initial state and from a state 7 steps in
@@ -94,7 +94,7 @@ def train_golden(ref):
             prep_n.append(n)
             prep_groups.append(g)
     prep_counts = np.array(PREP_COUNTS * 2, np.uint32)
-    # --- config 1: He weights, 16,384 records with lognormal(0, 1.5) targets
+    # --- the single-step case: He weights, 16,384 records with lognormal(0, 1.5) targets
     n = 16384
     w32 = rng.normal(0.0, np.sqrt(2.0 / 64.0), O.P).astype(np.float32)
     w16 = w32.astype(np.float16).view(np.uint16)
@@ -102,7 +102,7 @@ def train_golden(ref):
     enc = O.encode(rec[:, 6:])
     pred = O.forward_f32(w16, enc, nthreads=8)  # unclamped outputs, as the gradient pass uses them
     grad = O.train_grad(w16, enc, rec[:, :3], mode=0, nthreads=8)[0].astype(np.float32)
-    # --- loss rows: config 1's (prediction, target) pairs, then edge pairs
+    # --- loss rows: that case's (prediction, target) pairs, then edge pairs
     edge_p = np.array([[0, 0, 0], [-1, -2, -3], [0.5, -0.5, 2.0], [1e-3, 1e-3, 1e-3], [100, 100, 100],
                        [0, 0, 0], [0, 0, 0], [-5, 0.25, 0.0], [3e4, -3e4, 1.0], [0.1, 0.2, 0.3]], np.float32)
     edge_t = np.array([[0, 0, 0], [1, 2, 3], [0.5, 0.5, 0.5], [400.0, 1.0, 0.0], [0, 0, 0],
@@ -111,7 +111,7 @@ def train_golden(ref):
     loss_pred = np.concatenate([pred, edge_p])
     loss_target = np.concatenate([rec[:, :3], edge_t])
     loss_rows = O.ref_loss_rows(loss_pred, loss_target, 1.0)
-    # --- optimizer: step 1 from the He initialisation on config 1's gradient
+    # --- optimizer: step 1 from the He initialisation on that case's gradient
     st1 = O.OptState(0, 1.0, 1.0, 1.0, 0.0)
     O.ref_prepare(n, st1)
     e_he = np.zeros((O.P, 4), np.float32)

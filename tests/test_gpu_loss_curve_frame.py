@@ -1,4 +1,4 @@
-"""BASELINE config 2's training at its own batch: 1000 online frames, each with
+"""The online-training loss curve at the frame's own batch: 1000 frames, each with
 four chained training steps of 16,384 freshly drawn records (nrc_train_batches:
 one launch per frame, as the reference's frame schedule runs its four train
 passes, src/rg/NRCRenderGraph.cpp:57-80), lr 1e-3, beta 0.9 / 0.99, eps 1e-8.

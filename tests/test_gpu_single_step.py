@@ -1,4 +1,4 @@
-"""BASELINE config 1 exactly, on the GPU: He-initialised weights, 16,384 train
+"""The single-step training case on the GPU: He-initialised weights, 16,384 train
 records with lognormal(0, 1.5) targets, one Adam step at lr 1e-3, beta 0.9 /
 0.99, eps 1e-8, then 65,536 queries from the same distributions.
 
@@ -34,7 +34,7 @@ def overflow_rows(oracle, w16, rec):
     return np.isinf(h.view(np.float16)).any(1)
 
 
-def test_config1_train_step_and_query(cuda, oracle):
+def test_single_step_train_and_query(cuda, oracle):
     import torch
     from vknrc_gb300 import Cache, synthetic as S
 

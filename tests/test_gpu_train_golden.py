@@ -26,7 +26,7 @@ def state_tuple(t):
     return (int(t[0]), *(float(np.float32(x)) for x in t[1:]))
 
 
-def test_optimize_first_step_config1_vs_reference(cuda):
+def test_optimize_first_step_vs_reference(cuda):
     tg = dict(np.load(TG.GOLDEN))
     e_in = np.zeros((20672, 4), np.float32)
     e_in[:, 2] = tg["he_w32"]
@@ -86,19 +86,19 @@ def test_prepare_vs_reference(cuda, k):
                 np.testing.assert_array_equal(c.get_weights(1), w0)
 
 
-@pytest.mark.parametrize("part", ["config1", "edges"])
+@pytest.mark.parametrize("part", ["records", "edges"])
 def test_loss_rows_vs_reference(cuda, part):
     import torch
     from vknrc_gb300 import nrc
 
     tg = dict(np.load(TG.GOLDEN))
-    sl = slice(0, 16384) if part == "config1" else slice(16384, None)
+    sl = slice(0, 16384) if part == "records" else slice(16384, None)
     p, t = tg["loss_pred"][sl], tg["loss_target"][sl]
     rows = torch.zeros((p.shape[0], 2), dtype=torch.int32, device="cuda")
     nrc.loss_gradient(dev(p), dev(t), count(p.shape[0]), rows)
     got = host(rows).view(np.uint32)
     TG.check_loss_rows(got, tg["loss_rows"][sl])
-    if part == "config1":
+    if part == "records":
         assert np.isinf(TG.f16_words(got)).any()  # the lognormal(0, 1.5) tail overflows as in the reference
 
 
@@ -115,7 +115,7 @@ def test_loss_rows_bf16_vs_oracle(cuda, oracle):
 
 def test_fused_step_equals_gradient_then_optimize(cuda):
     """nrc_train (one fused launch) gives exactly what nrc_gradient followed by
-    nrc_optimize gives on the same records (BASELINE config 1's: lognormal(0, 1.5)
+    nrc_optimize gives on the same records (16,384 records with lognormal(0, 1.5)
     targets, whose fp16 overflow the optimizer scrubs)."""
     import torch
     from vknrc_gb300 import Cache, synthetic as S

@@ -3,8 +3,8 @@
 tests/golden/train_golden.npz holds the outputs of nrc_train_prepare.comp,
 nrc_optimize.comp and NN_nv.glsl's NNLoadDA3_RelativeL2LuminanceLoss compiled
 from the reference tree as C++ (oracle/ref/ref_train.cpp, made by
-tests/golden/make_golden.py) on BASELINE config 1's records (16,384 records,
-lognormal(0, 1.5) targets, He weights) and on edge cases.
+tests/golden/make_golden.py) on the single-step training case's records (16,384
+records, lognormal(0, 1.5) targets, He weights) and on edge cases.
 
 Tolerances. GLSL lets a compiler contract a*b + c into one fused multiply-add;
 the reference's code compiled here keeps every product rounded, while the oracle
@@ -110,12 +110,12 @@ def test_prepare_dispatch_size(tg):
     assert np.array_equal(tg["prep_groups"], (tg["prep_n"].astype(np.int64) + 127) // 128)
 
 
-def test_loss_rows_config1(tg):
+def test_loss_rows_single_step(tg):
     n = 16384
     got = O.loss_rows(tg["loss_pred"][:n], tg["loss_target"][:n], 1.0)
     same = check_loss_rows(got, tg["loss_rows"][:n])
     assert same > 0.999
-    # config 1's lognormal(0, 1.5) tail overflows fp16 in the reference
+    # the lognormal(0, 1.5) tail overflows fp16 in the reference
     assert np.isinf(f16_words(tg["loss_rows"][:n])).any()
 
 
@@ -130,7 +130,7 @@ def _optimizer(tg, entries_in, st):
     return opt
 
 
-def test_optimize_first_step_config1(tg):
+def test_optimize_first_step(tg):
     e_in = np.zeros((O.P, 4), np.float32)
     e_in[:, 2] = tg["he_w32"]
     e_in[:, 3] = tg["he_w32"]
