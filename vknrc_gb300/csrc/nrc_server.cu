@@ -660,14 +660,12 @@ int nrc_server_submit(nrc_server* S, uint32_t id, uint32_t slot, void* ready, ui
     e.ticket = t;
     std::atomic_thread_fence(std::memory_order_seq_cst);  // the entry before the head that publishes it
     S->shared->head = h + 1;
-    const int st = loop_kick(S);
-    if (st != NRC_OK) return st;
     S->submitted_at[t] = {now_ns(), id};
     S->outstanding.insert(t);
     ++S->sessions[id].pending;
     ++S->submitted;
     *ticket = t;
-    return NRC_OK;
+    return loop_kick(S);  // on failure the request stays in the ring for the next launch
   }
   {
     std::lock_guard<std::mutex> lk(S->m);
