@@ -830,6 +830,7 @@ def serving_leg(evals, trains, seconds=2.0, sessions=32, rate=2000.0, budget=40 
     return report
 
 
+E2E_SETS = 3  # device buffer sets of the end-to-end pipelines (copies of one frame overlap the others' work)
 PACKED_EVAL_BYTES = 20   # nrc_eval_record
 PACKED_TRAIN_BYTES = 40  # nrc_packed_train_record
 
@@ -906,19 +907,19 @@ def packed_leg(cache, stream, E, world, frames=4):
     # end to end with host buffers
     h_ev = [t.pin_memory() for t in ev_h[:2]]
     h_tr = [[t.pin_memory() for t in f] for f in tr_h[:2]]
-    d_ev = [torch.empty_like(ev_d[0]) for _ in range(2)]
-    d_tr = [[torch.empty_like(tr_d[0][0]) for _ in range(B)] for _ in range(2)]
-    d_out = [out, torch.empty_like(out)]
-    h_out = [torch.empty((Q, 3), dtype=torch.float32).pin_memory() for _ in range(2)]
+    d_ev = [torch.empty_like(ev_d[0]) for _ in range(E2E_SETS)]
+    d_tr = [[torch.empty_like(tr_d[0][0]) for _ in range(B)] for _ in range(E2E_SETS)]
+    d_out = [out] + [torch.empty_like(out) for _ in range(E2E_SETS - 1)]
+    h_out = [torch.empty((Q, 3), dtype=torch.float32).pin_memory() for _ in range(E2E_SETS)]
     h2d = Q * PACKED_EVAL_BYTES + B * R * PACKED_TRAIN_BYTES
     d2h = Q * OUT_BYTES
     up_s, down_s = torch.cuda.Stream(), torch.cuda.Stream()
-    ev_up = [torch.cuda.Event() for _ in range(2)]
-    ev_done = [torch.cuda.Event() for _ in range(2)]
-    ev_back = [torch.cuda.Event() for _ in range(2)]
+    ev_up = [torch.cuda.Event() for _ in range(E2E_SETS)]
+    ev_done = [torch.cuda.Event() for _ in range(E2E_SETS)]
+    ev_back = [torch.cuda.Event() for _ in range(E2E_SETS)]
 
     def e2e_frame(k):
-        j = k % 2
+        j = k % E2E_SETS
         with torch.cuda.stream(up_s):
             up_s.wait_event(ev_done[j])
             d_ev[j].copy_(h_ev[k % 2], non_blocking=True)
@@ -934,7 +935,7 @@ def packed_leg(cache, stream, E, world, frames=4):
             h_out[j].copy_(d_out[j], non_blocking=True)
             ev_back[j].record(down_s)
 
-    for j in range(2):
+    for j in range(E2E_SETS):
         ev_done[j].record(stream)
         ev_back[j].record(stream)
     for k in range(3):
@@ -956,8 +957,8 @@ def packed_leg(cache, stream, E, world, frames=4):
         "e2e": {"value": world * Q * E / e2e_s, "unit": "queries/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "steps": E, "call": "nrc_frame_packed",
                 "schedule": "the reference's record formats (20-byte eval records, 40-byte train records) of a "
-                            "522,254-triangle scene resident on the device; pinned host buffers, frame k's H2D "
-                            "overlapping frame k-1's compute and frame k-2's D2H"},
+                            "522,254-triangle scene resident on the device; pinned host buffers, three device "
+                            "buffer sets: frame k's H2D overlapping earlier frames' compute and D2H"},
         "frame_packed": {"ms_per_frame": frame_s * 1e3, "queries_per_s": Q / frame_s,
                          "train_records_per_s": B * R / frame_s, "frames": K,
                          "what": "nrc_frame_packed with resident inputs (4 record frames rotated, L2-cold): "
@@ -1025,33 +1026,33 @@ def ours_arm(args, world, rank, local):
 
     # end to end through the C ABI with host buffers: H2D of each frame's records
     # from pinned memory, the frame, D2H of the query results. Frames are
-    # pipelined over two device buffer sets: frame k's upload (copy stream) runs
-    # while frame k-1 computes and frame k-2's results come back (second copy
-    # stream), as a host-fed renderer would schedule them.
+    # pipelined over E2E_SETS device buffer sets: frame k's upload (copy
+    # stream) runs while earlier frames compute and their results come back
+    # (second copy stream), as a host-fed renderer would schedule them.
     E = max(1, min(args.e2e_steps, K))
     h_eval = [evals[f].cpu().pin_memory() for f in range(min(2, len(evals)))]
     h_train = [[t.cpu().pin_memory() for t in trains[f]] for f in range(min(2, len(trains)))]
-    d_eval = [torch.empty_like(evals[0]) for _ in range(2)]
-    d_train = [[torch.empty_like(trains[0][0]) for _ in range(B)] for _ in range(2)]
-    d_out = [out, torch.empty_like(out)]
-    h_out = [torch.empty((Q, 3), dtype=torch.float32).pin_memory() for _ in range(2)]
+    d_eval = [torch.empty_like(evals[0]) for _ in range(E2E_SETS)]
+    d_train = [[torch.empty_like(trains[0][0]) for _ in range(B)] for _ in range(E2E_SETS)]
+    d_out = [out] + [torch.empty_like(out) for _ in range(E2E_SETS - 1)]
+    h_out = [torch.empty((Q, 3), dtype=torch.float32).pin_memory() for _ in range(E2E_SETS)]
     h2d = Q * EVAL_BYTES + B * R * TRAIN_BYTES
     d2h = Q * OUT_BYTES
     up_s, down_s = torch.cuda.Stream(), torch.cuda.Stream()
-    ev_up = [torch.cuda.Event() for _ in range(2)]       # buffer set holds frame k's inputs
-    ev_done = [torch.cuda.Event() for _ in range(2)]     # frame k computed (inputs free, outputs ready)
-    ev_back = [torch.cuda.Event() for _ in range(2)]     # frame k's outputs are on the host
+    ev_up = [torch.cuda.Event() for _ in range(E2E_SETS)]    # buffer set holds frame k's inputs
+    ev_done = [torch.cuda.Event() for _ in range(E2E_SETS)]  # frame k computed (inputs free, outputs ready)
+    ev_back = [torch.cuda.Event() for _ in range(E2E_SETS)]  # frame k's outputs are on the host
 
     def e2e_frame(k):
-        j = k % 2
+        j = k % E2E_SETS
         with torch.cuda.stream(up_s):
-            up_s.wait_event(ev_done[j])  # frame k-2 no longer reads this set
+            up_s.wait_event(ev_done[j])  # the set's previous frame no longer reads it
             d_eval[j].copy_(h_eval[k % len(h_eval)], non_blocking=True)
             for b in range(B):
                 d_train[j][b].copy_(h_train[k % len(h_train)][b], non_blocking=True)
             ev_up[j].record(up_s)
         stream.wait_event(ev_up[j])
-        stream.wait_event(ev_back[j])  # frame k-2's results have left d_out[j]
+        stream.wait_event(ev_back[j])  # the set's previous results have left d_out[j]
         cache.frame_overlapped(d_eval[j], eval_cnt, d_out[j], d_train[j], train_cnt)
         ev_done[j].record(stream)
         with torch.cuda.stream(down_s):
@@ -1059,7 +1060,7 @@ def ours_arm(args, world, rank, local):
             h_out[j].copy_(d_out[j], non_blocking=True)
             ev_back[j].record(down_s)
 
-    for j in range(2):
+    for j in range(E2E_SETS):
         ev_done[j].record(stream)
         ev_back[j].record(stream)
     for k in range(3):
@@ -1158,9 +1159,9 @@ def ours_arm(args, world, rank, local):
         "e2e_unpacked_records": {"value": world * Q * E / e2e_s, "unit": "queries/s", "h2d_bytes_per_step": h2d,
                                  "d2h_bytes_per_step": d2h, "steps": E, "call": "nrc_frame_overlapped",
                                  "schedule": "56-byte unpacked records (nrc_input) and 80-byte train records; pinned "
-                                             "host buffers, frame k's H2D overlapping frame k-1's compute and frame "
-                                             "k-2's D2H (bounded by the host-to-device link: 121 MB per frame at "
-                                             "about 210 GB/s)"},
+                                             "host buffers, three device buffer sets: frame k's H2D overlapping "
+                                             "earlier frames' compute and D2H (bounded by the host-to-device link: "
+                                             "121 MB per frame at about 210 GB/s)"},
         "frame_packed": packed["frame_packed"],
         "query_packed_alone_ms": packed["query_packed_alone_ms"],
         "unpack_eval_us": packed["unpack_eval_us"],
