@@ -830,7 +830,7 @@ def serving_leg(evals, trains, seconds=2.0, sessions=32, rate=2000.0, budget=40 
     return report
 
 
-E2E_SETS = 3  # device buffer sets of the end-to-end pipelines (copies of one frame overlap the others' work)
+E2E_SETS = 2  # device buffer sets of the end-to-end pipelines (three measured no faster)
 PACKED_EVAL_BYTES = 20   # nrc_eval_record
 PACKED_TRAIN_BYTES = 40  # nrc_packed_train_record
 
@@ -957,8 +957,9 @@ def packed_leg(cache, stream, E, world, frames=4):
         "e2e": {"value": world * Q * E / e2e_s, "unit": "queries/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "steps": E, "call": "nrc_frame_packed",
                 "schedule": "the reference's record formats (20-byte eval records, 40-byte train records) of a "
-                            "522,254-triangle scene resident on the device; pinned host buffers, three device "
-                            "buffer sets: frame k's H2D overlapping earlier frames' compute and D2H"},
+                            "522,254-triangle scene resident on the device; pinned host buffers, "
+                            f"{E2E_SETS} device buffer sets: frame k's H2D overlapping earlier frames' compute "
+                            "and D2H"},
         "frame_packed": {"ms_per_frame": frame_s * 1e3, "queries_per_s": Q / frame_s,
                          "train_records_per_s": B * R / frame_s, "frames": K,
                          "what": "nrc_frame_packed with resident inputs (4 record frames rotated, L2-cold): "
@@ -1159,9 +1160,9 @@ def ours_arm(args, world, rank, local):
         "e2e_unpacked_records": {"value": world * Q * E / e2e_s, "unit": "queries/s", "h2d_bytes_per_step": h2d,
                                  "d2h_bytes_per_step": d2h, "steps": E, "call": "nrc_frame_overlapped",
                                  "schedule": "56-byte unpacked records (nrc_input) and 80-byte train records; pinned "
-                                             "host buffers, three device buffer sets: frame k's H2D overlapping "
-                                             "earlier frames' compute and D2H (bounded by the host-to-device link: "
-                                             "121 MB per frame at about 210 GB/s)"},
+                                             f"host buffers, {E2E_SETS} device buffer sets: frame k's H2D "
+                                             "overlapping earlier frames' compute and D2H (bounded by the "
+                                             "host-to-device link: 121 MB per frame at about 210 GB/s)"},
         "frame_packed": packed["frame_packed"],
         "query_packed_alone_ms": packed["query_packed_alone_ms"],
         "unpack_eval_us": packed["unpack_eval_us"],
