@@ -72,3 +72,45 @@ def test_renderer_frames(cuda):
     assert np.all(np.isfinite(host(acc)))
     assert losses[-1] < losses[0], losses
     bvh.close()
+
+
+def test_traced_records_unpack_equal_through_scene_tables(cuda):
+    """The path tracer's own eval and train records unpack to the same inputs
+    bit for bit over the scene's gather tables as over its buffers."""
+    import torch
+
+    from vknrc_gb300 import nrc, synthetic as S
+
+    w, h = 128, 80
+    sc = S.terrain_scene(S.rng_for(5), n=64)
+    ds = nrc.DeviceScene(sc)
+    dt = nrc.DeviceScene(sc).prepare()
+    bvh = nrc.Bvh(ds)
+    buf = nrc.TraceBuffers(w, h)
+    P = nrc.TraceParams()
+    P.origin[:] = (0.0, 0.3, -1.9)
+    P.look[:] = (0.0, -0.25, 1.0)
+    P.side[:] = (0.8, 0.0, 0.0)
+    P.up[:] = (0.0, 0.8 * h / w, 0.0)
+    P.width, P.height, P.left_method, P.right_method, P.train_probability = w, h, 1, 1, 0.25
+    P.seed = 2024
+    buf.reset()
+    nrc.path_trace(ds, bvh, P, buf)
+    cap = buf.eval_capacity
+    outs = []
+    for scene in (ds, dt):
+        inputs = torch.full((cap, 14), -1.0, dtype=torch.float32, device="cuda")
+        dst = torch.zeros(cap, dtype=torch.int32, device="cuda")
+        nrc.unpack_eval(scene, buf.eval, buf.eval_count, inputs, dst, capacity=cap)
+        tr = [torch.full((16384, 20), -1.0, dtype=torch.float32, device="cuda") for _ in range(4)]
+        for b in range(4):
+            nrc.unpack_train(scene, buf.train[b], buf.train_counts[b], tr[b], capacity=16384)
+        outs.append((host(inputs), host(dst), [host(t) for t in tr]))
+    n = int(host(buf.eval_count)[0])
+    assert n > 0
+    np.testing.assert_array_equal(outs[0][0], outs[1][0])
+    np.testing.assert_array_equal(outs[0][1], outs[1][1])
+    for a, b in zip(outs[0][2], outs[1][2]):
+        np.testing.assert_array_equal(a, b)
+    assert np.all(outs[1][0][n:] == -1.0)  # nothing past the count
+    bvh.close()
