@@ -1,7 +1,7 @@
-// Scene unpack shared by the unpack kernel (nrc_unpack.cu) and the query
-// kernel's packed-record form (nrc_infer.cu): UnpackNRCInput
+// Per-record arithmetic of the unpack kernels (nrc_unpack.cu): UnpackNRCInput
 // (shader/src/NRCRecord.glsl:97-125) over the scene buffers
-// (shader/src/Scene.glsl:50-71).
+// (shader/src/Scene.glsl:50-71) or over the scene's gather tables
+// (nrc_scene_prepare), which hold the same values laid out for the gathers.
 //
 // Per record: the primitive's three vertices through the instance transform
 // (vec4(p, 1) * mat3x4), the face normal normalize(cross(v1 - v0, v2 - v0)),
