@@ -643,14 +643,13 @@ int frame_overlapped(nrc_context* c, const nrc_input* eval_in, const uint32_t* d
   // as all training CTAs run (programmatic dependence, no wait for the
   // training's end): plan.query_ctas of its CTAs start beside the training and
   // the others on the training's SMs as it finishes.
-  // The staged weights are copied into use_weights by the query's last CTA,
-  // after its wait for the training grid (or, without a query, by the
-  // training's last CTA), so no copy waits in the stream between frames.
+  // The staged weights are copied into use_weights by the query CTA that is
+  // the last to load its weights, after its wait for the training grid (or,
+  // without a query, by the training's last CTA), so no copy waits in the
+  // stream between frames.
   nrc::FrameJoin join = {};
-  join.counter = c->tiles + 2;
   join.src = reinterpret_cast<const uint4*>(c->use_next);
   join.dst = reinterpret_cast<uint4*>(c->use16);
-  join.arrivals = 1u;
   p.use16 = c->use_next;
   if (eval_capacity == 0) p.join = join;
   e = nrc::launch_train(p, &c->map_w16, static_cast<int>(plan.train_ctas), st);

@@ -215,6 +215,25 @@ __device__ __forceinline__ void infer_body(const InferLaunch<N>& L) {
   bool ok = true;
   uint32_t ph_d = 0, ph_a = 0;
   if (issuer) ok = warp_all(mbar_wait(w_full, 0, kWaitLimitNs));  // before this slot's first MMA
+  // The overlapped frame: once every CTA has its weights in shared memory,
+  // use_weights is read no more; the CTA that loaded last waits for the
+  // training grid and copies the staged weights in (its first slot starts
+  // late, off the frame's end).
+  if (dyn && J.join.src != nullptr && warp == 0) {
+    uint32_t last_load = 0;
+    if (lane == 0) {
+      __threadfence();
+      last_load = atomicAdd(J.tiles + 2, 1u) == gridDim.x - 1 ? 1u : 0u;
+      if (last_load != 0u) {
+        reinterpret_cast<volatile uint32_t*>(J.tiles)[2] = 0u;  // for the next launch
+        __threadfence();
+      }
+    }
+    if (__shfl_sync(0xffffffffu, last_load, 0) != 0u) {
+      griddep_wait();  // the training grid has completed: its staged weights are final
+      join_copy(J.join, lane, 32);
+    }
+  }
   for (uint32_t it = 0; ok; ++it) {
     uint32_t tile = tile_of(it);
     if (dyn) {  // the slot's next tile (or the end mark) arrives with its record stage
@@ -387,15 +406,13 @@ __device__ __forceinline__ void infer_body(const InferLaunch<N>& L) {
       }
     }
     __syncthreads();
-    if (*last != 0u) {
-      // A launch that started without waiting for the preceding grid (the
-      // overlapped frame's training) completes only after it: the last CTA
-      // waits for that grid here, so that whatever follows this query in the
-      // stream also follows the training. The training is resident (this grid
-      // launched once all of its CTAs ran) and never waits for the query.
-      if (J.no_wait) griddep_wait();
-      if (J.join.counter != nullptr) frame_join(J.join, last + 1);
-    }
+    // A launch that started without waiting for the preceding grid (the
+    // overlapped frame's training) completes only after it, so that whatever
+    // follows this query in the stream also follows the training: the CTA that
+    // copied the staged weights has waited for that grid, else the last CTA
+    // out waits here. The training is resident (this grid launched once all of
+    // its CTAs ran) and never waits for the query.
+    if (*last != 0u && J.no_wait && J.join.src == nullptr) griddep_wait();
   }
 }
 

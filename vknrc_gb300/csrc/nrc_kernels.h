@@ -57,52 +57,35 @@ cudaError_t launch_infer(const void* input, bool encoded, const uint32_t* d_coun
                          cudaStream_t stream, bool bf16 = false);
 
 // The overlapped frame's copy of the staged rendering weights src -> dst
-// (kParams 16-bit words: 2,584 x 16 bytes), made by the last CTA out of the
-// kernel that ends the frame (the query, after its wait for the training grid;
-// the training when the frame has no query). Each arrival adds one to
-// *counter, the one that brings it to `arrivals` copies and returns the
-// counter to zero. counter null: no copy.
+// (kParams 16-bit words: 2,584 x 16 bytes), made once the training grid has
+// completed and no query CTA reads dst any more: by the query CTA that is the
+// last to have its weights in shared memory (after its wait for the training
+// grid), or, when the frame has no query, by the training's last CTA. src
+// null: no copy.
 struct FrameJoin {
-  uint32_t* counter;
   const uint4* src;
   uint4* dst;
-  uint32_t arrivals;
 };
 
 constexpr uint32_t kJoinChunks = 2584;  // 16-byte chunks of the 20,672 16-bit weights
 
 #ifdef __CUDACC__
-// FrameJoin, called by every thread of its kernel's last CTA (after the
-// kernel's writes are complete and fenced by the CTA that made them).
-// `slot`: a shared-memory word for the CTA's decision.
-__device__ __forceinline__ void frame_join(const FrameJoin& j, uint32_t* slot) {
-  if (threadIdx.x == 0) {
-    __threadfence();
-    *slot = atomicAdd(j.counter, 1u) == j.arrivals - 1 ? 1u : 0u;
-    __threadfence();
-  }
-  __syncthreads();
-  if (*slot != 0u) {
-    // all of a thread's loads (from L2: other CTAs wrote the source) are in
-    // flight before its stores, so the copy costs about one memory round trip
-    constexpr uint32_t kUnroll = 8;
-    for (uint32_t base = 0; base < kJoinChunks; base += kUnroll * blockDim.x) {
-      uint4 v[kUnroll];
+// The copy by `nthreads` threads of the calling CTA (t: this thread's index
+// among them); each thread's loads (from L2: other CTAs wrote the source) are
+// in flight before its stores.
+__device__ __forceinline__ void join_copy(const FrameJoin& j, uint32_t t, uint32_t nthreads) {
+  constexpr uint32_t kUnroll = 8;
+  for (uint32_t base = 0; base < kJoinChunks; base += kUnroll * nthreads) {
+    uint4 v[kUnroll];
 #pragma unroll
-      for (uint32_t u = 0; u < kUnroll; ++u) {
-        const uint32_t i = base + u * blockDim.x + threadIdx.x;
-        if (i < kJoinChunks) v[u] = __ldcg(j.src + i);
-      }
-#pragma unroll
-      for (uint32_t u = 0; u < kUnroll; ++u) {
-        const uint32_t i = base + u * blockDim.x + threadIdx.x;
-        if (i < kJoinChunks) j.dst[i] = v[u];
-      }
+    for (uint32_t u = 0; u < kUnroll; ++u) {
+      const uint32_t i = base + u * nthreads + t;
+      if (i < kJoinChunks) v[u] = __ldcg(j.src + i);
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      __threadfence();
-      *reinterpret_cast<volatile uint32_t*>(j.counter) = 0u;
+#pragma unroll
+    for (uint32_t u = 0; u < kUnroll; ++u) {
+      const uint32_t i = base + u * nthreads + t;
+      if (i < kJoinChunks) j.dst[i] = v[u];
     }
   }
 }
@@ -118,14 +101,15 @@ struct InferJob {
   QueryOut q;
   const Fp8State* fp8;  // the FP8 query's scales (fp8 launches only)
   // Dynamic tiles (single-cache record queries): tiles[0] hands out the next
-  // tile, tiles[1] counts exiting CTAs (both zero between launches; the last
-  // CTA resets them). Null: each CTA takes a fixed share of the tiles.
+  // tile, tiles[1] counts exiting CTAs, tiles[2] (with a join) CTAs whose
+  // weights have landed (all zero between launches; the last CTA of each
+  // count resets it). Null: each CTA takes a fixed share of the tiles.
   uint32_t* tiles;
   // 1: start without waiting for the preceding grid in the stream (the
   // overlapped frame's query, launched behind the training it runs beside,
   // reads nothing that training writes).
   uint32_t no_wait;
-  FrameJoin join;  // dynamic tiles only: joined by the last CTA out
+  FrameJoin join;  // dynamic tiles only: the staged weights copied by the CTA that loads its weights last
 };
 
 // Kernel parameters of a query launch over up to N caches; CTAs
@@ -198,7 +182,7 @@ struct TrainParams {
   uint32_t* err;
   int bf16;          // weights and operands in bf16 (host side: selects the kernel)
   uint32_t* amax;    // Fp8State::amax_x of a cache with fp8 inference, or null
-  FrameJoin join;    // joined by the last CTA out
+  FrameJoin join;    // the staged weights copied by the last CTA out (a frame without a query)
 };
 
 // One cache's share of a training launch: its weight tensor map and parameters.

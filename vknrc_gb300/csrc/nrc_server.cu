@@ -345,24 +345,37 @@ int loop_kick(nrc_server* S) {
 
 // Every request written to the ring completes and the loop's launches end (so
 // that device memory can be allocated or freed: both may wait for the device).
+// A request still in the ring once the launches have ended (a launch that
+// failed, or the two sides' flags crossed) gets a launch of its own first.
 int loop_pause(nrc_server* S) {
   S->shared->stop = 1u;
   std::atomic_thread_fence(std::memory_order_seq_cst);
   // bounded: the loop ends once the requests written have run (each kernel's
   // own waits are bounded too)
   const int64_t t0 = now_ns();
-  cudaError_t e = cudaStreamQuery(S->loop_stream);
-  while (e == cudaErrorNotReady && now_ns() - t0 < 60000000000ll) {
+  for (;;) {
+    const cudaError_t e = cudaStreamQuery(S->loop_stream);
+    if (e == cudaSuccess) {
+      std::atomic_thread_fence(std::memory_order_seq_cst);
+      // no launch runs: every request the loop took from the ring has run
+      if (S->shared->tail == S->shared->head) break;
+      S->shared->active = 0u;
+      if (loop_kick(S) != NRC_OK) return NRC_ERROR_CUDA;  // the requests stay in the ring
+    } else if (e != cudaErrorNotReady) {
+      return NRC_ERROR_CUDA;
+    }
+    if (now_ns() - t0 > 60000000000ll) return NRC_ERROR_DEVICE_TIMEOUT;  // still running: left as it is
     std::this_thread::sleep_for(std::chrono::microseconds(50));
-    e = cudaStreamQuery(S->loop_stream);
   }
-  if (e == cudaErrorNotReady) return NRC_ERROR_DEVICE_TIMEOUT;  // still running: left as it is
   S->shared->stop = 0u;
-  return e == cudaSuccess ? NRC_OK : NRC_ERROR_CUDA;
+  return NRC_OK;
 }
 
 // Collects the completions the loop has published.
 void loop_poll(nrc_server* S) {
+  // requests the scheduler completed without running them (no valid slot): never
+  // expected, since submit checks the session first
+  if (S->shared->dropped != 0ull) S->worker_status = NRC_ERROR_INVALID_ARGUMENT;
   for (auto it = S->outstanding.begin(); it != S->outstanding.end();) {
     const uint64_t t = *it;
     const uint32_t k = static_cast<uint32_t>(t & (nrc::kLoopRing - 1));
@@ -593,12 +606,15 @@ int nrc_server_close_session(nrc_server* S, uint32_t id) {
   if (S->device_loop) {
     std::lock_guard<std::mutex> lk(S->m);
     if (!valid_session(S, id)) return NRC_ERROR_INVALID_ARGUMENT;
-    int st = loop_pause(S);  // every request written, this session's included, completes
+    // every request written, this session's included, completes; if the loop
+    // could not be paused its kernels may still read the session: it stays open
+    const int paused = loop_pause(S);
+    if (paused != NRC_OK) return paused;
     loop_poll(S);
+    const int st = loop_write_slots(S, id, nullptr);
     s = std::move(S->sessions[id]);
     S->sessions[id] = Session{};
     S->bytes_in_use -= s.bytes;
-    if (st == NRC_OK) st = loop_write_slots(S, id, nullptr);
     nrc_destroy(s.ctx);
     cudaFree(s.block);
     return st;

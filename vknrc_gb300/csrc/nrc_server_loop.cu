@@ -109,10 +109,20 @@ __global__ void __launch_bounds__(32) loop_schedule_kernel(LoopShared* S, LoopDe
     bool full = false;
     for (uint32_t i = 0; i < npend; ++i) {
       const LoopEntry e = D->pend[i];
-      const uint32_t s = e.session < kLoopMaxSessions ? e.session : 0u;
+      const bool in_range = e.session < kLoopMaxSessions && e.slot < kLoopMaxSlots;
+      const uint32_t k = in_range ? e.session * kLoopMaxSlots + e.slot : 0u;
+      if (!in_range || __ldcg(&slots[k].valid) == 0u) {
+        // a request for no open session's slot (the host submits none): its
+        // jobs are never launched; it completes at once and is counted
+        S->done_ns[e.ticket & (kLoopRing - 1)] = globaltimer_ns();
+        __threadfence_system();
+        S->done_ticket[e.ticket & (kLoopRing - 1)] = e.ticket;
+        S->dropped = S->dropped + 1ull;
+        continue;
+      }
+      const uint32_t s = e.session;
       const bool seen = (busy[s >> 5] >> (s & 31u)) & 1u;
       busy[s >> 5] |= 1u << (s & 31u);
-      const uint32_t k = s * kLoopMaxSlots + (e.slot < kLoopMaxSlots ? e.slot : 0u);
       bool take = false;
       if (!seen && !full) {
         const uint32_t tc = __ldcg(&slots[k].train_ctas);

@@ -38,7 +38,8 @@ struct LoopShared {
   volatile unsigned long long batches, batched_requests;  // device: launched batches and their requests
   volatile unsigned long long calib_ns;                   // device clock at the calibration's go
   volatile unsigned long long idle_polls;                 // device: scheduler passes that found no request
-  unsigned long long pad3[4];
+  volatile unsigned long long dropped;                    // device: requests for no valid slot, completed unrun
+  unsigned long long pad3[3];
   LoopEntry ring[kLoopRing];
   volatile unsigned long long done_ticket[kLoopRing];  // device: completed ticket t at t % kLoopRing
   volatile unsigned long long done_ns[kLoopRing];      // device: its completion time (%globaltimer)

@@ -723,9 +723,9 @@ __device__ __forceinline__ void train_body(const TrainLaunch<N>& L) {
   }
   // the overlapped frame: the group's last CTA out joins the frame (every CTA's
   // weight writes are complete and fenced by now)
-  if (P.join.counter != nullptr) {
+  if (P.join.src != nullptr) {
     __syncthreads();
-    if (B->sync_ok != 0u) frame_join(P.join, &B->tmem_base);
+    if (B->sync_ok != 0u) join_copy(P.join, threadIdx.x, blockDim.x);
   }
 }
 
