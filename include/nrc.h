@@ -245,10 +245,11 @@ typedef struct nrc_frame_plan {
 /* nrc_frame with the query and the training run at the same time. The
  * reference's frame reads use_weights in its query and writes them in its last
  * training step (src/rg/NRCRenderGraph.cpp:52, :77); here the training writes
- * them into a second buffer of the context, copied into use_weights (41 KB) by
- * the query's last CTA once both kernels are done. The
- * query therefore reads exactly the weights it reads in nrc_frame, and
- * use_weights change only at the end of the call, as there. The training runs
+ * them into a second buffer of the context, copied into use_weights (41 KB)
+ * once the training has completed and every query CTA has loaded the previous
+ * ones. The query therefore reads exactly the weights it reads in nrc_frame,
+ * and work that follows the call in the stream sees the new ones, as there
+ * (no other work may read use_weights while the call runs). The training runs
  * with plan->train_ctas CTAs, so its gradient sums are grouped as
  * nrc_train_many with that count groups them. It is launched first on
  * `stream`; the query follows as a dependent launch that starts once every
