@@ -1,8 +1,9 @@
 """The overlapped frame (nrc_frame_overlapped): the query of a frame and its
 four training steps at the same time (the training on its CTAs, the query's
 tiles handed out by a counter to CTAs beside it and, as it finishes, on its
-SMs), the training's new rendering weights staged and copied in by the kernel
-that finishes last, and the autotuner that picks the split.
+SMs), the training's new rendering weights staged and copied in once the
+training has completed and every query CTA has loaded the previous ones, and
+the autotuner that picks the split.
 
 The query reads the same use_weights as in the sequential frame, so its
 answers are the same bit for bit; the training with a group of train_ctas
@@ -108,9 +109,9 @@ def test_overlapped_frame_graph_replays(cuda):
 @pytest.mark.parametrize("queries", ["none", "zero"])
 def test_overlapped_frame_without_queries_publishes_the_weights(cuda, queries):
     """No query launched (capacity 0: the training's last CTA copies the staged
-    rendering weights) or a query with no records (the query's last CTA copies
-    them after its wait for the training): use_weights match the grouped
-    training's either way."""
+    rendering weights) or a query with no records (the query CTA that loads its
+    weights last copies them after its wait for the training): use_weights
+    match the grouped training's either way."""
     import torch
 
     from vknrc_gb300 import Cache, nrc
