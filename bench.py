@@ -12,7 +12,7 @@ inputs are cold in L2).
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
 Prints one JSON line. With --gpus N > 1 (under torchrun) every rank runs an
-independent replica (the path has no data-path exchange on one box).
+independent replica (the path has no data-path exchange between GPUs).
 """
 from __future__ import annotations
 

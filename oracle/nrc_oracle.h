@@ -2,8 +2,9 @@
  * CPU oracle for the neural-radiance-cache hot path — TEST INFRASTRUCTURE ONLY.
  *
  * A plain-C restatement of the reference's shader math, used by tests/, by
- * __graft_entry__.smoke() and by bench.py's CPU-baseline leg as the checker. The
- * product (libnrc.so) never links, loads or calls anything in this directory.
+ * __graft_entry__.smoke() and by bench.py's CPU-baseline leg to check the GPU
+ * path against. The product (libnrc.so) never links, loads or calls anything in
+ * this directory.
  *
  * Parity status:
  *   - Record encoding: pinned against the reference's own NRCRecord.glsl compiled

@@ -2,8 +2,8 @@
  * CPU oracle of the record producer (the path tracer) — TEST INFRASTRUCTURE ONLY.
  *
  * A plain-C restatement of shader/src/path_tracer.comp (with CookTorranceBRDF.glsl,
- * Sample.glsl, RNG.glsl and Scene.glsl) used by tests/ as the checker of the GPU
- * tracer. GLSL leaves the order of floating-point operations and the accuracy of
+ * Sample.glsl, RNG.glsl and Scene.glsl) used by tests/ to check the GPU tracer
+ * against. GLSL leaves the order of floating-point operations and the accuracy of
  * its transcendental functions to the implementation; this restatement fixes one
  * choice: every expression is evaluated left to right with no contraction (built
  * with -ffp-contract=off), fused multiply-adds appear only as explicit fmaf, and

@@ -1,7 +1,7 @@
 """ctypes wrapper of the CPU oracle (oracle/_build/liboracle.so) — TEST INFRASTRUCTURE.
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import this
-module, and only as the checker. The product library never uses it.
+module, and only to check the GPU path against. The product library never uses it.
 """
 from __future__ import annotations
 

@@ -8,7 +8,8 @@
 # Sources are read in place from the reference tree (REF_DIR; default
 # /root/reference, else a reference tree mounted at baseline/_ref); nothing is
 # copied into the repository. Outputs go only to oracle/_ref/. Exits 0 without
-# building when no reference tree is found (the GPU machine does not have it).
+# building when no reference tree is found (a machine without the reference
+# sources).
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
 if [ -z "${REF_DIR:-}" ]; then
