@@ -135,17 +135,13 @@ __device__ __forceinline__ uint32_t relu_mask_f16x2(uint32_t g, uint32_t a) {
   return g & __hgt2_mask(a2, __float2half2_rn(0.0f)) & ~__hneu2_mask(g2, g2);
 }
 
-// The same on bf16 pairs, on the bit patterns: a half is kept where the
-// activation is greater than zero (sign clear, non-zero, not NaN) and the
-// gradient is not NaN.
+// The same on bf16 pairs: a half is kept where the activation is greater than
+// zero (IEEE compare: positive, non-zero, not NaN; subnormals count) and the
+// gradient is not NaN, two packed compares as for fp16.
 __device__ __forceinline__ uint32_t relu_mask_bf16x2(uint32_t g, uint32_t a) {
-  uint32_t keep = 0;
-#pragma unroll
-  for (int h = 0; h < 32; h += 16) {
-    const uint32_t ah = (a >> h) & 0xFFFFu, gh = (g >> h) & 0xFFFFu;
-    if (ah != 0u && ah <= 0x7F80u && (gh & 0x7FFFu) <= 0x7F80u) keep |= 0xFFFFu << h;
-  }
-  return g & keep;
+  const __nv_bfloat162 g2 = *reinterpret_cast<const __nv_bfloat162*>(&g);
+  const __nv_bfloat162 a2 = *reinterpret_cast<const __nv_bfloat162*>(&a);
+  return g & __hgt2_mask(a2, __float2bfloat162_rn(0.0f)) & ~__hneu2_mask(g2, g2);
 }
 
 template <bool kBF16>
