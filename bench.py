@@ -634,6 +634,8 @@ def fp8_leg(evals, trains, eval_cnt, train_cnt, steps=500):
         if c.error() != 0:
             raise RuntimeError("device error in the fp8 leg")
     return {"infer_ms": q_s * 1e3, "queries_per_s": Q / q_s, "frame_ms": f_s * 1e3, "steps": steps,
+            "frame_schedule": "sequential: nrc_infer_fp8 on every SM, then nrc_train_batches on every SM "
+                              "(the overlapped frame's query is the 16-bit one)",
             "accuracy": "tests/test_gpu_fp8.py: query error against the FP64 oracle"}
 
 
