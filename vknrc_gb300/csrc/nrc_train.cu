@@ -192,8 +192,9 @@ __device__ __forceinline__ bool grid_sync(uint32_t* counter, uint32_t target, ui
   __syncthreads();
   if (threadIdx.x == 0) {
     fence_proxy_async_global();
-    __threadfence();
-    atomicAdd(counter, 1u);
+    // the arrival releases the CTA's writes (ordered before it by the CTA
+    // barrier above); the polling load acquires the other CTAs'
+    asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(counter) : "memory");
     bool ok = true;
     if (ld_acquire_gpu(counter) < target) {
       const uint64_t t0 = globaltimer_ns();
@@ -205,7 +206,6 @@ __device__ __forceinline__ bool grid_sync(uint32_t* counter, uint32_t target, ui
         __nanosleep(32);
       }
     }
-    __threadfence();
     fence_proxy_async_global();
     *sync_ok = ok ? 1u : 0u;
   }
