@@ -469,7 +469,10 @@ NRC_API int nrc_server_create(const nrc_server_config* cfg, nrc_server** out);
 /* Finishes every submitted request, stops the worker, closes all sessions. */
 NRC_API int nrc_server_destroy(nrc_server* srv);
 NRC_API int nrc_server_open_session(nrc_server* srv, const nrc_session_desc* desc, uint32_t* session);
-/* Waits for the session's requests to finish, then frees its memory. */
+/* Waits for the session's requests to finish, then frees its memory. With
+ * the device loop every request written so far completes first; if the loop
+ * cannot be paused (NRC_ERROR_DEVICE_TIMEOUT after 60 s, or a CUDA error) the
+ * session stays open and the status is returned. */
 NRC_API int nrc_server_close_session(nrc_server* srv, uint32_t session);
 NRC_API int nrc_server_frame_buffers(nrc_server* srv, uint32_t session, uint32_t slot, nrc_frame_buffers* out);
 /* The session's cache, for nrc_get_weights / nrc_get_optimizer and the like
