@@ -201,10 +201,15 @@ __device__ __forceinline__ void encode_input(const float (&r)[kInFloats], uint32
 
 // The same features in E4M3 for the FP8 query: feature k, multiplied by inv_s
 // (448 / the features' absmax scale), rounded to nearest even and saturated,
-// in byte k % 4 of word k / 4. Split like the 16-bit encode at feature 32:
-// half 0 gives words 0..7 (features 0..31), half 1 words 8..15.
+// in byte k % 4 of word k / 4 (the multiplies two per packed f32x2
+// instruction, each rounded as one __fmul_rn). Split like the 16-bit encode at
+// feature 32: half 0 gives words 0..7 (features 0..31), half 1 words 8..15.
 __device__ __forceinline__ uint32_t e4m3_q4(float a, float b, float c, float d, float inv_s) {
-  return pack4_e4m3(__fmul_rn(a, inv_s), __fmul_rn(b, inv_s), __fmul_rn(c, inv_s), __fmul_rn(d, inv_s));
+  const uint64_t s2 = f32x2(inv_s, inv_s);
+  float a0, a1, a2, a3;
+  f32x2_split(mul_x2(f32x2(a, b), s2), a0, a1);
+  f32x2_split(mul_x2(f32x2(c, d), s2), a2, a3);
+  return pack4_e4m3(a0, a1, a2, a3);
 }
 // triangle-wave frequency k of coordinate p (the two forms agree; see enc_tri_h)
 __device__ __forceinline__ float enc_tri_k(float p, int k) {

@@ -336,22 +336,20 @@ __device__ __forceinline__ void infer_body(const InferLaunch<N>& L) {
       ph_d ^= 1u;
       tc_fence_after();
       if (kF8 && l < 5) {
-        uint32_t v[32], p[16];
+        // all 64 accumulator columns in one load and one wait, packed in place
+        // (word j from values 4j..4j+3, j <= 4j); the scale multiplies two
+        // lanes per instruction (IEEE-rounded like __fmul_rn each)
+        uint32_t v[64];
+        tmem_ld64(d_col + lane_off, v);
+        const uint64_t c2 = f32x2(cl, cl);
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          tmem_ld32(d_col + lane_off + 32 * h, v);
-          // the scale multiplies two lanes per instruction (IEEE-rounded like
-          // __fmul_rn each; 3% faster query than one multiply per value)
-#pragma unroll
-          for (int j = 0; j < 8; ++j) {
-            const uint64_t c2 = f32x2(cl, cl);
-            float a0, a1, a2, a3;
-            f32x2_split(mul_x2(f32x2(__uint_as_float(v[4 * j]), __uint_as_float(v[4 * j + 1])), c2), a0, a1);
-            f32x2_split(mul_x2(f32x2(__uint_as_float(v[4 * j + 2]), __uint_as_float(v[4 * j + 3])), c2), a2, a3);
-            p[8 * h + j] = pack4_relu_e4m3(a0, a1, a2, a3);
-          }
+        for (int j = 0; j < 16; ++j) {
+          float a0, a1, a2, a3;
+          f32x2_split(mul_x2(f32x2(__uint_as_float(v[4 * j]), __uint_as_float(v[4 * j + 1])), c2), a0, a1);
+          f32x2_split(mul_x2(f32x2(__uint_as_float(v[4 * j + 2]), __uint_as_float(v[4 * j + 3])), c2), a2, a3);
+          v[j] = pack4_relu_e4m3(a0, a1, a2, a3);
         }
-        tmem_st16(a_col + lane_off, p);
+        tmem_st16(a_col + lane_off, *reinterpret_cast<uint32_t(*)[16]>(v));
         tc_fence_before();
         arrive_warp(&B.a_ready);
       } else if (l < 5) {
